@@ -1,0 +1,274 @@
+/*
+ * sgl.h — C ABI of the GB300 renderer for swegl scenes.
+ *
+ * The library keeps scenes resident in device memory and renders them with
+ * hand-written sm_103a kernels.  Every entry point returns an sgl_status
+ * (0 = success, negative = error); the text of the last error of a context is
+ * available from sgl_last_error().  No entry point aborts or traps.
+ *
+ * Reference interfaces this ABI replaces (paths inside gbizzotto/swegl):
+ *   swegl::render(scene_t&, T&... viewports)      swegl/render/renderer.hpp:27-34
+ *   swegl::_render(scene_t&, viewport_t&)         src/render/renderer.cpp:77-235
+ *   scene_t / node_t / primitive_t / mesh_vertex_t  swegl/data/model.hpp:20-178
+ *   material_t / point_source_light               swegl/data/model.hpp:74-87
+ *   texture_t / mipmap_t                          swegl/data/texture.hpp:12-38
+ *   viewport_t(x, y, w, h, surface, shader, layers) swegl/render/viewport.hpp:27-62
+ *   camera_t (view / projection matrices, centre) swegl/projection/camera.hpp:10-24
+ *   pixel_shader_light_and_texture<pixel_shader_lights_phong,
+ *       pixel_shader_texture_bilinear>            swegl/render/pixel_shaders.hpp:121-179
+ *   post_shader_t::shade(viewport_t&)             swegl/render/post_shaders.hpp:33-47
+ */
+#ifndef SGL_H
+#define SGL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SGL_API __attribute__((visibility("default")))
+#else
+#define SGL_API
+#endif
+
+typedef int sgl_status;
+
+enum {
+    SGL_OK              = 0,
+    SGL_ERR_INVALID     = -1,  /* bad argument (null pointer, bad size, bad index)      */
+    SGL_ERR_OOM         = -2,  /* device or host allocation failed                      */
+    SGL_ERR_CUDA        = -3,  /* a CUDA runtime call failed                            */
+    SGL_ERR_NOT_FOUND   = -4,  /* unknown scene id / ticket                             */
+    SGL_ERR_BUDGET      = -5,  /* request can never fit the serving memory budget       */
+    SGL_ERR_TIMEOUT     = -6,  /* a bounded wait ran out                                */
+    SGL_ERR_NO_DEVICE   = -7,  /* no CUDA device                                        */
+    SGL_ERR_UNSUPPORTED = -8,  /* feature the GPU path does not implement               */
+    SGL_ERR_BUSY        = -9   /* result not ready yet (polling)                        */
+};
+
+/* primitive_t::index_mode_t (swegl/data/model.hpp:33-42); only the triangle
+ * modes are rasterised by the reference. */
+enum {
+    SGL_TRIANGLES      = 4,
+    SGL_TRIANGLE_STRIP = 5,
+    SGL_TRIANGLE_FAN   = 6
+};
+
+/* ---------------------------------------------------------------- scenes -- */
+
+/* node_t (swegl/data/model.hpp:50-71): local matrix = scale(rotation, scale)
+ * followed by translate(translation); world = parent_world * local. */
+typedef struct sgl_node_desc {
+    float scale[3];
+    float rotation[16];   /* row-major 4x4, matrix44_t layout */
+    float translation[3];
+    int   parent;         /* index of the parent node, -1 for a root node */
+} sgl_node_desc;
+
+/* primitive_t (swegl/data/model.hpp:31-48).  Vertices are owned by the
+ * primitive: indices are local to [vertex_offset, vertex_offset+vertex_count). */
+typedef struct sgl_primitive_desc {
+    int      node;
+    int      mode;          /* SGL_TRIANGLES / SGL_TRIANGLE_STRIP / SGL_TRIANGLE_FAN */
+    int      material;      /* index into materials; -1 selects default_material */
+    uint32_t vertex_offset;
+    uint32_t vertex_count;
+    uint32_t index_offset;
+    uint32_t index_count;
+} sgl_primitive_desc;
+
+/* material_t (swegl/data/model.hpp:80-87).  `shininess` is the point-light
+ * specular exponent; the reference hard-codes 32 (src/render/pixel_shaders.cpp:192). */
+typedef struct sgl_material_desc {
+    uint32_t color;         /* 0xAARRGGBB, used when texture == -1 */
+    int      texture;       /* index into textures, -1 = none */
+    int      double_sided;
+    int      shininess;     /* integer exponent, 1..1024 */
+} sgl_material_desc;
+
+/* texture_t mip level 0 (swegl/data/texture.hpp:12-27): 0xAARRGGBB texels. */
+typedef struct sgl_texture_desc {
+    const uint32_t *texels;
+    int             width;
+    int             height;
+} sgl_texture_desc;
+
+/* point_source_light (swegl/data/model.hpp:74-78) */
+typedef struct sgl_point_light {
+    float position[3];
+    float intensity;
+} sgl_point_light;
+
+/* scene_t (swegl/data/model.hpp:128-178), flattened: vertex attributes are
+ * structure-of-arrays (positions xyz, normals xyz, uvs uv). */
+typedef struct sgl_scene_desc {
+    int                        n_nodes;
+    const sgl_node_desc       *nodes;
+    int                        n_primitives;
+    const sgl_primitive_desc  *primitives;
+    uint32_t                   n_vertices;
+    const float               *positions;   /* 3 * n_vertices */
+    const float               *normals;     /* 3 * n_vertices */
+    const float               *uvs;         /* 2 * n_vertices */
+    uint32_t                   n_indices;
+    const uint32_t            *indices;
+    int                        n_materials;
+    const sgl_material_desc   *materials;
+    int                        n_textures;
+    const sgl_texture_desc    *textures;
+    int                        n_point_lights;
+    const sgl_point_light     *point_lights;
+    float                      ambient;          /* scene_t::ambient_light_intensity */
+    float                      sun_direction[3]; /* scene_t::sun_direction (normalised) */
+    float                      sun_intensity;    /* scene_t::sun_intensity */
+    sgl_material_desc          default_material; /* scene_t::default_material */
+} sgl_scene_desc;
+
+/* ----------------------------------------------------------------- views -- */
+
+/* Depth-of-field gather (replaces post_shader_depth_box,
+ * swegl/render/post_shaders.hpp:51-132, whose own output is not usable). */
+typedef struct sgl_dof_desc {
+    int   enabled;
+    float focus;        /* view-space focus distance */
+    float aperture;     /* lens aperture in world units */
+    float max_radius;   /* circle of confusion clamp, pixels */
+    float px_scale;     /* pixels per world unit at unit distance; 0 = P11*h/2 */
+} sgl_dof_desc;
+
+/* viewport_t + camera_t (swegl/render/viewport.hpp:27-62,
+ * swegl/projection/camera.hpp:10-24). */
+typedef struct sgl_view {
+    int          x, y, w, h;        /* viewport rectangle inside the target surface */
+    float        view[16];          /* camera_t::m_viewmatrix, row-major */
+    float        proj[16];          /* camera_t::m_projectionmatrix, row-major */
+    float        camera_pos[3];     /* camera_t::m_center */
+    sgl_dof_desc dof;
+} sgl_view;
+
+/* The SDL_Surface fields the reference writes (pixels, pitch, w, h with
+ * BytesPerPixel = 4) plus viewport_t::m_zbuffer (w*h floats of the view). */
+typedef struct sgl_target {
+    void  *pixels;      /* BGRA8 surface */
+    int    pitch;       /* bytes per surface row */
+    int    width;       /* surface width in pixels */
+    int    height;      /* surface height in pixels */
+    float *zbuffer;     /* view w*h depth values, may be NULL */
+} sgl_target;
+
+/* Per-frame counters filled by sgl_render when `stats` is non-NULL. */
+typedef struct sgl_frame_stats {
+    uint64_t triangles;       /* triangles in the scene */
+    uint64_t drawn_triangles; /* (sub-)triangles that reached scanline setup */
+    uint64_t fragments;       /* covered (triangle, pixel) pairs of all spans */
+    uint64_t pixels;          /* viewport pixels written */
+    uint32_t kernel_launches; /* kernels this call launched */
+    uint32_t reserved;
+} sgl_frame_stats;
+
+/* ----------------------------------------------------------- entry points -- */
+
+typedef struct sgl_ctx sgl_ctx;
+
+/* Create a context on CUDA `device`.  One context per host thread, or
+ * external locking: a context is not re-entrant. */
+SGL_API sgl_status sgl_create(sgl_ctx **out, int device);
+SGL_API void       sgl_destroy(sgl_ctx *ctx);
+SGL_API const char *sgl_last_error(const sgl_ctx *ctx);
+SGL_API const char *sgl_status_string(sgl_status status);
+SGL_API int        sgl_version(void);
+
+/* Copy a scene into device memory (replaces the per-frame scene_t walk of
+ * renderer.cpp:83-231).  Host arrays may be freed after the call. */
+SGL_API sgl_status sgl_scene_upload(sgl_ctx *ctx, const sgl_scene_desc *desc, int *scene_id);
+SGL_API sgl_status sgl_scene_release(sgl_ctx *ctx, int scene_id);
+/* Replace node transforms (scene_t::animate, model.hpp:146-177). */
+SGL_API sgl_status sgl_scene_set_nodes(sgl_ctx *ctx, int scene_id, const sgl_node_desc *nodes, int n_nodes);
+/* Replace the lights (scene_t ambient / sun / point_source_lights). */
+SGL_API sgl_status sgl_scene_set_lights(sgl_ctx *ctx, int scene_id, float ambient,
+                                        const float sun_direction[3], float sun_intensity,
+                                        const sgl_point_light *lights, int n_lights);
+SGL_API sgl_status sgl_scene_info(sgl_ctx *ctx, int scene_id, uint64_t *n_triangles, uint64_t *n_vertices,
+                                  uint64_t *device_bytes);
+
+/* swegl::render(scene, vp...) (renderer.hpp:27-34) for the
+ * Phong + bilinear shader: world transform once, then each view in order.
+ * `targets[i]` receives view i.  When `device_buffers` is 0 the target
+ * pointers are host memory and the call copies in and out (synchronous);
+ * when 1 they are device memory and the call is asynchronous on `stream`
+ * (a cudaStream_t, NULL = legacy default stream). */
+SGL_API sgl_status sgl_render(sgl_ctx *ctx, int scene_id, const sgl_view *views, const sgl_target *targets,
+                              int n_views, int device_buffers, void *stream, sgl_frame_stats *stats);
+
+/* Debug variant of one view: writes the per-pixel winner slot
+ * (2 * draw-order triangle index + clip sub-triangle, 0xFFFFFFFF = none) and
+ * the per-slot "reached scanline setup" flags, used to check depth-test
+ * winners bit-exactly.  Host buffers; `winner` holds w*h, `slot_flags`
+ * 2 * n_triangles bytes. */
+SGL_API sgl_status sgl_render_debug(sgl_ctx *ctx, int scene_id, const sgl_view *view, const sgl_target *target,
+                                    uint32_t *winner, uint8_t *slot_flags, sgl_frame_stats *stats);
+
+/* Depth-of-field gather alone on a rendered view (device or host buffers). */
+SGL_API sgl_status sgl_dof(sgl_ctx *ctx, const sgl_view *view, const sgl_target *in, const sgl_target *out,
+                           int device_buffers, void *stream);
+
+/* ------------------------------------------------------------- batching -- */
+
+/* Batched renderer: many views (of one or several resident scenes) rendered
+ * by one CUDA-graph launch.  Tile size and bin capacity come from the
+ * autotuner unless fixed in `opts`. */
+typedef struct sgl_batch_opts {
+    int tile;            /* 0 = autotune, else 8, 16 or 32 */
+    int bin_capacity;    /* 0 = autotune */
+    int use_graph;       /* capture the launch sequence in a CUDA graph */
+} sgl_batch_opts;
+
+typedef struct sgl_batch_item {
+    int        scene_id;
+    sgl_view   view;
+    sgl_target target;   /* device buffers */
+} sgl_batch_item;
+
+SGL_API sgl_status sgl_render_batch(sgl_ctx *ctx, const sgl_batch_item *items, int n_items,
+                                    const sgl_batch_opts *opts, void *stream, sgl_frame_stats *stats);
+SGL_API sgl_status sgl_autotune(sgl_ctx *ctx, const sgl_batch_item *items, int n_items, sgl_batch_opts *chosen);
+
+/* -------------------------------------------------------------- serving -- */
+
+typedef struct sgl_server sgl_server;
+
+typedef struct sgl_serve_opts {
+    uint64_t budget_bytes;     /* framebuffer + bin memory admitted at once */
+    int      max_batch;        /* views per batch */
+    int      streams;          /* batches in flight */
+    int      copy_out;         /* 1 = copy each finished frame to host memory */
+} sgl_serve_opts;
+
+typedef struct sgl_request {
+    int      scene_id;
+    sgl_view view;             /* x = y = 0; w, h = frame size */
+    uint32_t *host_pixels;     /* optional, w*h BGRA8 when copy_out */
+    float    *host_zbuffer;    /* optional */
+} sgl_request;
+
+typedef struct sgl_request_result {
+    sgl_status status;
+    double     submit_s, start_s, done_s;   /* host clock, seconds */
+    uint64_t   fragments;
+} sgl_request_result;
+
+SGL_API sgl_status sgl_server_create(sgl_ctx *ctx, const sgl_serve_opts *opts, sgl_server **out);
+SGL_API sgl_status sgl_server_submit(sgl_server *srv, const sgl_request *req, uint64_t *ticket);
+SGL_API sgl_status sgl_server_poll(sgl_server *srv, uint64_t ticket, sgl_request_result *result);
+SGL_API sgl_status sgl_server_wait(sgl_server *srv, uint64_t ticket, double timeout_s, sgl_request_result *result);
+SGL_API sgl_status sgl_server_drain(sgl_server *srv, double timeout_s);
+SGL_API void       sgl_server_destroy(sgl_server *srv);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGL_H */

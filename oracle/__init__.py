@@ -1,0 +1,123 @@
+"""The oracle: CPU renderers that the GPU path is checked against.
+
+TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg may import this package; the product never does.
+
+Two renderers share one calling convention:
+  * `restatement` — oracle/sgl_oracle.c, a C restatement of gbizzotto/swegl's
+    render path (builds anywhere with gcc; travels to the GPU machine as source);
+  * `reference`   — the reference's own sources compiled headless by
+    oracle/ref (only where the reference sources exist).  Its outputs are
+    committed as golden fixtures under tests/golden.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from swegl_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libsgl_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libswegl_ref.so")
+REFERENCE_SRC = "/root/reference"
+
+KIND_FULL, KIND_ORDINAL, KIND_PROGRESS, KIND_PHONG, KIND_TEXTURE = 0, 1, 2, 3, 4
+
+_libs: dict[str, C.CDLL] = {}
+
+
+def build(reference: bool | None = None) -> None:
+    """Compile the restatement, and the reference too when its sources exist."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if reference is None:
+        reference = os.path.isdir(os.path.join(REFERENCE_SRC, "src", "render"))
+    if reference:
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "-j8"], check=True)
+
+
+def restatement() -> C.CDLL:
+    if "orc" not in _libs:
+        if not os.path.exists(ORACLE_SO):
+            build(reference=False)
+        lib = C.CDLL(ORACLE_SO)
+        lib.orc_render.restype = C.c_int
+        lib.orc_render_parallel.restype = C.c_int
+        lib.orc_triangle_count.restype = C.c_uint64
+        _libs["orc"] = lib
+    return _libs["orc"]
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def reference() -> C.CDLL:
+    if "ref" not in _libs:
+        lib = C.CDLL(REF_SO)
+        lib.ref_render.restype = C.c_int
+        _libs["ref"] = lib
+    return _libs["ref"]
+
+
+class Result:
+    def __init__(self, frames, stats, winner):
+        self.frames = frames          # list of abi.HostFrame
+        self.stats = stats            # per view: (drawn, fragments, clip_one, clip_two); reference: (drawn, None)
+        self.winner = winner          # winner slots of view 0 or None
+
+    @property
+    def pixels(self):
+        return self.frames[0].pixels
+
+    @property
+    def zbuffer(self):
+        return self.frames[0].zbuffer
+
+
+def render(scene, views, kind: int = KIND_FULL, which: str = "restatement", winner: bool = False,
+           shared_surface: tuple[int, int] | None = None) -> Result:
+    """Render `views` in order (swegl::render(scene, vp0, vp1, ...)).
+
+    Each view gets its own surface of the view's size unless `shared_surface`
+    = (width, height) asks for one surface shared by all views."""
+    holder = abi.SceneDescHolder(scene)
+    if shared_surface:
+        surf = abi.HostFrame(*shared_surface)
+        frames = []
+        for v in views:
+            f = abi.HostFrame(*shared_surface, zw=v.w, zh=v.h)
+            f.pixels = surf.pixels
+            frames.append(f)
+    else:
+        frames = [abi.HostFrame(v.w, v.h) for v in views]
+    vd = (abi.ViewDesc * len(views))(*[abi.view_desc(v) for v in views])
+    td = (abi.Target * len(views))(*[f.target() for f in frames])
+    win = np.full((views[0].h, views[0].w), 0xFFFFFFFF, np.uint32) if winner else None
+    if which == "reference":
+        calls = (C.c_uint64 * len(views))()
+        rc = reference().ref_render(holder.ref(), vd, td, len(views), kind, calls)
+        stats = [(int(calls[i]), None) for i in range(len(views))]
+    else:
+        st = (C.c_uint64 * (4 * len(views)))()
+        wp = win.ctypes.data_as(C.POINTER(C.c_uint32)) if winner else None
+        rc = restatement().orc_render(holder.ref(), vd, td, len(views), kind, wp, st)
+        stats = [tuple(int(st[4 * i + k]) for k in range(4)) for i in range(len(views))]
+    if rc != 0:
+        raise RuntimeError(f"{which} render failed ({rc})")
+    return Result(frames, stats, win)
+
+
+def render_parallel(scene, views, threads: int) -> list:
+    """Independent views rendered on `threads` host threads (CPU baseline)."""
+    holder = abi.SceneDescHolder(scene)
+    frames = [abi.HostFrame(v.w, v.h) for v in views]
+    vd = (abi.ViewDesc * len(views))(*[abi.view_desc(v) for v in views])
+    td = (abi.Target * len(views))(*[f.target() for f in frames])
+    rc = restatement().orc_render_parallel(holder.ref(), vd, td, len(views), threads)
+    if rc != 0:
+        raise RuntimeError(f"parallel oracle render failed ({rc})")
+    return frames
