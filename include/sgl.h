@@ -211,62 +211,6 @@ SGL_API sgl_status sgl_render(sgl_ctx *ctx, int scene_id, const sgl_view *views,
 SGL_API sgl_status sgl_render_debug(sgl_ctx *ctx, int scene_id, const sgl_view *view, const sgl_target *target,
                                     uint32_t *winner, uint8_t *slot_flags, sgl_frame_stats *stats);
 
-/* Depth-of-field gather alone on a rendered view (device or host buffers). */
-SGL_API sgl_status sgl_dof(sgl_ctx *ctx, const sgl_view *view, const sgl_target *in, const sgl_target *out,
-                           int device_buffers, void *stream);
-
-/* ------------------------------------------------------------- batching -- */
-
-/* Batched renderer: many views (of one or several resident scenes) rendered
- * by one CUDA-graph launch.  Tile size and bin capacity come from the
- * autotuner unless fixed in `opts`. */
-typedef struct sgl_batch_opts {
-    int tile;            /* 0 = autotune, else 8, 16 or 32 */
-    int bin_capacity;    /* 0 = autotune */
-    int use_graph;       /* capture the launch sequence in a CUDA graph */
-} sgl_batch_opts;
-
-typedef struct sgl_batch_item {
-    int        scene_id;
-    sgl_view   view;
-    sgl_target target;   /* device buffers */
-} sgl_batch_item;
-
-SGL_API sgl_status sgl_render_batch(sgl_ctx *ctx, const sgl_batch_item *items, int n_items,
-                                    const sgl_batch_opts *opts, void *stream, sgl_frame_stats *stats);
-SGL_API sgl_status sgl_autotune(sgl_ctx *ctx, const sgl_batch_item *items, int n_items, sgl_batch_opts *chosen);
-
-/* -------------------------------------------------------------- serving -- */
-
-typedef struct sgl_server sgl_server;
-
-typedef struct sgl_serve_opts {
-    uint64_t budget_bytes;     /* framebuffer + bin memory admitted at once */
-    int      max_batch;        /* views per batch */
-    int      streams;          /* batches in flight */
-    int      copy_out;         /* 1 = copy each finished frame to host memory */
-} sgl_serve_opts;
-
-typedef struct sgl_request {
-    int      scene_id;
-    sgl_view view;             /* x = y = 0; w, h = frame size */
-    uint32_t *host_pixels;     /* optional, w*h BGRA8 when copy_out */
-    float    *host_zbuffer;    /* optional */
-} sgl_request;
-
-typedef struct sgl_request_result {
-    sgl_status status;
-    double     submit_s, start_s, done_s;   /* host clock, seconds */
-    uint64_t   fragments;
-} sgl_request_result;
-
-SGL_API sgl_status sgl_server_create(sgl_ctx *ctx, const sgl_serve_opts *opts, sgl_server **out);
-SGL_API sgl_status sgl_server_submit(sgl_server *srv, const sgl_request *req, uint64_t *ticket);
-SGL_API sgl_status sgl_server_poll(sgl_server *srv, uint64_t ticket, sgl_request_result *result);
-SGL_API sgl_status sgl_server_wait(sgl_server *srv, uint64_t ticket, double timeout_s, sgl_request_result *result);
-SGL_API sgl_status sgl_server_drain(sgl_server *srv, double timeout_s);
-SGL_API void       sgl_server_destroy(sgl_server *srv);
-
 #ifdef __cplusplus
 }
 #endif

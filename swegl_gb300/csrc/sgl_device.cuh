@@ -1,0 +1,166 @@
+// sgl_device.cuh — device-side arithmetic of the swegl render path.
+//
+// Every helper performs the same IEEE single-precision operations, in the same
+// order, as the reference function cited beside it (paths inside
+// gbizzotto/swegl), so that coverage, depth and the depth-test winner are
+// bit-exact.  The library is compiled with -fmad=false (no fused
+// multiply-add contraction), IEEE division and square root (no fast-math) and
+// denormals preserved, matching the reference's x86-64 SSE build.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sgl {
+
+struct V3 {
+    float x, y, z;
+};
+struct V2 {
+    float x, y;
+};
+
+__device__ __forceinline__ V3 mk3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 add3(V3 a, V3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 sub3(V3 a, V3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 mul3(V3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 neg3(V3 a) { return mk3(-a.x, -a.y, -a.z); }
+// vector_t::dot (swegl/projection/points.hpp:91-94)
+__device__ __forceinline__ float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V2 mk2(float x, float y) { return V2{x, y}; }
+__device__ __forceinline__ V2 add2(V2 a, V2 b) { return mk2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ V2 sub2(V2 a, V2 b) { return mk2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ V2 mul2(V2 a, float s) { return mk2(a.x * s, a.y * s); }
+
+// vector_t::normalize (swegl/projection/points.hpp:71-90)
+__device__ __forceinline__ V3 normalize3(V3 v)
+{
+    float l = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    if (l != 0.0f) {
+        v.x = v.x / l;
+        v.y = v.y / l;
+        v.z = v.z / l;
+    }
+    return v;
+}
+
+// cross() returns a normalised normal_t (src/projection/points.cpp:32-37)
+__device__ __forceinline__ V3 cross_n(V3 a, V3 b)
+{
+    return normalize3(mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x));
+}
+
+// transform(vertex, m): rows 0-2 only (src/projection/points.cpp:8-13)
+__device__ __forceinline__ V3 transform3(V3 v, const float *m)
+{
+    return mk3(m[0] * v.x + m[1] * v.y + m[2] * v.z + m[3], m[4] * v.x + m[5] * v.y + m[6] * v.z + m[7],
+               m[8] * v.x + m[9] * v.y + m[10] * v.z + m[11]);
+}
+
+// rotate(normal, m) then the normal_t constructor (src/projection/points.cpp:44-49)
+__device__ __forceinline__ V3 rotate_n(V3 v, const float *m)
+{
+    return normalize3(mk3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
+                          m[8] * v.x + m[9] * v.y + m[10] * v.z));
+}
+
+// (int)f as the reference's x86-64 build evaluates it (cvttss2si): out of
+// range and NaN give INT_MIN.  The hardware conversion saturates instead.
+__device__ __forceinline__ int f2i(float f)
+{
+    return (f >= -2147483648.0f && f < 2147483648.0f) ? __float2int_rz(f) : INT32_MIN;
+}
+
+// The reference compares floats with the double constants 0.001 and 0.05
+// (renderer.cpp:65,281,286,489; pixel_shaders.cpp:179).  0.001f and 0.05f are
+// the smallest floats above those doubles, so for a float x:
+//   (double)x <  0.001  <=>  x <  0.001f      (double)x >= 0.001  <=>  x >= 0.001f
+//   (double)x <= 0.001  <=>  x <  0.001f      (double)x <  0.05   <=>  x <  0.05f
+// which keeps these tests off the FP64 pipe.
+__device__ __forceinline__ bool below_near(float x) { return x < 0.001f; }    // (double)x < 0.001, or <= 0.001
+__device__ __forceinline__ bool at_or_past_near(float x) { return x >= 0.001f; } // (double)x >= 0.001
+
+// interpolator_g<1> (swegl/render/interpolator.hpp:52-104)
+struct Interp {
+    float top, tstep, alpha, bottom, bstep, v0, dv;
+
+    __device__ __forceinline__ void init_self(float dist, float z1, float z2)
+    {
+        v0 = z1;
+        dv = z2 - z1;
+        float alphastep = 1.0f / dist;
+        bottom = 1.0f / z1;
+        float invz2 = 1.0f / z2;
+        alpha = 0.0f;
+        top = alpha;
+        top = top * bottom;
+        tstep = (1.0f * invz2 - top) * alphastep;
+        bstep = (invz2 - bottom) * alphastep;
+    }
+    __device__ __forceinline__ void displace(float move)
+    {
+        top = top + tstep * move;
+        bottom = bottom + bstep * move;
+        alpha = top / bottom;
+    }
+    __device__ __forceinline__ void step()
+    {
+        top = top + tstep;
+        bottom = bottom + bstep;
+        alpha = top / bottom;
+    }
+    __device__ __forceinline__ float value() const { return v0 + dv * alpha; }
+};
+
+// line_side (src/render/renderer.cpp:21-26)
+struct Side {
+    Interp it;
+    float ratio;
+    float x;
+};
+
+// Float-float helpers for the specular power.  The reference evaluates
+// pow((double)s, p) and rounds to float (src/render/pixel_shaders.cpp:193);
+// s^p is formed here by binary exponentiation on (hi, lo) float pairs with
+// exact products (error-free transformations built on fmaf), ~44 bits of
+// precision, then rounded to float.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_prod(float a, float b)
+{
+    float p = a * b;
+    float e = fmaf(a, b, -p);
+    return FF{p, e};
+}
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b)
+{
+    float s = a + b;
+    float e = b - (s - a);
+    return FF{s, e};
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b)
+{
+    FF p = ff_two_prod(a.hi, b.hi);
+    float cross = fmaf(a.hi, b.lo, a.lo * b.hi);
+    return ff_fast_two_sum(p.hi, p.lo + cross);
+}
+__device__ __forceinline__ float spec_pow(float s, int p)
+{
+    FF base{s, 0.0f};
+    FF acc{1.0f, 0.0f};
+    bool first = true;
+    while (p > 0) {
+        if (p & 1) {
+            acc = first ? base : ff_mul(acc, base);
+            first = false;
+        }
+        p >>= 1;
+        if (p)
+            base = ff_mul(base, base);
+    }
+    // round the pair to the nearest float
+    return acc.hi + acc.lo;
+}
+
+} // namespace sgl

@@ -1,0 +1,153 @@
+"""Python binding of the C ABI (include/sgl.h) over ctypes.
+
+This mirrors the reference's render interface for tests and benchmarks:
+`Renderer.render(scene_id, views)` is swegl::render(scene, vp0, vp1, ...)
+(swegl/render/renderer.hpp:27-34) for the Phong + bilinear pixel shader, with
+each view written to its own surface (or a shared one) and z-buffer.
+
+The GPU library is required: there is no CPU fallback.  Loading fails loudly
+when swegl_gb300/_build/libsgl.so has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsgl.so")
+
+_lib = None
+
+
+class SglError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def library() -> C.CDLL:
+    """The in-tree CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        lib = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        sigs = {
+            "sgl_version": ([], C.c_int),
+            "sgl_status_string": ([C.c_int], C.c_char_p),
+            "sgl_create": ([P(C.c_void_p), C.c_int], C.c_int),
+            "sgl_destroy": ([C.c_void_p], None),
+            "sgl_last_error": ([C.c_void_p], C.c_char_p),
+            "sgl_scene_upload": ([C.c_void_p, P(abi.SceneDesc), P(C.c_int)], C.c_int),
+            "sgl_scene_release": ([C.c_void_p, C.c_int], C.c_int),
+            "sgl_scene_set_nodes": ([C.c_void_p, C.c_int, P(abi.NodeDesc), C.c_int], C.c_int),
+            "sgl_scene_set_lights": ([C.c_void_p, C.c_int, C.c_float, P(C.c_float), C.c_float, P(abi.PointLight),
+                                      C.c_int], C.c_int),
+            "sgl_scene_info": ([C.c_void_p, C.c_int, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)], C.c_int),
+            "sgl_render": ([C.c_void_p, C.c_int, P(abi.ViewDesc), P(abi.Target), C.c_int, C.c_int, C.c_void_p,
+                            P(abi.FrameStats)], C.c_int),
+            "sgl_render_debug": ([C.c_void_p, C.c_int, P(abi.ViewDesc), P(abi.Target), P(C.c_uint32), P(C.c_uint8),
+                                  P(abi.FrameStats)], C.c_int),
+        }
+        for name, (args, res) in sigs.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = lib
+    return _lib
+
+
+class Renderer:
+    """One sgl context on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = library()
+        h = C.c_void_p()
+        st = self.lib.sgl_create(C.byref(h), device)
+        if st != 0:
+            raise SglError(st, "sgl_create failed")
+        self.ctx = h
+        self._holders = {}
+
+    def close(self):
+        if self.ctx:
+            self.lib.sgl_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st != 0:
+            raise SglError(st, self.lib.sgl_last_error(self.ctx).decode(errors="replace"))
+
+    # scenes ---------------------------------------------------------------
+    def upload(self, scene) -> int:
+        holder = abi.SceneDescHolder(scene)
+        sid = C.c_int()
+        self._check(self.lib.sgl_scene_upload(self.ctx, C.byref(holder.desc), C.byref(sid)))
+        return sid.value
+
+    def release(self, scene_id: int):
+        self._check(self.lib.sgl_scene_release(self.ctx, scene_id))
+
+    def scene_info(self, scene_id: int) -> dict:
+        t, v, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._check(self.lib.sgl_scene_info(self.ctx, scene_id, C.byref(t), C.byref(v), C.byref(b)))
+        return {"triangles": t.value, "vertices": v.value, "device_bytes": b.value}
+
+    # rendering ------------------------------------------------------------
+    def render(self, scene_id: int, views, shared_surface=None, stats: bool = False):
+        """Render `views` in order into host surfaces (one per view, or one
+        shared surface of size `shared_surface`).  Returns (frames, stats)."""
+        if shared_surface:
+            surf = abi.HostFrame(*shared_surface)
+            frames = []
+            for v in views:
+                f = abi.HostFrame(*shared_surface, zw=v.w, zh=v.h)
+                f.pixels = surf.pixels
+                frames.append(f)
+        else:
+            frames = [abi.HostFrame(v.w, v.h) for v in views]
+        vd = (abi.ViewDesc * len(views))(*[abi.view_desc(v) for v in views])
+        td = (abi.Target * len(views))(*[f.target() for f in frames])
+        fs = abi.FrameStats()
+        self._check(self.lib.sgl_render(self.ctx, scene_id, vd, td, len(views), 0, None,
+                                        C.byref(fs) if stats else None))
+        return frames, (_stats_dict(fs) if stats else None)
+
+    def render_device(self, scene_id: int, views, targets, stream: int = 0, stats: bool = False):
+        """Render into device buffers (targets: list of abi.Target with device pointers)."""
+        vd = (abi.ViewDesc * len(views))(*[abi.view_desc(v) for v in views])
+        td = (abi.Target * len(views))(*targets)
+        fs = abi.FrameStats()
+        self._check(self.lib.sgl_render(self.ctx, scene_id, vd, td, len(views), 1, C.c_void_p(stream),
+                                        C.byref(fs) if stats else None))
+        return _stats_dict(fs) if stats else None
+
+    def render_debug(self, scene_id: int, view):
+        """One view with the per-pixel winner slot and per-slot setup flags."""
+        info = self.scene_info(scene_id)
+        frame = abi.HostFrame(view.w, view.h)
+        winner = np.empty((view.h, view.w), np.uint32)
+        flags = np.zeros(2 * max(1, info["triangles"]), np.uint8)
+        fs = abi.FrameStats()
+        vd = abi.view_desc(view)
+        td = frame.target()
+        self._check(self.lib.sgl_render_debug(self.ctx, scene_id, C.byref(vd), C.byref(td),
+                                              winner.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                              flags.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(fs)))
+        return frame, winner, flags, _stats_dict(fs)
+
+
+def _stats_dict(fs: abi.FrameStats) -> dict:
+    return {"triangles": fs.triangles, "drawn_triangles": fs.drawn_triangles, "fragments": fs.fragments,
+            "pixels": fs.pixels, "kernel_launches": fs.kernel_launches}
