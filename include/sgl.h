@@ -211,6 +211,15 @@ SGL_API sgl_status sgl_render(sgl_ctx *ctx, int scene_id, const sgl_view *views,
 SGL_API sgl_status sgl_render_debug(sgl_ctx *ctx, int scene_id, const sgl_view *view, const sgl_target *target,
                                     uint32_t *winner, uint8_t *slot_flags, sgl_frame_stats *stats);
 
+/* Per-kernel device timing (CUDA events on the launching stream around each
+ * kernel of every frame rendered while enabled).  Enabling resets the totals.
+ * Kernels are numbered 0..n-1; reading past the last returns SGL_ERR_NOT_FOUND.
+ * No reference counterpart: the reference's only timer is the demo's frame
+ * clock (src/test_1.cpp:365-376). */
+SGL_API sgl_status sgl_profile(sgl_ctx *ctx, int enable);
+SGL_API sgl_status sgl_profile_read(sgl_ctx *ctx, int kernel, const char **name, double *total_ms,
+                                    uint64_t *launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -344,6 +344,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     CUDA_TRY(upload(d_texs, texs.data(), texs.size()));
     CUDA_TRY(d_wpos.ensure(sizeof(float4) * std::max<size_t>(n_vertices, 1)));
     CUDA_TRY(d_wnrm.ensure(sizeof(float4) * std::max<size_t>(n_vertices, 1)));
+    CUDA_TRY(d_uv.ensure(sizeof(float2) * std::max<size_t>(n_vertices, 1)));
     dev = SceneDev{};
     dev.pos_u = (const float4 *)d_pos_u.ptr;
     dev.nrm_v = (const float4 *)d_nrm_v.ptr;
@@ -354,6 +355,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     dev.texs = (const TexDesc *)d_texs.ptr;
     dev.wpos = (float4 *)d_wpos.ptr;
     dev.wnrm = (float4 *)d_wnrm.ptr;
+    dev.uv = (float2 *)d_uv.ptr;
     dev.n_vertices = n_vertices;
     dev.n_triangles = n_triangles;
     dev.n_mats = d->n_materials;
@@ -369,7 +371,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     if (st != SGL_OK)
         return st;
     device_bytes = d_pos_u.bytes + d_nrm_v.bytes + d_vnode.bytes + d_tris.bytes + d_prims.bytes + d_mats.bytes +
-                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_node_world.bytes + d_node_rs.bytes;
+                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_uv.bytes + d_node_world.bytes + d_node_rs.bytes;
     return SGL_OK;
 }
 
@@ -414,25 +416,38 @@ sgl_status check_view(Ctx *ctx, const sgl_view &v, const sgl_target &t)
 
 // Render one view into device buffers (surface rect + z) on `st`.
 sgl_status render_view_device(Ctx *ctx, Scene &s, const sgl_view &view, uint32_t *rect_pixels, int pitch_px,
-                              float *zbuf, FrameScratch &fs, cudaStream_t st, uint8_t *slot_flags, int *launches)
+                              float *zbuf, FrameScratch &fs, cudaStream_t st, uint8_t *slot_flags, int *launches,
+                              Profiler *prof)
 {
     const size_t px = (size_t)view.w * view.h;
+    const size_t span_cap = std::max<size_t>(65536, px / 8);
     CUDA_TRY(fs.ndc.ensure(sizeof(float4) * std::max<uint32_t>(s.n_vertices, 1)));
     CUDA_TRY(fs.yes.ensure(std::max<uint32_t>(s.n_vertices, 1)));
     CUDA_TRY(fs.key.ensure(sizeof(unsigned long long) * px));
-    CUDA_TRY(fs.counters.ensure(4 * sizeof(unsigned long long)));
-    CUDA_TRY(cudaMemsetAsync(fs.counters.ptr, 0, 4 * sizeof(unsigned long long), st));
+    CUDA_TRY(fs.prec.ensure(sizeof(float4) * px));
+    CUDA_TRY(fs.classes.ensure(sizeof(uint32_t) * kClasses * (size_t)std::max<uint32_t>(s.n_triangles, 1)));
+    CUDA_TRY(fs.cliptri.ensure(sizeof(uint32_t) * std::max<uint32_t>(s.n_triangles, 1)));
+    CUDA_TRY(fs.clippx.ensure(sizeof(uint32_t) * px));
+    CUDA_TRY(fs.spans.ensure(sizeof(SpanRec) * span_cap));
+    CUDA_TRY(fs.counters.ensure(kCounterWords * sizeof(unsigned long long)));
     FrameDev f;
     f.ndc = (float4 *)fs.ndc.ptr;
     f.yes = (uint8_t *)fs.yes.ptr;
     f.key = (unsigned long long *)fs.key.ptr;
+    f.prec = (float4 *)fs.prec.ptr;
+    f.classes = (uint32_t *)fs.classes.ptr;
+    f.cliptri = (uint32_t *)fs.cliptri.ptr;
+    f.clippx = (uint32_t *)fs.clippx.ptr;
+    f.spans = (SpanRec *)fs.spans.ptr;
+    f.span_cap = (uint32_t)std::min<size_t>(fs.spans.bytes / sizeof(SpanRec), 0xFFFFFFFFu);
     f.pixels = rect_pixels;
     f.pitch_px = pitch_px;
     f.zbuf = zbuf;
     f.counters = (unsigned long long *)fs.counters.ptr;
+    f.counters32 = (uint32_t *)fs.counters.ptr;
     f.slot_flags = slot_flags;
     const ViewDev v = make_view(view);
-    CUDA_TRY(launch_frame(s.dev, s.lights, v, f, st, launches));
+    CUDA_TRY(launch_frame(s.dev, s.lights, v, f, st, launches, prof));
     return SGL_OK;
 }
 
@@ -591,7 +606,7 @@ SGL_API sgl_status sgl_scene_info(sgl_ctx *c, int scene_id, uint64_t *n_triangle
 
 static sgl_status read_stats(Ctx *ctx, FrameScratch &fs, cudaStream_t st, sgl_frame_stats *acc)
 {
-    unsigned long long h[2];
+    unsigned long long h[2]; // [C_DRAWN], [C_FRAGMENTS]
     CUDA_TRY(cudaMemcpyAsync(h, fs.counters.ptr, sizeof h, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     acc->drawn_triangles += h[0];
@@ -626,7 +641,7 @@ SGL_API sgl_status sgl_render(sgl_ctx *c, int scene_id, const sgl_view *views, c
         if (device_buffers) {
             uint32_t *rect = (uint32_t *)t.pixels + (size_t)v.y * pitch_px + v.x;
             sgl_status r = render_view_device(ctx, *s, v, rect, pitch_px, t.zbuffer, ctx->frame, st, nullptr,
-                                              &launches);
+                                              &launches, &ctx->prof);
             if (r != SGL_OK)
                 return r;
         } else {
@@ -634,7 +649,8 @@ SGL_API sgl_status sgl_render(sgl_ctx *c, int scene_id, const sgl_view *views, c
             CUDA_TRY(ctx->stage_pixels.ensure(4 * px));
             CUDA_TRY(ctx->stage_z.ensure(4 * px));
             sgl_status r = render_view_device(ctx, *s, v, (uint32_t *)ctx->stage_pixels.ptr, v.w,
-                                              (float *)ctx->stage_z.ptr, ctx->frame, st, nullptr, &launches);
+                                              (float *)ctx->stage_z.ptr, ctx->frame, st, nullptr, &launches,
+                                              &ctx->prof);
             if (r != SGL_OK)
                 return r;
             uint8_t *dst = (uint8_t *)t.pixels + (size_t)v.y * t.pitch + 4 * (size_t)v.x;
@@ -716,6 +732,37 @@ SGL_API sgl_status sgl_render_debug(sgl_ctx *c, int scene_id, const sgl_view *vi
         acc.kernel_launches = (uint32_t)launches;
         *stats = acc;
     }
+    return SGL_OK;
+}
+
+SGL_API sgl_status sgl_profile(sgl_ctx *c, int enable)
+{
+    Ctx *ctx = reinterpret_cast<Ctx *>(c);
+    if (!ctx)
+        return SGL_ERR_INVALID;
+    prof_flush(&ctx->prof);
+    ctx->prof.enabled = enable != 0;
+    for (int k = 0; k < kProfKernels; k++) {
+        ctx->prof.ms[k] = 0.0;
+        ctx->prof.launches[k] = 0;
+    }
+    return SGL_OK;
+}
+
+SGL_API sgl_status sgl_profile_read(sgl_ctx *c, int kernel, const char **name, double *total_ms, uint64_t *launches)
+{
+    Ctx *ctx = reinterpret_cast<Ctx *>(c);
+    if (!ctx || kernel < 0)
+        return SGL_ERR_INVALID;
+    if (kernel >= kProfKernels)
+        return SGL_ERR_NOT_FOUND;
+    prof_flush(&ctx->prof);
+    if (name)
+        *name = prof_kernel_name(kernel);
+    if (total_ms)
+        *total_ms = ctx->prof.ms[kernel];
+    if (launches)
+        *launches = ctx->prof.launches[kernel];
     return SGL_OK;
 }
 

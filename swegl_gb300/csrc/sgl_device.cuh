@@ -50,6 +50,16 @@ __device__ __forceinline__ V3 cross_n(V3 a, V3 b)
     return normalize3(mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x));
 }
 
+// cross(a, b).z() of the normalised cross product (points.cpp:32-37) without
+// the two divisions whose results are discarded: normalize() divides each
+// component by the same length independently.
+__device__ __forceinline__ float cross_n_z(V3 a, V3 b)
+{
+    const float x = a.y * b.z - a.z * b.y, y = a.z * b.x - a.x * b.z, z = a.x * b.y - a.y * b.x;
+    const float l = sqrtf(x * x + y * y + z * z);
+    return l != 0.0f ? z / l : z;
+}
+
 // transform(vertex, m): rows 0-2 only (src/projection/points.cpp:8-13)
 __device__ __forceinline__ V3 transform3(V3 v, const float *m)
 {

@@ -28,15 +28,15 @@ struct DevBuf {
 // Per-view scratch reused across frames: vertex NDC, visibility flags,
 // per-pixel depth keys and the frame counters.
 struct FrameScratch {
-    DevBuf ndc, yes, key, counters;
+    DevBuf ndc, yes, key, prec, classes, cliptri, clippx, spans, counters;
 };
 
 struct Ctx;
 
 // A scene resident in device memory.
 struct Scene {
-    DevBuf d_pos_u, d_nrm_v, d_vnode, d_tris, d_prims, d_mats, d_texs, d_texels, d_wpos, d_wnrm, d_node_world,
-        d_node_rs;
+    DevBuf d_pos_u, d_nrm_v, d_vnode, d_tris, d_prims, d_mats, d_texs, d_texels, d_wpos, d_wnrm, d_uv,
+        d_node_world, d_node_rs;
     SceneDev dev{};
     LightsDev lights{};
     std::vector<sgl_node_desc> nodes;
@@ -58,6 +58,7 @@ struct Ctx {
     int next_scene_id = 1;
     FrameScratch frame;
     DevBuf stage_pixels, stage_z, debug_flags;
+    Profiler prof;
 
     void fail(const char *fmt, ...) __attribute__((format(printf, 2, 3)));
     Scene *find(int id)
@@ -70,6 +71,7 @@ struct Ctx {
 ViewDev make_view(const sgl_view &v);
 sgl_status check_view(Ctx *ctx, const sgl_view &v, const sgl_target &t);
 sgl_status render_view_device(Ctx *ctx, Scene &s, const sgl_view &view, uint32_t *rect_pixels, int pitch_px,
-                              float *zbuf, FrameScratch &fs, cudaStream_t st, uint8_t *slot_flags, int *launches);
+                              float *zbuf, FrameScratch &fs, cudaStream_t st, uint8_t *slot_flags, int *launches,
+                              Profiler *prof = nullptr);
 
 } // namespace sgl

@@ -1,0 +1,223 @@
+// sgl_shade.cuh — the pixel shader of the swegl render path on the device:
+// pixel_shader_light_and_texture<pixel_shader_lights_phong,
+// pixel_shader_texture_bilinear> (swegl/render/pixel_shaders.hpp:121-179,
+// src/render/pixel_shaders.cpp:88-205,284-384), with the reference's
+// single-precision operation order.
+#pragma once
+
+#include "sgl_device.cuh"
+#include "sgl_internal.h"
+
+namespace sgl {
+
+// The state of pixel_shader_light_and_texture<lights_phong, texture_bilinear>
+// (swegl/render/pixel_shaders.hpp:76-97,125-150,121-179).
+struct Shader {
+    V3 v0, v1, v2, n0, n1, n2;
+    V3 vleft, vright, vleftdir, vrightdir, nleft, nright, nleftdir, nrightdir;
+    V3 v, vdir, n, ndir;
+    V2 t0, t1, t2, side_long_t_dir, side_short_t, side_short_t_dir, t_left, t_dir;
+    bool llr;
+    const uint32_t *tex;
+    uint32_t color;
+    int tw, th, shininess;
+};
+
+// pixel_shader_*::prepare_for_triangle (src/render/pixel_shaders.cpp:88-105,304-318)
+__device__ __forceinline__ void sh_prepare_triangle(Shader &sh, const V3 w[3], const V3 n[3], const V2 uv[3],
+                                                    bool inverted)
+{
+    sh.v0 = w[0];
+    sh.v1 = w[1];
+    sh.v2 = w[2];
+    if (!inverted) {
+        sh.n0 = n[0];
+        sh.n1 = n[1];
+        sh.n2 = n[2];
+    } else {
+        sh.n0 = neg3(n[0]);
+        sh.n1 = neg3(n[1]);
+        sh.n2 = neg3(n[2]);
+    }
+    const float tw = (float)sh.tw, th = (float)sh.th;
+    sh.t0 = mk2(uv[0].x * tw, uv[0].y * th);
+    sh.t1 = mk2(uv[1].x * tw, uv[1].y * th);
+    sh.t2 = mk2(uv[2].x * tw, uv[2].y * th);
+    sh.side_long_t_dir = sub2(sh.t2, sh.t0);
+}
+
+// pixel_shaders.cpp:106-126,320-325
+__device__ __forceinline__ void sh_prepare_upper(Shader &sh, bool llr)
+{
+    sh.vleft = sh.v0;
+    sh.vright = sh.v0;
+    sh.vleftdir = llr ? sub3(sh.v1, sh.v0) : sub3(sh.v2, sh.v0);
+    sh.vrightdir = llr ? sub3(sh.v2, sh.v0) : sub3(sh.v1, sh.v0);
+    sh.nleft = sh.n0;
+    sh.nright = sh.n0;
+    sh.nleftdir = llr ? sub3(sh.n1, sh.n0) : sub3(sh.n2, sh.n0);
+    sh.nrightdir = llr ? sub3(sh.n2, sh.n0) : sub3(sh.n1, sh.n0);
+    sh.llr = llr;
+    sh.side_short_t = sh.t0;
+    sh.side_short_t_dir = sub2(sh.t1, sh.t0);
+}
+
+// pixel_shaders.cpp:127-151,327-332
+__device__ __forceinline__ void sh_prepare_lower(Shader &sh, bool llr)
+{
+    if (llr) {
+        sh.vright = sh.v0;
+        sh.vrightdir = sub3(sh.v2, sh.v0);
+        sh.vleft = sh.v1;
+        sh.vleftdir = sub3(sh.v2, sh.v1);
+        sh.nright = sh.n0;
+        sh.nrightdir = sub3(sh.n2, sh.n0);
+        sh.nleft = sh.n1;
+        sh.nleftdir = sub3(sh.n2, sh.n1);
+    } else {
+        sh.vleft = sh.v0;
+        sh.vleftdir = sub3(sh.v2, sh.v0);
+        sh.vright = sh.v1;
+        sh.vrightdir = sub3(sh.v2, sh.v1);
+        sh.nleft = sh.n0;
+        sh.nleftdir = sub3(sh.n2, sh.n0);
+        sh.nright = sh.n1;
+        sh.nrightdir = sub3(sh.n2, sh.n1);
+    }
+    sh.llr = llr;
+    sh.side_short_t = sh.t1;
+    sh.side_short_t_dir = sub2(sh.t2, sh.t1);
+}
+
+// pixel_shaders.cpp:152-158,334-346
+__device__ __forceinline__ void sh_prepare_scanline(Shader &sh, float pl, float pr)
+{
+    sh.v = add3(sh.vleft, mul3(sh.vleftdir, pl));
+    sh.vdir = sub3(add3(sh.vright, mul3(sh.vrightdir, pr)), sh.v);
+    sh.n = add3(sh.nleft, mul3(sh.nleftdir, pl));
+    sh.ndir = sub3(add3(sh.nright, mul3(sh.nrightdir, pr)), sh.n);
+    if (sh.llr) {
+        sh.t_left = add2(sh.side_short_t, mul2(sh.side_short_t_dir, pl));
+        sh.t_dir = sub2(add2(sh.t0, mul2(sh.side_long_t_dir, pr)), sh.t_left);
+    } else {
+        sh.t_left = add2(sh.t0, mul2(sh.side_long_t_dir, pl));
+        sh.t_dir = sub2(add2(sh.side_short_t, mul2(sh.side_short_t_dir, pr)), sh.t_left);
+    }
+}
+
+// pixel_shader_lights_phong::shade (src/render/pixel_shaders.cpp:159-205)
+__device__ __forceinline__ int sh_phong(const Shader &sh, const LightsDev &L, const ViewDev &v, float progress)
+{
+    const V3 center = add3(sh.v, mul3(sh.vdir, progress));
+    const V3 normal = normalize3(add3(sh.n, mul3(sh.ndir, progress)));
+    const V3 camvec = normalize3(sub3(mk3(v.campos[0], v.campos[1], v.campos[2]), center));
+    float face_sun = -dot3(normal, mk3(L.sun[0], L.sun[1], L.sun[2]));
+    if (face_sun < 0.0f)
+        face_sun = 0.0f;
+    else
+        face_sun = face_sun * L.sun_intensity;
+    float dyn = 0.0f;
+    for (int l = 0; l < L.n; l++) {
+        const float4 pl = L.pl[l];
+        V3 ld = sub3(center, mk3(pl.x, pl.y, pl.z));
+        const float d2 = ld.x * ld.x + ld.y * ld.y + ld.z * ld.z;
+        float diffuse = pl.w / d2;
+        if (diffuse < 0.05f) // (double)diffuse < 0.05, see sgl_device.cuh
+            continue;
+        ld = normalize3(ld);
+        const float alignment = -dot3(normal, ld);
+        if (alignment < 0.0f)
+            continue;
+        diffuse = diffuse * alignment;
+        const V3 reflection = add3(ld, mul3(normal, alignment * 2.0f));
+        float specular = dot3(reflection, camvec);
+        if (specular > 0.0f) {
+            specular = spec_pow(specular, sh.shininess);
+            specular = specular * (float)sh.shininess / 2.0f;
+            dyn = dyn + (diffuse + specular / d2);
+        } else {
+            dyn = dyn + diffuse;
+        }
+    }
+    return f2i(65536.0f * (L.ambient + face_sun + dyn));
+}
+
+// pixel_shader_texture_bilinear::shade (src/render/pixel_shaders.cpp:348-384)
+// with the pixel_colors_f sums of src/render/colors.cpp:11-30.  v comes from
+// t.x and u from t.y, as in the reference.
+__device__ __forceinline__ uint32_t sh_bilinear(const Shader &sh, float progress)
+{
+    const V2 t = add2(sh.t_left, mul2(sh.t_dir, progress));
+    float v = t.x;
+    float u = t.y;
+    // (float)(u - 0.5) in double equals u - 0.5f in float: 0.5 is exact and
+    // double rounding is innocuous for a single subtraction.
+    const float u1 = u - 0.5f, u2 = u + 0.5f, v1 = v - 0.5f, v2 = v + 0.5f;
+    u = floorf(u2);
+    v = floorf(v2);
+    const int tw = sh.tw, th = sh.th;
+    int v1m = (f2i(v1) + th) % th;
+    int v2m = v1m + 1;
+    if (v2m == th)
+        v2m = 0;
+    v1m *= tw;
+    v2m *= tw;
+    const int u1m = (f2i(u1) + tw) % tw;
+    int u2m = u1m + 1;
+    if (u2m == tw)
+        u2m = 0;
+    const long long n = (long long)tw * th;
+    const long long i11 = (long long)v1m + u1m, i21 = (long long)v2m + u1m, i12 = (long long)v1m + u2m,
+                    i22 = (long long)v2m + u2m;
+    if (i11 < 0 || i11 >= n || i21 < 0 || i21 >= n || i12 < 0 || i12 >= n || i22 < 0 || i22 >= n)
+        return 0u; // the reference reads outside the texture here
+    const float w11 = (u - u1) * (v - v1), w21 = (u - u1) * (v2 - v), w12 = (u2 - u) * (v - v1),
+                w22 = (u2 - u) * (v2 - v);
+    uint32_t c11 = sh.color, c21 = sh.color, c12 = sh.color, c22 = sh.color; // untextured: 1x1 of the colour
+    if (sh.tex) {
+        c11 = __ldg(sh.tex + i11);
+        c21 = __ldg(sh.tex + i21);
+        c12 = __ldg(sh.tex + i12);
+        c22 = __ldg(sh.tex + i22);
+    }
+    uint32_t out = 0;
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) {
+        const int sft = 8 * ch;
+        float acc = (float)((c11 >> sft) & 0xFFu) * w11;
+        acc = acc + (float)((c21 >> sft) & 0xFFu) * w21;
+        acc = acc + (float)((c12 >> sft) & 0xFFu) * w12;
+        acc = acc + (float)((c22 >> sft) & 0xFFu) * w22;
+        out |= ((uint32_t)f2i(roundf(acc)) & 0xFFu) << sft;
+    }
+    return out;
+}
+
+// pixel_shader_light_and_texture::shade (swegl/render/pixel_shaders.hpp:159-178)
+__device__ __forceinline__ uint32_t sh_shade(const Shader &sh, const LightsDev &L, const ViewDev &v, float progress)
+{
+    uint32_t color = sh_bilinear(sh, progress);
+    // (float)(i / 65536.0): the int rounded to float, then an exact power-of-two scale
+    float light = __int2float_rn(sh_phong(sh, L, v, progress)) * (1.0f / 65536.0f);
+    uint32_t out = color & 0xFF000000u;
+    if (light < 1.0f) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint32_t c = (color >> (8 * k)) & 0xFFu;
+            out |= ((uint32_t)f2i((float)c * light) & 0xFFu) << (8 * k);
+        }
+    } else {
+        light = sqrtf(light);
+        light = sqrtf(light);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint32_t c = (color >> (8 * k)) & 0xFFu;
+            const uint32_t q = (uint32_t)f2i((float)(255u - c) / light) & 0xFFu;
+            out |= ((255u - q) & 0xFFu) << (8 * k);
+        }
+    }
+    return out;
+}
+
+
+} // namespace sgl

@@ -53,6 +53,8 @@ def library() -> C.CDLL:
                             P(abi.FrameStats)], C.c_int),
             "sgl_render_debug": ([C.c_void_p, C.c_int, P(abi.ViewDesc), P(abi.Target), P(C.c_uint32), P(C.c_uint8),
                                   P(abi.FrameStats)], C.c_int),
+            "sgl_profile": ([C.c_void_p, C.c_int], C.c_int),
+            "sgl_profile_read": ([C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_uint64)], C.c_int),
         }
         for name, (args, res) in sigs.items():
             fn = getattr(lib, name)
@@ -146,6 +148,23 @@ class Renderer:
                                               winner.ctypes.data_as(C.POINTER(C.c_uint32)),
                                               flags.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(fs)))
         return frame, winner, flags, _stats_dict(fs)
+
+    # per-kernel device timing ----------------------------------------------
+    def profile(self, enable: bool = True):
+        self._check(self.lib.sgl_profile(self.ctx, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        out = {}
+        k = 0
+        while True:
+            name, ms, n = C.c_char_p(), C.c_double(), C.c_uint64()
+            st = self.lib.sgl_profile_read(self.ctx, k, C.byref(name), C.byref(ms), C.byref(n))
+            if st == -4:
+                break
+            self._check(st)
+            out[name.value.decode()] = {"total_ms": ms.value, "launches": n.value}
+            k += 1
+        return out
 
 
 def _stats_dict(fs: abi.FrameStats) -> dict:
