@@ -211,6 +211,32 @@ SGL_API sgl_status sgl_render(sgl_ctx *ctx, int scene_id, const sgl_view *views,
 SGL_API sgl_status sgl_render_debug(sgl_ctx *ctx, int scene_id, const sgl_view *view, const sgl_target *target,
                                     uint32_t *winner, uint8_t *slot_flags, sgl_frame_stats *stats);
 
+/* ------------------------------------------------------------- batching -- */
+
+/* Batched renderer: many views, of one or several resident scenes and of
+ * uneven sizes, rendered by one launch sequence (one CUDA graph launch when
+ * use_graph is set).  Targets are device buffers and must not overlap.
+ * Replaces a loop of swegl::_render calls (src/render/renderer.cpp:77-235)
+ * over independent viewports. */
+typedef struct sgl_batch_opts {
+    int tile;      /* shade tile edge: 8, 16 or 32 pixels (0 = context default) */
+    int span_bin;  /* spans wider than this many pixels are binned to the
+                      warp-cooperative span kernels (1..64, 0 = default 16) */
+    int use_graph; /* run the launch sequence as a captured CUDA graph */
+} sgl_batch_opts;
+
+typedef struct sgl_batch_item {
+    int        scene_id;
+    sgl_view   view;
+    sgl_target target; /* device buffers */
+} sgl_batch_item;
+
+/* Asynchronous on `stream` unless `stats` is requested (then it waits). */
+SGL_API sgl_status sgl_render_batch(sgl_ctx *ctx, const sgl_batch_item *items, int n_items,
+                                    const sgl_batch_opts *opts, void *stream, sgl_frame_stats *stats);
+/* Times every tile x span_bin choice on this batch and returns the fastest. */
+SGL_API sgl_status sgl_autotune(sgl_ctx *ctx, const sgl_batch_item *items, int n_items, sgl_batch_opts *chosen);
+
 /* Per-kernel device timing (CUDA events on the launching stream around each
  * kernel of every frame rendered while enabled).  Enabling resets the totals.
  * Kernels are numbered 0..n-1; reading past the last returns SGL_ERR_NOT_FOUND.

@@ -76,7 +76,7 @@ class FrameStats(C.Structure):
 
 
 class BatchOpts(C.Structure):
-    _fields_ = [("tile", C.c_int), ("bin_capacity", C.c_int), ("use_graph", C.c_int)]
+    _fields_ = [("tile", C.c_int), ("span_bin", C.c_int), ("use_graph", C.c_int)]
 
 
 class BatchItem(C.Structure):

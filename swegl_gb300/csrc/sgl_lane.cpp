@@ -1,0 +1,251 @@
+// sgl_lane.cpp — batches of views on one stream: descriptor staging, scratch
+// pools, the launch sequence and its CUDA graphs.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "sgl.h"
+#include "sgl_internal.h"
+#include "sgl_runtime.h"
+
+namespace sgl {
+
+HostBuf::~HostBuf()
+{
+    if (ptr)
+        cudaFreeHost(ptr);
+}
+
+cudaError_t HostBuf::ensure(size_t need)
+{
+    if (need <= bytes && ptr)
+        return cudaSuccess;
+    if (ptr)
+        cudaFreeHost(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    size_t n = std::max<size_t>(need, 256);
+    cudaError_t e = cudaHostAlloc(&ptr, n, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        return e;
+    }
+    bytes = n;
+    return cudaSuccess;
+}
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+size_t view_scratch_bytes(uint32_t n_vertices, uint32_t n_triangles, int w, int h)
+{
+    const size_t px = (size_t)w * h;
+    return align_up(16 * (size_t)n_vertices, 256) + align_up(n_vertices, 256) + 8 * px + 16 * px  // ndc yes key prec
+           + 8 * (size_t)n_triangles + 8 * px + sizeof(SpanRec) * (px / 8 + 64);                   // lists, bins
+}
+
+Lane::~Lane()
+{
+    for (auto &sl : slots) {
+        for (auto &g : sl.graph)
+            if (g)
+                cudaGraphExecDestroy(g);
+        if (sl.staged)
+            cudaEventDestroy(sl.staged);
+        if (sl.done)
+            cudaEventDestroy(sl.done);
+    }
+    if (own_stream && stream)
+        cudaStreamDestroy(stream);
+    if (capture_stream)
+        cudaStreamDestroy(capture_stream);
+}
+
+sgl_status Lane::init(Ctx *ctx, int max_items_, cudaStream_t external)
+{
+    max_items = max_items_;
+    if (external) {
+        stream = external;
+        own_stream = false;
+    } else {
+        CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = true;
+    }
+    for (auto &sl : slots) {
+        CUDA_TRY(sl.d_items.ensure(sizeof(ItemDev) * (size_t)max_items));
+        CUDA_TRY(sl.d_bases.ensure(sizeof(uint32_t) * 4 * ((size_t)max_items + 1)));
+        CUDA_TRY(sl.d_batch.ensure(sizeof(BatchDev)));
+        CUDA_TRY(sl.d_counters.ensure(sizeof(unsigned long long) * kCounterWords));
+        CUDA_TRY(sl.d_item_counters.ensure(2 * sizeof(unsigned long long) * (size_t)max_items));
+        CUDA_TRY(sl.h_items.ensure(sizeof(ItemDev) * (size_t)max_items));
+        CUDA_TRY(sl.h_bases.ensure(sizeof(uint32_t) * 4 * ((size_t)max_items + 1)));
+        CUDA_TRY(sl.h_batch.ensure(sizeof(BatchDev)));
+        CUDA_TRY(sl.h_counters.ensure(sizeof(unsigned long long) * (kCounterWords + 2 * (size_t)max_items)));
+        CUDA_TRY(cudaEventCreateWithFlags(&sl.staged, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+    }
+    return SGL_OK;
+}
+
+sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inline_span, uint8_t *slot_flags,
+                         int *slot_out)
+{
+    if (n <= 0 || n > max_items) {
+        ctx->fail("batch of %d views; this lane takes 1..%d", n, max_items);
+        return SGL_ERR_INVALID;
+    }
+    const int si = next;
+    next = (next + 1) % kSlots;
+    Slot &sl = slots[si];
+    if (sl.used)
+        CUDA_TRY(cudaEventSynchronize(sl.done)); // its staging buffers are free again
+    // prefixes and pool offsets
+    uint32_t *hb = (uint32_t *)sl.h_bases.ptr;
+    uint32_t *vb = hb, *tb = hb + (n + 1), *pb = hb + 2 * (n + 1), *gb = hb + 3 * (n + 1);
+    uint64_t tv = 0, tt = 0, tp = 0, tg = 0;
+    size_t ndc_off = 0, yes_off = 0;
+    std::vector<size_t> ndc_at(n), yes_at(n);
+    for (int i = 0; i < n; i++) {
+        const Scene &s = *e[i].scene;
+        const sgl_view &v = e[i].view;
+        vb[i] = (uint32_t)tv;
+        tb[i] = (uint32_t)tt;
+        pb[i] = (uint32_t)tp;
+        gb[i] = (uint32_t)tg;
+        tv += s.n_vertices;
+        tt += s.n_triangles;
+        tp += (uint64_t)v.w * v.h;
+        tg += (uint64_t)((v.w + tile - 1) / tile) * (uint64_t)((v.h + tile - 1) / tile);
+        ndc_at[i] = ndc_off;
+        yes_at[i] = yes_off;
+        ndc_off += align_up(s.n_vertices, 16);
+        yes_off += align_up(s.n_vertices, 256);
+    }
+    if (tv >= (1ull << 32) || tt >= (1ull << 31) || tp >= (1ull << 32) || tg >= (1ull << 32)) {
+        ctx->fail("batch too large (%llu vertices, %llu triangles, %llu pixels)", (unsigned long long)tv,
+                  (unsigned long long)tt, (unsigned long long)tp);
+        return SGL_ERR_UNSUPPORTED;
+    }
+    vb[n] = (uint32_t)tv;
+    tb[n] = (uint32_t)tt;
+    pb[n] = (uint32_t)tp;
+    gb[n] = (uint32_t)tg;
+    const size_t span_cap = std::max<size_t>(65536, tp / 8);
+    CUDA_TRY(ndc.ensure(sizeof(float4) * std::max<size_t>(ndc_off, 1)));
+    CUDA_TRY(yes.ensure(std::max<size_t>(yes_off, 1)));
+    CUDA_TRY(key.ensure(sizeof(unsigned long long) * std::max<uint64_t>(tp, 1)));
+    CUDA_TRY(prec.ensure(sizeof(float4) * std::max<uint64_t>(tp, 1)));
+    CUDA_TRY(list.ensure(sizeof(uint2) * std::max<uint64_t>(tt, 1)));
+    CUDA_TRY(clippx.ensure(sizeof(uint2) * std::max<uint64_t>(tp, 1)));
+    CUDA_TRY(spans.ensure(sizeof(SpanRec) * span_cap));
+    ItemDev *hi = (ItemDev *)sl.h_items.ptr;
+    for (int i = 0; i < n; i++) {
+        const BatchEntry &en = e[i];
+        ItemDev it{};
+        it.s = en.scene->dev;
+        it.v = make_view(en.view);
+        it.ndc = (float4 *)ndc.ptr + ndc_at[i];
+        it.yes = (uint8_t *)yes.ptr + yes_at[i];
+        it.key = (unsigned long long *)key.ptr + pb[i];
+        it.prec = (float4 *)prec.ptr + pb[i];
+        it.pixels = en.rect_pixels;
+        it.pitch_px = en.pitch_px;
+        it.zbuf = en.zbuf;
+        it.tiles_x = (en.view.w + tile - 1) / tile;
+        it.tile_base = gb[i];
+        hi[i] = it;
+    }
+    BatchDev *hbd = (BatchDev *)sl.h_batch.ptr;
+    BatchDev bd{};
+    bd.items = (const ItemDev *)sl.d_items.ptr;
+    const uint32_t *db = (const uint32_t *)sl.d_bases.ptr;
+    bd.vtx_base = db;
+    bd.tri_base = db + (n + 1);
+    bd.px_base = db + 2 * (n + 1);
+    bd.tile_base = db + 3 * (n + 1);
+    bd.n_items = n;
+    bd.inline_span = inline_span;
+    bd.total_vtx = (uint32_t)tv;
+    bd.total_tri = (uint32_t)tt;
+    bd.total_px = (uint32_t)tp;
+    bd.total_tiles = (uint32_t)tg;
+    bd.list = (uint2 *)list.ptr;
+    bd.list_cap = (uint32_t)std::max<uint64_t>(tt, 1);
+    bd.clip = (uint2 *)list.ptr; // shares the list buffer, filled from its end
+    bd.clip_cap = bd.list_cap;
+    bd.clippx = (uint2 *)clippx.ptr;
+    bd.clippx_cap = (uint32_t)std::max<uint64_t>(tp, 1);
+    bd.spans = (SpanRec *)spans.ptr;
+    bd.span_cap = (uint32_t)std::min<size_t>(spans.bytes / sizeof(SpanRec), 0xFFFFFFFFu);
+    bd.counters = (unsigned long long *)sl.d_counters.ptr;
+    bd.item_counters = (unsigned long long *)sl.d_item_counters.ptr;
+    bd.slot_flags = slot_flags;
+    *hbd = bd;
+    CUDA_TRY(cudaMemcpyAsync(sl.d_items.ptr, hi, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(sl.d_bases.ptr, hb, sizeof(uint32_t) * 4 * (n + 1), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(sl.d_batch.ptr, hbd, sizeof(BatchDev), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemsetAsync(sl.d_counters.ptr, 0, sizeof(unsigned long long) * kCounterWords, stream));
+    CUDA_TRY(cudaMemsetAsync(sl.d_item_counters.ptr, 0, 2 * sizeof(unsigned long long) * n, stream));
+    CUDA_TRY(cudaEventRecord(sl.staged, stream));
+    sl.used = true;
+    sl.n_items = n;
+    *slot_out = si;
+    return SGL_OK;
+}
+
+static int tile_index(int tile) { return tile == 8 ? 0 : (tile == 32 ? 2 : 1); }
+
+sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launches, Profiler *prof)
+{
+    Slot &sl = slots[si];
+    const BatchDev *db = (const BatchDev *)sl.d_batch.ptr;
+    if (use_graph) {
+        cudaGraphExec_t &g = sl.graph[tile_index(tile)];
+        if (!g) {
+            // captured on a private stream (the caller's may be the legacy
+            // default stream, which cannot be captured), launched on the caller's
+            if (!capture_stream)
+                CUDA_TRY(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking));
+            cudaGraph_t graph = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal));
+            int dummy = 0;
+            cudaError_t le = launch_batch(db, tile, capture_stream, &dummy, nullptr);
+            cudaError_t ce = cudaStreamEndCapture(capture_stream, &graph);
+            CUDA_TRY(le);
+            CUDA_TRY(ce);
+            cudaError_t ie = cudaGraphInstantiate(&g, graph, 0);
+            cudaGraphDestroy(graph);
+            CUDA_TRY(ie);
+        }
+        CUDA_TRY(cudaGraphLaunch(g, stream));
+        if (launches)
+            *launches += 1;
+    } else {
+        CUDA_TRY(launch_batch(db, tile, stream, launches, prof));
+    }
+    unsigned long long *hc = (unsigned long long *)sl.h_counters.ptr;
+    CUDA_TRY(cudaMemcpyAsync(hc, sl.d_counters.ptr, sizeof(unsigned long long) * kCounterWords,
+                             cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(hc + kCounterWords, sl.d_item_counters.ptr,
+                             2 * sizeof(unsigned long long) * sl.n_items, cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaEventRecord(sl.done, stream));
+    return SGL_OK;
+}
+
+sgl_status Lane::read_counters(Ctx *ctx, int si, unsigned long long *drawn, unsigned long long *fragments,
+                               std::vector<unsigned long long> *per_item)
+{
+    Slot &sl = slots[si];
+    CUDA_TRY(cudaEventSynchronize(sl.done));
+    const unsigned long long *hc = (const unsigned long long *)sl.h_counters.ptr;
+    if (drawn)
+        *drawn = hc[C_DRAWN];
+    if (fragments)
+        *fragments = hc[C_FRAGMENTS];
+    if (per_item)
+        per_item->assign(hc + kCounterWords, hc + kCounterWords + 2 * sl.n_items);
+    return SGL_OK;
+}
+
+} // namespace sgl

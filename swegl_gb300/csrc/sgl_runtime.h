@@ -13,6 +13,17 @@
 
 namespace sgl {
 
+constexpr int kMaxBatch = 4096; // views per batch
+
+#define CUDA_TRY(expr)                                                                                                 \
+    do {                                                                                                               \
+        cudaError_t _e = (expr);                                                                                       \
+        if (_e != cudaSuccess) {                                                                                       \
+            ctx->fail("%s: %s", #expr, cudaGetErrorString(_e));                                                        \
+            return _e == cudaErrorMemoryAllocation ? SGL_ERR_OOM : SGL_ERR_CUDA;                                       \
+        }                                                                                                              \
+    } while (0)
+
 // A grow-only device allocation.
 struct DevBuf {
     void *ptr = nullptr;
@@ -25,10 +36,15 @@ struct DevBuf {
     void release();
 };
 
-// Per-view scratch reused across frames: vertex NDC, visibility flags,
-// per-pixel depth keys and the frame counters.
-struct FrameScratch {
-    DevBuf ndc, yes, key, prec, classes, cliptri, clippx, spans, counters;
+// A pinned host allocation.
+struct HostBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    HostBuf() = default;
+    HostBuf(const HostBuf &) = delete;
+    HostBuf &operator=(const HostBuf &) = delete;
+    ~HostBuf();
+    cudaError_t ensure(size_t need);
 };
 
 struct Ctx;
@@ -36,7 +52,7 @@ struct Ctx;
 // A scene resident in device memory.
 struct Scene {
     DevBuf d_pos_u, d_nrm_v, d_vnode, d_tris, d_prims, d_mats, d_texs, d_texels, d_wpos, d_wnrm, d_uv,
-        d_node_world, d_node_rs;
+        d_node_world, d_node_rs, d_lights;
     SceneDev dev{};
     LightsDev lights{};
     std::vector<sgl_node_desc> nodes;
@@ -50,15 +66,66 @@ struct Scene {
                           int n);
 };
 
+// One view of a batch on the host side: its scene, camera and device buffers.
+struct BatchEntry {
+    Scene *scene;
+    sgl_view view;
+    uint32_t *rect_pixels; // device, at the viewport's top-left pixel
+    int pitch_px;
+    float *zbuf;           // device, w*h, may be null
+};
+
+// Scratch bytes a view needs beyond its output buffers: vertex NDC and flags,
+// per-pixel keys and winner records, and its share of the batch lists.
+size_t view_scratch_bytes(uint32_t n_vertices, uint32_t n_triangles, int w, int h);
+
+// A stream with everything a batch launch sequence needs.  Descriptors are
+// staged in pinned memory and copied per batch; a ring of staging slots lets
+// several batches be queued on the stream.  The device buffers that the
+// launch sequence names directly (descriptors, counters) never move, so a
+// captured CUDA graph stays valid; the pools they point to may grow.
+struct Lane {
+    static constexpr int kSlots = 4;
+    int max_items = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    bool own_stream = false;
+    struct Slot {
+        DevBuf d_items, d_bases, d_batch, d_counters, d_item_counters;
+        HostBuf h_items, h_bases, h_batch, h_counters;
+        cudaEvent_t staged = nullptr; // staging copies of this slot done
+        cudaEvent_t done = nullptr;   // launch sequence of this slot done
+        bool used = false;
+        cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr}; // per tile 8/16/32
+        int n_items = 0;
+    } slots[kSlots];
+    int next = 0;
+    DevBuf list, clip, clippx, spans, ndc, yes, key, prec;
+    ~Lane();
+
+    sgl_status init(Ctx *ctx, int max_items, cudaStream_t external);
+    // Stage and copy the descriptors of a batch into a free slot; returns its index.
+    sgl_status prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inline_span, uint8_t *slot_flags,
+                       int *slot_out);
+    // Run the launch sequence of a prepared slot (directly, or as a CUDA graph).
+    sgl_status launch(Ctx *ctx, int slot, int tile, bool use_graph, int *launches, Profiler *prof);
+    // Per-batch and per-item counters of a finished slot (synchronises the slot).
+    sgl_status read_counters(Ctx *ctx, int slot, unsigned long long *drawn, unsigned long long *fragments,
+                             std::vector<unsigned long long> *per_item);
+};
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string last_error;
     std::map<int, std::unique_ptr<Scene>> scenes;
     int next_scene_id = 1;
-    FrameScratch frame;
+    std::unique_ptr<Lane> lane;        // the plain renderer's lane (internal stream)
+    std::unique_ptr<Lane> ext_lane;    // lane bound to caller streams
     DevBuf stage_pixels, stage_z, debug_flags;
     Profiler prof;
+    int tile = 16;                     // shade tile of the plain renderer
+    int inline_span = 16;              // long-span bin threshold of the plain renderer
 
     void fail(const char *fmt, ...) __attribute__((format(printf, 2, 3)));
     Scene *find(int id)
@@ -70,8 +137,5 @@ struct Ctx {
 
 ViewDev make_view(const sgl_view &v);
 sgl_status check_view(Ctx *ctx, const sgl_view &v, const sgl_target &t);
-sgl_status render_view_device(Ctx *ctx, Scene &s, const sgl_view &view, uint32_t *rect_pixels, int pitch_px,
-                              float *zbuf, FrameScratch &fs, cudaStream_t st, uint8_t *slot_flags, int *launches,
-                              Profiler *prof = nullptr);
 
 } // namespace sgl

@@ -54,6 +54,9 @@ def library() -> C.CDLL:
             "sgl_render_debug": ([C.c_void_p, C.c_int, P(abi.ViewDesc), P(abi.Target), P(C.c_uint32), P(C.c_uint8),
                                   P(abi.FrameStats)], C.c_int),
             "sgl_profile": ([C.c_void_p, C.c_int], C.c_int),
+            "sgl_render_batch": ([C.c_void_p, P(abi.BatchItem), C.c_int, P(abi.BatchOpts), C.c_void_p,
+                                  P(abi.FrameStats)], C.c_int),
+            "sgl_autotune": ([C.c_void_p, P(abi.BatchItem), C.c_int, P(abi.BatchOpts)], C.c_int),
             "sgl_profile_read": ([C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_uint64)], C.c_int),
         }
         for name, (args, res) in sigs.items():
@@ -148,6 +151,31 @@ class Renderer:
                                               winner.ctypes.data_as(C.POINTER(C.c_uint32)),
                                               flags.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(fs)))
         return frame, winner, flags, _stats_dict(fs)
+
+    # batches --------------------------------------------------------------
+    def render_batch(self, items, tile: int = 0, span_bin: int = 0, use_graph: bool = True, stream: int = 0,
+                     stats: bool = False):
+        """items: list of (scene_id, view, abi.Target with device pointers)."""
+        arr = (abi.BatchItem * len(items))()
+        for i, (sid, v, t) in enumerate(items):
+            arr[i].scene_id = sid
+            arr[i].view = abi.view_desc(v)
+            arr[i].target = t
+        opts = abi.BatchOpts(tile, span_bin, 1 if use_graph else 0)
+        fs = abi.FrameStats()
+        self._check(self.lib.sgl_render_batch(self.ctx, arr, len(items), C.byref(opts), C.c_void_p(stream),
+                                              C.byref(fs) if stats else None))
+        return _stats_dict(fs) if stats else None
+
+    def autotune(self, items) -> dict:
+        arr = (abi.BatchItem * len(items))()
+        for i, (sid, v, t) in enumerate(items):
+            arr[i].scene_id = sid
+            arr[i].view = abi.view_desc(v)
+            arr[i].target = t
+        opts = abi.BatchOpts()
+        self._check(self.lib.sgl_autotune(self.ctx, arr, len(items), C.byref(opts)))
+        return {"tile": opts.tile, "span_bin": opts.span_bin, "use_graph": opts.use_graph}
 
     # per-kernel device timing ----------------------------------------------
     def profile(self, enable: bool = True):
