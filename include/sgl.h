@@ -237,6 +237,62 @@ SGL_API sgl_status sgl_render_batch(sgl_ctx *ctx, const sgl_batch_item *items, i
 /* Times every tile x span_bin choice on this batch and returns the fastest. */
 SGL_API sgl_status sgl_autotune(sgl_ctx *ctx, const sgl_batch_item *items, int n_items, sgl_batch_opts *chosen);
 
+/* ------------------------------------------------------- depth of field -- */
+
+/* The depth-of-field gather alone on a rendered view (replaces
+ * post_shader_t::shade / post_shader_depth_box::shade,
+ * swegl/render/post_shaders.hpp:33-132, whose own output is not usable: it
+ * reads a z-buffer the opaque path never writes).  `in` holds the view's
+ * colour rectangle and z-buffer, `out` receives the gathered colour in its
+ * rectangle.  Per pixel: view depth z = (z' - P23) / P22 from the z-buffer,
+ * circle of confusion r = K * aperture * |z - focus| / z pixels (K =
+ * px_scale, or P11 * h / 2 when 0) clamped to [0, max_radius], and the mean of
+ * the 32 taps of sgl_dof_taps.h at offsets roundf(r * tap) clamped to the
+ * view, integer sums rounded half up; alpha is kept.  sgl_render applies the
+ * same gather to every view whose dof.enabled is set. */
+SGL_API sgl_status sgl_dof(sgl_ctx *ctx, const sgl_view *view, const sgl_target *in, const sgl_target *out,
+                           int device_buffers, void *stream);
+
+/* -------------------------------------------------------------- serving -- */
+
+/* A request loop that keeps scenes resident, admits render requests of any
+ * scene and viewport size against a device-memory budget (framebuffer +
+ * scratch bytes), batches them as they arrive and keeps several batches in
+ * flight on separate streams (continuous batching).  No reference
+ * counterpart: the reference renders one frame per call of
+ * swegl::render (src/test_1.cpp:365-376). */
+typedef struct sgl_server sgl_server;
+
+typedef struct sgl_serve_opts {
+    uint64_t budget_bytes; /* device bytes admitted at once (0 = 40 GiB) */
+    int      max_batch;    /* views per batch (0 = 64) */
+    int      streams;      /* batches in flight (0 = 3) */
+    int      copy_out;     /* 1 = copy each frame to the request's host buffers */
+} sgl_serve_opts;
+
+typedef struct sgl_request {
+    int       scene_id;
+    sgl_view  view;          /* x, y ignored: the frame is w x h */
+    uint32_t *host_pixels;   /* w*h BGRA8, written when copy_out (may be NULL) */
+    float    *host_zbuffer;  /* w*h depth, written when copy_out (may be NULL) */
+} sgl_request;
+
+typedef struct sgl_request_result {
+    sgl_status status;
+    double     submit_s, start_s, done_s; /* steady host clock, seconds */
+    uint64_t   fragments;                 /* covered (triangle, pixel) pairs */
+} sgl_request_result;
+
+SGL_API sgl_status sgl_server_create(sgl_ctx *ctx, const sgl_serve_opts *opts, sgl_server **out);
+/* Queue a request; SGL_ERR_BUDGET when it alone exceeds the budget. */
+SGL_API sgl_status sgl_server_submit(sgl_server *srv, const sgl_request *req, uint64_t *ticket);
+/* SGL_OK with the result (once per ticket), SGL_ERR_BUSY while in flight. */
+SGL_API sgl_status sgl_server_poll(sgl_server *srv, uint64_t ticket, sgl_request_result *result);
+SGL_API sgl_status sgl_server_wait(sgl_server *srv, uint64_t ticket, double timeout_s, sgl_request_result *result);
+/* Wait until every submitted request is done (SGL_ERR_TIMEOUT otherwise). */
+SGL_API sgl_status sgl_server_drain(sgl_server *srv, double timeout_s);
+SGL_API void       sgl_server_destroy(sgl_server *srv);
+
 /* Per-kernel device timing (CUDA events on the launching stream around each
  * kernel of every frame rendered while enabled).  Enabling resets the totals.
  * Kernels are numbered 0..n-1; reading past the last returns SGL_ERR_NOT_FOUND.

@@ -47,6 +47,7 @@ def restatement() -> C.CDLL:
         lib.orc_render.restype = C.c_int
         lib.orc_render_parallel.restype = C.c_int
         lib.orc_triangle_count.restype = C.c_uint64
+        lib.orc_dof.restype = C.c_int
         _libs["orc"] = lib
     return _libs["orc"]
 
@@ -121,3 +122,19 @@ def render_parallel(scene, views, threads: int) -> list:
     if rc != 0:
         raise RuntimeError(f"parallel oracle render failed ({rc})")
     return frames
+
+
+def dof(view, pixels: np.ndarray, zbuffer: np.ndarray) -> np.ndarray:
+    """The depth-of-field gather on a (h, w) uint32 frame and its z-buffer."""
+    h, w = pixels.shape
+    src = np.ascontiguousarray(pixels, np.uint32)
+    z = np.ascontiguousarray(zbuffer, np.float32)
+    out = np.zeros_like(src)
+    vd = abi.view_desc(view)
+    vd.x = vd.y = 0
+    t_in = abi.Target(src.ctypes.data, 4 * w, w, h, z.ctypes.data_as(C.POINTER(C.c_float)))
+    t_out = abi.Target(out.ctypes.data, 4 * w, w, h, None)
+    rc = restatement().orc_dof(C.byref(vd), C.byref(t_in), C.byref(t_out))
+    if rc != 0:
+        raise RuntimeError("oracle dof failed")
+    return out

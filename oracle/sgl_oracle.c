@@ -19,6 +19,12 @@
  * One extension: the point-light specular exponent comes from the material
  * (sgl_material_desc::shininess); the reference hard-codes 32
  * (src/render/pixel_shaders.cpp:192) and golden scenes use 32.
+ *
+ * The depth-of-field gather (orc_dof) is not the reference's: its
+ * post_shader_depth_box (swegl/render/post_shaders.hpp:51-132) reads a
+ * z-buffer the opaque path never writes and indexes past its source row.  It
+ * is the CPU oracle of the gather specified in include/sgl.h (sgl_dof) with
+ * the tap table of include/sgl_dof_taps.h.
  */
 #include <math.h>
 #include <pthread.h>
@@ -27,6 +33,7 @@
 #include <string.h>
 
 #include "sgl.h"
+#include "sgl_dof_taps.h"
 
 #define ORC_API __attribute__((visibility("default")))
 
@@ -857,11 +864,78 @@ static int render_view(const oscene *s, const sgl_view *view, const sgl_target *
     return 0;
 }
 
+/* --------------------------------------------------------- depth of field -- */
+
+/* The depth-of-field gather of include/sgl.h (sgl_dof): src/out are the view's
+ * colour (pitches in pixels), z its z-buffer (w*h). */
+static void dof_gather(const sgl_view *view, const uint32_t *src, int src_pitch, const float *z, uint32_t *out,
+                       int out_pitch)
+{
+    const int w = view->w, h = view->h;
+    const float k = view->dof.px_scale > 0.0f ? view->dof.px_scale : (view->proj[5] * (float)h) / 2.0f;
+    const float ka = k * view->dof.aperture;
+    const float p22 = view->proj[10], p23 = view->proj[11];
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const float zp = z[(long)y * w + x];
+            const float zv = (zp - p23) / p22;
+            float r = (ka * fabsf(zv - view->dof.focus)) / zv;
+            if (!(r >= 0.0f && r <= view->dof.max_radius))
+                r = view->dof.max_radius;
+            uint32_t sb = 0, sg = 0, sr = 0;
+            for (int t = 0; t < SGL_DOF_TAPS; t++) {
+                int sx = x + (int)roundf(r * sgl_dof_taps[t][0]);
+                int sy = y + (int)roundf(r * sgl_dof_taps[t][1]);
+                sx = sx < 0 ? 0 : (sx >= w ? w - 1 : sx);
+                sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
+                const uint32_t c = src[(long)sy * src_pitch + sx];
+                sb += c & 0xFFu;
+                sg += (c >> 8) & 0xFFu;
+                sr += (c >> 16) & 0xFFu;
+            }
+            const uint32_t centre = src[(long)y * src_pitch + x];
+            out[(long)y * out_pitch + x] = (centre & 0xFF000000u) | (((sr + 16u) / 32u) << 16) |
+                                           (((sg + 16u) / 32u) << 8) | ((sb + 16u) / 32u);
+        }
+}
+
+/* The gather alone on host buffers: `in` holds the view's colour rectangle and
+ * z-buffer, `out` receives the result in its rectangle. */
+ORC_API int orc_dof(const sgl_view *view, const sgl_target *in, const sgl_target *out)
+{
+    if (!view || !in || !out || !in->zbuffer || view->w <= 0 || view->h <= 0)
+        return -1;
+    const int ip = in->pitch / 4, op = out->pitch / 4;
+    const uint32_t *src = (const uint32_t *)in->pixels + (long)view->y * ip + view->x;
+    uint32_t *dst = (uint32_t *)out->pixels + (long)view->y * op + view->x;
+    dof_gather(view, src, ip, in->zbuffer, dst, op);
+    return 0;
+}
+
+/* After render_view: the gather over the view's own rectangle when enabled. */
+static int apply_dof(const sgl_view *view, const sgl_target *target)
+{
+    if (!view->dof.enabled || !target->zbuffer)
+        return 0;
+    const int p = target->pitch / 4;
+    const size_t px = (size_t)view->w * view->h;
+    uint32_t *tmp = (uint32_t *)malloc(4 * px);
+    if (!tmp)
+        return -1;
+    uint32_t *rect = (uint32_t *)target->pixels + (long)view->y * p + view->x;
+    for (int y = 0; y < view->h; y++)
+        memcpy(tmp + (size_t)y * view->w, rect + (long)y * p, 4 * (size_t)view->w);
+    dof_gather(view, tmp, view->w, target->zbuffer, rect, p);
+    free(tmp);
+    return 0;
+}
+
 /* ------------------------------------------------------------------- API -- */
 
 /* Render views in order, as swegl::render(scene, vp0, vp1, ...) does.
- * kind: 0 Phong + bilinear, 1 winner ordinal, 2 progress bits, 3 Phong light
- * int, 4 bilinear texel.  winner_slot (view 0, may be NULL) receives
+ * kind: 0 Phong + bilinear (then the depth-of-field gather of views that
+ * enable it), 1 winner ordinal, 2 progress bits, 3 Phong light int, 4
+ * bilinear texel.  winner_slot (view 0, may be NULL) receives
  * 2 * triangle + sub-triangle of the pixel's winner.  stats (may be NULL)
  * receives [drawn, fragments, clip_one, clip_two] per view. */
 ORC_API int orc_render(const sgl_scene_desc *desc, const sgl_view *views, const sgl_target *targets, int n_views,
@@ -878,6 +952,8 @@ ORC_API int orc_render(const sgl_scene_desc *desc, const sgl_view *views, const 
     for (int i = 0; i < n_views && rc == 0; i++) {
         view_stats st;
         rc = render_view(&s, &views[i], &targets[i], kind, i == 0 ? winner_slot : NULL, &st);
+        if (rc == 0 && kind == 0)
+            rc = apply_dof(&views[i], &targets[i]);
         if (stats) {
             stats[4 * i] = st.drawn;
             stats[4 * i + 1] = st.fragments;
@@ -918,7 +994,7 @@ static void *par_worker(void *arg)
         pthread_mutex_unlock(&j->mu);
         if (i >= j->n)
             return NULL;
-        if (render_view(j->s, &j->views[i], &j->targets[i], 0, NULL, NULL))
+        if (render_view(j->s, &j->views[i], &j->targets[i], 0, NULL, NULL) || apply_dof(&j->views[i], &j->targets[i]))
             j->rc = -1;
     }
 }

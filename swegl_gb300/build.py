@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libsgl.so")
 
-SOURCES = ["raster.cu", "sgl_api.cpp", "sgl_scene.cpp", "sgl_lane.cpp"]
+SOURCES = ["raster.cu", "sgl_api.cpp", "sgl_scene.cpp", "sgl_lane.cpp", "sgl_serve.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -50,7 +50,8 @@ def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "sgl.h"), __file__]
+    inc = os.path.join(ROOT, "include")
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(inc, f) for f in os.listdir(inc)] + [__file__]
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
@@ -62,6 +63,7 @@ def build(force: bool = False) -> str:
         objs = list(ex.map(_compile, SOURCES))
     tmp = LIB + ".tmp"
     cmd = [nvcc(), ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl"]
+    # headers under include/ are dependencies too
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -16,6 +16,7 @@
 //   k_walk_winner winner records of every span, only after a bin overflow
 //   k_shade       per pixel: background or the winner's colour, and depth
 //   k_shade_clip  winners that belong to near-clipped triangles (rare)
+//   k_dof         depth-of-field gather of the items that ask for it
 //
 // Depth test.  The reference draws triangles in order and keeps a fragment
 // when z < zbuffer (strict, src/render/renderer.cpp:489-499), so the earliest
@@ -29,6 +30,7 @@
 #include <cstdint>
 
 #include "sgl_device.cuh"
+#include "sgl_dof_taps.h"
 #include "sgl_internal.h"
 #include "sgl_shade.cuh"
 
@@ -908,6 +910,49 @@ __global__ void __launch_bounds__(128) k_shade_clip(const BatchDev *b)
     }
 }
 
+// ------------------------------------------------------------ depth of field --
+
+__constant__ float2 c_dof_taps[SGL_DOF_TAPS];
+
+// Depth-of-field gather (replaces post_shader_depth_box,
+// swegl/render/post_shaders.hpp:51-132).  Per pixel: view-space depth from the
+// z-buffer, z = (z' - P23) / P22; circle of confusion r = K*A*|z - F| / z
+// pixels, clamped to [0, max]; the mean of 32 taps of the golden-angle
+// pattern (sgl_dof_taps.h) at offsets roundf(r * tap), clamped to the
+// viewport, with integer sums rounded half up.  Every step is exact integer
+// or IEEE float arithmetic, so the CPU oracle gives the same bits.
+__global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
+{
+    for_each_in_items(b, b->px_base, b->total_px, [&](int item, uint32_t i) {
+        const ItemDev &it = b->items[item];
+        if (!it.dof)
+            return;
+        const int w = it.v.w, h = it.v.h;
+        const int y = (int)(i / (uint32_t)w), x = (int)(i - (uint32_t)y * (uint32_t)w);
+        const float zp = it.zbuf[i];
+        const float zv = (zp - it.p23) / it.p22;
+        float r = (it.dof_ka * fabsf(zv - it.dof_focus)) / zv;
+        if (!(r >= 0.0f && r <= it.dof_rmax))
+            r = it.dof_rmax;
+        uint32_t sb = 0, sg = 0, sr = 0;
+#pragma unroll 8
+        for (int k = 0; k < SGL_DOF_TAPS; k++) {
+            const float2 t = c_dof_taps[k];
+            int sx = x + (int)roundf(r * t.x), sy = y + (int)roundf(r * t.y);
+            sx = sx < 0 ? 0 : (sx >= w ? w - 1 : sx);
+            sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
+            const uint32_t c = __ldg(it.pixels + (size_t)sy * it.pitch_px + sx);
+            sb += c & 0xFFu;
+            sg += (c >> 8) & 0xFFu;
+            sr += (c >> 16) & 0xFFu;
+        }
+        const uint32_t centre = it.pixels[(size_t)y * it.pitch_px + x];
+        const uint32_t out = (centre & 0xFF000000u) | (((sr + 16u) / 32u) << 16) | (((sg + 16u) / 32u) << 8) |
+                             ((sb + 16u) / 32u);
+        it.dof_out[(size_t)y * it.dof_pitch + x] = out;
+    });
+}
+
 // ---------------------------------------------------------------- launches --
 
 static inline unsigned grid_for(uint64_t n, int block) { return (unsigned)((n + block - 1) / block); }
@@ -934,8 +979,9 @@ cudaError_t launch_world(const SceneDev &s, cudaStream_t st)
 
 const char *prof_kernel_name(int k)
 {
-    static const char *names[kProfKernels] = {"k_clear", "k_vertex", "k_flags", "k_compact",
-                                              "k_walk+clip", "k_spans", "winner records", "k_shade"};
+    static const char *names[kProfKernels] = {"k_clear",  "k_vertex",       "k_flags",
+                                              "k_compact", "k_walk+clip",   "k_spans",
+                                              "winner records", "k_shade", "k_dof"};
     return (k >= 0 && k < kProfKernels) ? names[k] : "?";
 }
 
@@ -961,7 +1007,23 @@ void prof_flush(Profiler *p) { prof_collect(p); }
 
 // The fixed launch sequence of a batch.  Grids do not depend on the batch:
 // every kernel strides over totals it reads from device memory.
-cudaError_t launch_batch(const BatchDev *b, int tile, cudaStream_t st, int *launches, Profiler *prof)
+// Constant tables of the current device (the depth-of-field taps); called
+// before any launch or graph capture on that device.
+cudaError_t init_device_constants()
+{
+    float2 taps[SGL_DOF_TAPS];
+    for (int k = 0; k < SGL_DOF_TAPS; k++)
+        taps[k] = make_float2(sgl_dof_taps[k][0], sgl_dof_taps[k][1]);
+    return cudaMemcpyToSymbol(c_dof_taps, taps, sizeof taps);
+}
+
+cudaError_t launch_dof(const BatchDev *b, cudaStream_t st)
+{
+    k_dof<<<sm_count() * 8, 256, 0, st>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t st, int *launches, Profiler *prof)
 {
     const bool timed = prof && prof->enabled;
     if (timed) {
@@ -1009,6 +1071,11 @@ cudaError_t launch_batch(const BatchDev *b, int tile, cudaStream_t st, int *laun
         k_shade<16><<<sms * 8, 256, 0, st>>>(b);
     k_shade_clip<<<sms, 128, 0, st>>>(b);
     n += 2;
+    mark(PK_DOF);
+    if (any_dof) {
+        k_dof<<<sms * 8, 256, 0, st>>>(b);
+        n++;
+    }
     if (timed) {
         cudaEventRecord(prof->ev[kProfKernels], st);
         prof->pending = true;

@@ -480,6 +480,78 @@ SGL_API sgl_status sgl_autotune(sgl_ctx *c, const sgl_batch_item *items, int n_i
     return SGL_OK;
 }
 
+SGL_API sgl_status sgl_dof(sgl_ctx *c, const sgl_view *view, const sgl_target *in, const sgl_target *out,
+                           int device_buffers, void *stream)
+{
+    Ctx *ctx = reinterpret_cast<Ctx *>(c);
+    if (!ctx || !view || !in || !out || !in->zbuffer)
+        return SGL_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    sgl_status r = check_view(ctx, *view, *in);
+    if (r == SGL_OK)
+        r = check_view(ctx, *view, *out);
+    if (r != SGL_OK)
+        return r;
+    const sgl_view &v = *view;
+    const size_t px = (size_t)v.w * v.h;
+    cudaStream_t st = device_buffers ? (cudaStream_t)stream : ctx->stream;
+    uint32_t *src = nullptr, *dst = nullptr;
+    int src_pitch = 0, dst_pitch = 0;
+    float *z = nullptr;
+    if (device_buffers) {
+        src = (uint32_t *)in->pixels + (size_t)v.y * (in->pitch / 4) + v.x;
+        dst = (uint32_t *)out->pixels + (size_t)v.y * (out->pitch / 4) + v.x;
+        src_pitch = in->pitch / 4;
+        dst_pitch = out->pitch / 4;
+        z = in->zbuffer;
+    } else {
+        CUDA_TRY(ctx->dof_stage.ensure(12 * px));
+        src = (uint32_t *)ctx->dof_stage.ptr;
+        dst = src + px;
+        z = (float *)(dst + px);
+        src_pitch = dst_pitch = v.w;
+        CUDA_TRY(cudaMemcpy2DAsync(src, 4 * (size_t)v.w, (const uint8_t *)in->pixels + (size_t)v.y * in->pitch +
+                                                            4 * (size_t)v.x,
+                                   in->pitch, 4 * (size_t)v.w, v.h, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(z, in->zbuffer, 4 * px, cudaMemcpyHostToDevice, st));
+    }
+    ItemDev it{};
+    it.v = make_view(v);
+    it.pixels = src;
+    it.pitch_px = src_pitch;
+    it.zbuf = z;
+    it.dof = 1;
+    it.dof_out = dst;
+    it.dof_pitch = dst_pitch;
+    const float k = v.dof.px_scale > 0.0f ? v.dof.px_scale : (v.proj[5] * (float)v.h) / 2.0f;
+    it.dof_focus = v.dof.focus;
+    it.dof_ka = k * v.dof.aperture;
+    it.dof_rmax = v.dof.max_radius;
+    it.p22 = v.proj[10];
+    it.p23 = v.proj[11];
+    CUDA_TRY(ctx->dof_desc.ensure(sizeof(ItemDev) + sizeof(BatchDev) + 4 * sizeof(uint32_t)));
+    uint8_t *dd = (uint8_t *)ctx->dof_desc.ptr;
+    ItemDev *d_it = (ItemDev *)dd;
+    BatchDev *d_b = (BatchDev *)(dd + sizeof(ItemDev));
+    uint32_t *d_base = (uint32_t *)(dd + sizeof(ItemDev) + sizeof(BatchDev));
+    BatchDev b{};
+    b.items = d_it;
+    b.px_base = d_base;
+    b.n_items = 1;
+    b.total_px = (uint32_t)px;
+    const uint32_t base[2] = {0u, (uint32_t)px};
+    CUDA_TRY(cudaMemcpyAsync(d_it, &it, sizeof it, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_b, &b, sizeof b, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_base, base, sizeof base, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(launch_dof(d_b, st));
+    if (!device_buffers) {
+        CUDA_TRY(cudaMemcpy2DAsync((uint8_t *)out->pixels + (size_t)v.y * out->pitch + 4 * (size_t)v.x, out->pitch,
+                                   dst, 4 * (size_t)v.w, 4 * (size_t)v.w, v.h, cudaMemcpyDeviceToHost, st));
+    }
+    CUDA_TRY(cudaStreamSynchronize(st)); // the descriptors above live on this call's stack
+    return SGL_OK;
+}
+
 SGL_API sgl_status sgl_profile(sgl_ctx *c, int enable)
 {
     Ctx *ctx = reinterpret_cast<Ctx *>(c);

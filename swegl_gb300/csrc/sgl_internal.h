@@ -78,6 +78,12 @@ struct ItemDev {
     float *zbuf;             // view w*h depth (may be null)
     int tiles_x;             // shade tiles across the view
     uint32_t tile_base;      // first shade tile of this item in the batch
+    // depth-of-field gather (when dof != 0 the shade kernel writes `pixels`
+    // as a scratch colour buffer of pitch w, and the gather writes dof_out)
+    int dof;
+    float dof_focus, dof_ka, dof_rmax, p22, p23;
+    uint32_t *dof_out;
+    int dof_pitch;
 };
 
 // A span handed from the triangle walk to the long-span kernels: the qpixel
@@ -128,8 +134,8 @@ struct BatchDev {
 
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each stage of a launch sequence (enabled with sgl_profile).
-constexpr int kProfKernels = 8;
-enum ProfKernel { PK_CLEAR = 0, PK_VERTEX, PK_FLAGS, PK_COMPACT, PK_DEPTH, PK_SPANS, PK_WINNER, PK_SHADE };
+constexpr int kProfKernels = 9;
+enum ProfKernel { PK_CLEAR = 0, PK_VERTEX, PK_FLAGS, PK_COMPACT, PK_DEPTH, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF };
 struct Profiler {
     bool enabled = false;
     cudaEvent_t ev[kProfKernels + 1] = {};
@@ -143,6 +149,11 @@ void prof_flush(Profiler *p);
 // kernel launchers (raster.cu)
 cudaError_t launch_world(const SceneDev &s, cudaStream_t st);
 // The launch sequence of a batch whose BatchDev lives at `b` (device memory).
-cudaError_t launch_batch(const BatchDev *b, int tile, cudaStream_t st, int *launches, Profiler *prof);
+// `any_dof` adds the depth-of-field gather.
+cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t st, int *launches, Profiler *prof);
+// The depth-of-field gather alone (items prepared by the caller).
+cudaError_t launch_dof(const BatchDev *b, cudaStream_t st);
+// Upload the constant tables (depth-of-field taps) to the current device.
+cudaError_t init_device_constants();
 
 } // namespace sgl

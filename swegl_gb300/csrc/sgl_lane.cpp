@@ -42,15 +42,17 @@ size_t view_scratch_bytes(uint32_t n_vertices, uint32_t n_triangles, int w, int 
 {
     const size_t px = (size_t)w * h;
     return align_up(16 * (size_t)n_vertices, 256) + align_up(n_vertices, 256) + 8 * px + 16 * px  // ndc yes key prec
-           + 8 * (size_t)n_triangles + 8 * px + sizeof(SpanRec) * (px / 8 + 64);                   // lists, bins
+           + 8 * (size_t)n_triangles + 8 * px + sizeof(SpanRec) * (px / 8 + 64)                    // lists, bins
+           + 8 * px;                                                                               // dof colour, depth
 }
 
 Lane::~Lane()
 {
     for (auto &sl : slots) {
-        for (auto &g : sl.graph)
-            if (g)
-                cudaGraphExecDestroy(g);
+        for (auto &gt : sl.graph)
+            for (auto &g : gt)
+                if (g)
+                    cudaGraphExecDestroy(g);
         if (sl.staged)
             cudaEventDestroy(sl.staged);
         if (sl.done)
@@ -65,6 +67,7 @@ Lane::~Lane()
 sgl_status Lane::init(Ctx *ctx, int max_items_, cudaStream_t external)
 {
     max_items = max_items_;
+    CUDA_TRY(init_device_constants());
     if (external) {
         stream = external;
         own_stream = false;
@@ -103,9 +106,9 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     // prefixes and pool offsets
     uint32_t *hb = (uint32_t *)sl.h_bases.ptr;
     uint32_t *vb = hb, *tb = hb + (n + 1), *pb = hb + 2 * (n + 1), *gb = hb + 3 * (n + 1);
-    uint64_t tv = 0, tt = 0, tp = 0, tg = 0;
+    uint64_t tv = 0, tt = 0, tp = 0, tg = 0, dof_px = 0, dofz_px = 0;
     size_t ndc_off = 0, yes_off = 0;
-    std::vector<size_t> ndc_at(n), yes_at(n);
+    std::vector<size_t> ndc_at(n), yes_at(n), dof_at(n), dofz_at(n);
     for (int i = 0; i < n; i++) {
         const Scene &s = *e[i].scene;
         const sgl_view &v = e[i].view;
@@ -121,6 +124,13 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         yes_at[i] = yes_off;
         ndc_off += align_up(s.n_vertices, 16);
         yes_off += align_up(s.n_vertices, 256);
+        dof_at[i] = dof_px;
+        dofz_at[i] = dofz_px;
+        if (v.dof.enabled) {
+            dof_px += align_up((size_t)v.w * v.h, 64);
+            if (!e[i].zbuf)
+                dofz_px += align_up((size_t)v.w * v.h, 64);
+        }
     }
     if (tv >= (1ull << 32) || tt >= (1ull << 31) || tp >= (1ull << 32) || tg >= (1ull << 32)) {
         ctx->fail("batch too large (%llu vertices, %llu triangles, %llu pixels)", (unsigned long long)tv,
@@ -139,6 +149,12 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     CUDA_TRY(list.ensure(sizeof(uint2) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(clippx.ensure(sizeof(uint2) * std::max<uint64_t>(tp, 1)));
     CUDA_TRY(spans.ensure(sizeof(SpanRec) * span_cap));
+    if (dof_px) {
+        CUDA_TRY(doftmp.ensure(4 * dof_px));
+        if (dofz_px)
+            CUDA_TRY(dofz.ensure(4 * dofz_px));
+    }
+    bool any_dof = false;
     ItemDev *hi = (ItemDev *)sl.h_items.ptr;
     for (int i = 0; i < n; i++) {
         const BatchEntry &en = e[i];
@@ -154,6 +170,24 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         it.zbuf = en.zbuf;
         it.tiles_x = (en.view.w + tile - 1) / tile;
         it.tile_base = gb[i];
+        if (en.view.dof.enabled) {
+            // the shade kernel fills a scratch colour buffer; the gather writes the target
+            const sgl_dof_desc &d = en.view.dof;
+            any_dof = true;
+            it.dof = 1;
+            it.dof_out = en.rect_pixels;
+            it.dof_pitch = en.pitch_px;
+            it.pixels = (uint32_t *)doftmp.ptr + dof_at[i];
+            it.pitch_px = en.view.w;
+            if (!en.zbuf)
+                it.zbuf = (float *)dofz.ptr + dofz_at[i];
+            const float k = d.px_scale > 0.0f ? d.px_scale : (en.view.proj[5] * (float)en.view.h) / 2.0f;
+            it.dof_focus = d.focus;
+            it.dof_ka = k * d.aperture;
+            it.dof_rmax = d.max_radius;
+            it.p22 = en.view.proj[10];
+            it.p23 = en.view.proj[11];
+        }
         hi[i] = it;
     }
     BatchDev *hbd = (BatchDev *)sl.h_batch.ptr;
@@ -190,6 +224,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     CUDA_TRY(cudaEventRecord(sl.staged, stream));
     sl.used = true;
     sl.n_items = n;
+    sl.any_dof = any_dof;
     *slot_out = si;
     return SGL_OK;
 }
@@ -201,7 +236,7 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
     Slot &sl = slots[si];
     const BatchDev *db = (const BatchDev *)sl.d_batch.ptr;
     if (use_graph) {
-        cudaGraphExec_t &g = sl.graph[tile_index(tile)];
+        cudaGraphExec_t &g = sl.graph[tile_index(tile)][sl.any_dof ? 1 : 0];
         if (!g) {
             // captured on a private stream (the caller's may be the legacy
             // default stream, which cannot be captured), launched on the caller's
@@ -210,7 +245,7 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
             cudaGraph_t graph = nullptr;
             CUDA_TRY(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal));
             int dummy = 0;
-            cudaError_t le = launch_batch(db, tile, capture_stream, &dummy, nullptr);
+            cudaError_t le = launch_batch(db, tile, sl.any_dof, capture_stream, &dummy, nullptr);
             cudaError_t ce = cudaStreamEndCapture(capture_stream, &graph);
             CUDA_TRY(le);
             CUDA_TRY(ce);
@@ -222,7 +257,7 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
         if (launches)
             *launches += 1;
     } else {
-        CUDA_TRY(launch_batch(db, tile, stream, launches, prof));
+        CUDA_TRY(launch_batch(db, tile, sl.any_dof, stream, launches, prof));
     }
     unsigned long long *hc = (unsigned long long *)sl.h_counters.ptr;
     CUDA_TRY(cudaMemcpyAsync(hc, sl.d_counters.ptr, sizeof(unsigned long long) * kCounterWords,

@@ -96,11 +96,12 @@ struct Lane {
         cudaEvent_t staged = nullptr; // staging copies of this slot done
         cudaEvent_t done = nullptr;   // launch sequence of this slot done
         bool used = false;
-        cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr}; // per tile 8/16/32
+        cudaGraphExec_t graph[3][2] = {}; // per tile 8/16/32, without / with depth of field
         int n_items = 0;
+        bool any_dof = false;
     } slots[kSlots];
     int next = 0;
-    DevBuf list, clip, clippx, spans, ndc, yes, key, prec;
+    DevBuf list, clip, clippx, spans, ndc, yes, key, prec, doftmp, dofz;
     ~Lane();
 
     sgl_status init(Ctx *ctx, int max_items, cudaStream_t external);
@@ -122,7 +123,7 @@ struct Ctx {
     int next_scene_id = 1;
     std::unique_ptr<Lane> lane;        // the plain renderer's lane (internal stream)
     std::unique_ptr<Lane> ext_lane;    // lane bound to caller streams
-    DevBuf stage_pixels, stage_z, debug_flags;
+    DevBuf stage_pixels, stage_z, debug_flags, dof_stage, dof_desc;
     Profiler prof;
     int tile = 16;                     // shade tile of the plain renderer
     int inline_span = 16;              // long-span bin threshold of the plain renderer

@@ -1,0 +1,351 @@
+// sgl_serve.cpp — the serving loop: render requests of different scenes and
+// viewport sizes are admitted against a device-memory budget (framebuffer +
+// scratch), batched as they arrive and run on several streams at once; each
+// finished frame can be copied to the caller's host buffers.
+//
+// Continuous batching: a worker thread keeps up to `streams` batches in
+// flight; whenever one finishes, its memory returns to the budget and the
+// requests that arrived meanwhile form the next batch on the freed stream.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "sgl.h"
+#include "sgl_internal.h"
+#include "sgl_runtime.h"
+
+namespace sgl {
+
+static double now_s()
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Job {
+    uint64_t ticket;
+    sgl_request req;
+    Scene *scene;
+    size_t bytes;
+    sgl_request_result res;
+};
+
+struct Server {
+    Ctx *ctx = nullptr;   // the owning context (scenes); only read by the worker
+    Ctx errors;           // the worker's own error sink (ctx->last_error belongs to the caller's thread)
+    sgl_serve_opts opts{};
+    struct LaneState {
+        std::unique_ptr<Lane> lane;
+        DevBuf frames; // framebuffers of the batch in flight: colour then depth per job
+        std::vector<Job> jobs;
+        size_t bytes = 0;
+        int slot = 0;
+        bool busy = false;
+    };
+    std::vector<std::unique_ptr<LaneState>> lanes;
+    std::mutex mu;
+    std::condition_variable cv_submit, cv_done;
+    std::deque<Job> pending;
+    std::unordered_map<uint64_t, sgl_request_result> done;
+    uint64_t next_ticket = 1;
+    uint64_t submitted = 0, completed = 0;
+    size_t in_flight_bytes = 0;
+    bool stop = false;
+    std::thread worker;
+    int tile = 16, span_bin = 16;
+
+    void run();
+    void launch_batch_on(LaneState &ls, std::vector<Job> &&jobs);
+    void finish(LaneState &ls);
+};
+
+static size_t request_bytes(const Scene *s, const sgl_view &v)
+{
+    return 8 * (size_t)v.w * v.h + view_scratch_bytes(s->n_vertices, s->n_triangles, v.w, v.h);
+}
+
+void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
+{
+    Ctx *c = &errors;
+    size_t fb = 0;
+    for (auto &j : jobs)
+        fb += 8 * (size_t)j.req.view.w * j.req.view.h;
+    sgl_status st = SGL_OK;
+    if (ls.frames.ensure(std::max<size_t>(fb, 256)) != cudaSuccess) {
+        c->fail("serving: framebuffer allocation of %zu bytes failed", fb);
+        st = SGL_ERR_OOM;
+    }
+    std::vector<BatchEntry> entries;
+    entries.reserve(jobs.size());
+    size_t off = 0;
+    std::vector<std::pair<uint32_t *, float *>> bufs;
+    for (auto &j : jobs) {
+        const size_t px = (size_t)j.req.view.w * j.req.view.h;
+        uint32_t *pix = (uint32_t *)((uint8_t *)ls.frames.ptr + off);
+        float *z = (float *)((uint8_t *)ls.frames.ptr + off + 4 * px);
+        off += 8 * px;
+        sgl_view v = j.req.view;
+        v.x = 0;
+        v.y = 0;
+        entries.push_back(BatchEntry{j.scene, v, pix, v.w, z});
+        bufs.emplace_back(pix, z);
+    }
+    const double t0 = now_s();
+    if (st == SGL_OK)
+        st = ls.lane->prepare(c, entries.data(), (int)entries.size(), tile, span_bin, nullptr, &ls.slot);
+    if (st == SGL_OK)
+        st = ls.lane->launch(c, ls.slot, tile, true, nullptr, nullptr);
+    if (st == SGL_OK && opts.copy_out) {
+        for (size_t i = 0; i < jobs.size() && st == SGL_OK; i++) {
+            const size_t px = (size_t)jobs[i].req.view.w * jobs[i].req.view.h;
+            if (jobs[i].req.host_pixels &&
+                cudaMemcpyAsync(jobs[i].req.host_pixels, bufs[i].first, 4 * px, cudaMemcpyDeviceToHost,
+                                ls.lane->stream) != cudaSuccess)
+                st = SGL_ERR_CUDA;
+            if (jobs[i].req.host_zbuffer &&
+                cudaMemcpyAsync(jobs[i].req.host_zbuffer, bufs[i].second, 4 * px, cudaMemcpyDeviceToHost,
+                                ls.lane->stream) != cudaSuccess)
+                st = SGL_ERR_CUDA;
+        }
+        // the lane's done event must come after the copies
+        if (st == SGL_OK && cudaEventRecord(ls.lane->slots[ls.slot].done, ls.lane->stream) != cudaSuccess)
+            st = SGL_ERR_CUDA;
+    }
+    for (auto &j : jobs) {
+        j.res.start_s = t0;
+        j.res.status = st;
+    }
+    ls.jobs = std::move(jobs);
+    ls.busy = true;
+}
+
+void Server::finish(LaneState &ls)
+{
+    std::vector<unsigned long long> per_item;
+    sgl_status st = ls.lane->read_counters(&errors, ls.slot, nullptr, nullptr, &per_item);
+    const double t = now_s();
+    std::lock_guard<std::mutex> g(mu);
+    for (size_t i = 0; i < ls.jobs.size(); i++) {
+        Job &j = ls.jobs[i];
+        j.res.done_s = t;
+        if (j.res.status == SGL_OK)
+            j.res.status = st;
+        j.res.fragments = (2 * i + 1 < per_item.size()) ? per_item[2 * i + 1] : 0;
+        done[j.ticket] = j.res;
+        in_flight_bytes -= j.bytes;
+        completed++;
+    }
+    ls.jobs.clear();
+    ls.busy = false;
+    cv_done.notify_all();
+}
+
+void Server::run()
+{
+    cudaSetDevice(ctx->device);
+    for (;;) {
+        // completions
+        for (auto &lp : lanes) {
+            LaneState &ls = *lp;
+            if (ls.busy) {
+                cudaError_t q = cudaEventQuery(ls.lane->slots[ls.slot].done);
+                if (q == cudaSuccess)
+                    finish(ls);
+                else if (q != cudaErrorNotReady) {
+                    cudaGetLastError();
+                    for (auto &j : ls.jobs)
+                        j.res.status = SGL_ERR_CUDA;
+                    finish(ls);
+                }
+            }
+        }
+        // admission: the requests that fit the budget, in arrival order, to a free stream
+        LaneState *free_lane = nullptr;
+        for (auto &lp : lanes)
+            if (!lp->busy) {
+                free_lane = lp.get();
+                break;
+            }
+        std::vector<Job> batch;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            if (stop && pending.empty()) {
+                bool any_busy = false;
+                for (auto &lp : lanes)
+                    any_busy |= lp->busy;
+                if (!any_busy)
+                    return;
+            }
+            if (free_lane) {
+                while (!pending.empty() && (int)batch.size() < opts.max_batch) {
+                    Job &j = pending.front();
+                    if (in_flight_bytes + j.bytes > opts.budget_bytes && !(batch.empty() && in_flight_bytes == 0))
+                        break; // wait for memory; a lone request larger than what is free still runs alone
+                    in_flight_bytes += j.bytes;
+                    batch.push_back(j);
+                    pending.pop_front();
+                }
+            }
+            if (batch.empty()) {
+                bool any_busy = false;
+                for (auto &lp : lanes)
+                    any_busy |= lp->busy;
+                if (!any_busy || !free_lane)
+                    cv_submit.wait_for(lk, std::chrono::microseconds(any_busy ? 20 : 2000));
+                else
+                    cv_submit.wait_for(lk, std::chrono::microseconds(20));
+                continue;
+            }
+        }
+        launch_batch_on(*free_lane, std::move(batch));
+    }
+}
+
+} // namespace sgl
+
+using namespace sgl;
+
+extern "C" {
+
+SGL_API sgl_status sgl_server_create(sgl_ctx *c, const sgl_serve_opts *opts, sgl_server **out)
+{
+    Ctx *ctx = reinterpret_cast<Ctx *>(c);
+    if (!ctx || !out)
+        return SGL_ERR_INVALID;
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    auto *srv = new (std::nothrow) Server();
+    if (!srv)
+        return SGL_ERR_OOM;
+    srv->ctx = ctx;
+    srv->errors.device = ctx->device;
+    srv->opts = opts ? *opts : sgl_serve_opts{};
+    if (srv->opts.budget_bytes == 0)
+        srv->opts.budget_bytes = 40ull << 30;
+    if (srv->opts.max_batch <= 0 || srv->opts.max_batch > kMaxBatch)
+        srv->opts.max_batch = 64;
+    if (srv->opts.streams <= 0 || srv->opts.streams > 16)
+        srv->opts.streams = 3;
+    srv->tile = ctx->tile;
+    srv->span_bin = ctx->inline_span;
+    for (int i = 0; i < srv->opts.streams; i++) {
+        srv->lanes.push_back(std::make_unique<Server::LaneState>());
+        Server::LaneState &ls = *srv->lanes.back();
+        ls.lane = std::make_unique<Lane>();
+        sgl_status st = ls.lane->init(&srv->errors, srv->opts.max_batch, nullptr);
+        if (st != SGL_OK) {
+            delete srv;
+            return st;
+        }
+    }
+    srv->worker = std::thread([srv] { srv->run(); });
+    *out = reinterpret_cast<sgl_server *>(srv);
+    return SGL_OK;
+}
+
+SGL_API sgl_status sgl_server_submit(sgl_server *s, const sgl_request *req, uint64_t *ticket)
+{
+    Server *srv = reinterpret_cast<Server *>(s);
+    if (!srv || !req || !ticket)
+        return SGL_ERR_INVALID;
+    Scene *scene = srv->ctx->find(req->scene_id);
+    if (!scene)
+        return SGL_ERR_NOT_FOUND;
+    const sgl_view &v = req->view;
+    if (v.w <= 0 || v.h <= 0 || (int64_t)v.w * v.h > (1ll << 28))
+        return SGL_ERR_INVALID;
+    Job j{};
+    j.req = *req;
+    j.scene = scene;
+    j.bytes = request_bytes(scene, v);
+    if (j.bytes > srv->opts.budget_bytes)
+        return SGL_ERR_BUDGET;
+    j.res.submit_s = now_s();
+    j.res.status = SGL_ERR_BUSY;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        if (srv->stop)
+            return SGL_ERR_INVALID;
+        j.ticket = srv->next_ticket++;
+        srv->pending.push_back(j);
+        srv->submitted++;
+    }
+    srv->cv_submit.notify_one();
+    *ticket = j.ticket;
+    return SGL_OK;
+}
+
+SGL_API sgl_status sgl_server_poll(sgl_server *s, uint64_t ticket, sgl_request_result *result)
+{
+    Server *srv = reinterpret_cast<Server *>(s);
+    if (!srv)
+        return SGL_ERR_INVALID;
+    std::lock_guard<std::mutex> g(srv->mu);
+    auto it = srv->done.find(ticket);
+    if (it == srv->done.end())
+        return (ticket == 0 || ticket >= srv->next_ticket) ? SGL_ERR_NOT_FOUND : SGL_ERR_BUSY;
+    if (result)
+        *result = it->second;
+    srv->done.erase(it);
+    return SGL_OK;
+}
+
+SGL_API sgl_status sgl_server_wait(sgl_server *s, uint64_t ticket, double timeout_s, sgl_request_result *result)
+{
+    Server *srv = reinterpret_cast<Server *>(s);
+    if (!srv)
+        return SGL_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+    for (;;) {
+        auto it = srv->done.find(ticket);
+        if (it != srv->done.end()) {
+            if (result)
+                *result = it->second;
+            srv->done.erase(it);
+            return SGL_OK;
+        }
+        if (ticket == 0 || ticket >= srv->next_ticket)
+            return SGL_ERR_NOT_FOUND;
+        if (srv->cv_done.wait_until(lk, deadline) == std::cv_status::timeout)
+            return SGL_ERR_TIMEOUT;
+    }
+}
+
+SGL_API sgl_status sgl_server_drain(sgl_server *s, double timeout_s)
+{
+    Server *srv = reinterpret_cast<Server *>(s);
+    if (!srv)
+        return SGL_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+    while (srv->completed < srv->submitted)
+        if (srv->cv_done.wait_until(lk, deadline) == std::cv_status::timeout)
+            return SGL_ERR_TIMEOUT;
+    return SGL_OK;
+}
+
+SGL_API void sgl_server_destroy(sgl_server *s)
+{
+    Server *srv = reinterpret_cast<Server *>(s);
+    if (!srv)
+        return;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        srv->stop = true;
+    }
+    srv->cv_submit.notify_all();
+    if (srv->worker.joinable())
+        srv->worker.join();
+    delete srv;
+}
+
+} // extern "C"

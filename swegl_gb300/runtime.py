@@ -57,6 +57,13 @@ def library() -> C.CDLL:
             "sgl_render_batch": ([C.c_void_p, P(abi.BatchItem), C.c_int, P(abi.BatchOpts), C.c_void_p,
                                   P(abi.FrameStats)], C.c_int),
             "sgl_autotune": ([C.c_void_p, P(abi.BatchItem), C.c_int, P(abi.BatchOpts)], C.c_int),
+            "sgl_dof": ([C.c_void_p, P(abi.ViewDesc), P(abi.Target), P(abi.Target), C.c_int, C.c_void_p], C.c_int),
+            "sgl_server_create": ([C.c_void_p, P(abi.ServeOpts), P(C.c_void_p)], C.c_int),
+            "sgl_server_submit": ([C.c_void_p, P(abi.Request), P(C.c_uint64)], C.c_int),
+            "sgl_server_poll": ([C.c_void_p, C.c_uint64, P(abi.RequestResult)], C.c_int),
+            "sgl_server_wait": ([C.c_void_p, C.c_uint64, C.c_double, P(abi.RequestResult)], C.c_int),
+            "sgl_server_drain": ([C.c_void_p, C.c_double], C.c_int),
+            "sgl_server_destroy": ([C.c_void_p], None),
             "sgl_profile_read": ([C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_uint64)], C.c_int),
         }
         for name, (args, res) in sigs.items():
@@ -177,6 +184,23 @@ class Renderer:
         self._check(self.lib.sgl_autotune(self.ctx, arr, len(items), C.byref(opts)))
         return {"tile": opts.tile, "span_bin": opts.span_bin, "use_graph": opts.use_graph}
 
+    # depth of field -------------------------------------------------------
+    def dof(self, view, pixels: np.ndarray, zbuffer: np.ndarray) -> np.ndarray:
+        """The depth-of-field gather on a host frame (h, w) and its z-buffer."""
+        h, w = pixels.shape
+        src = np.ascontiguousarray(pixels, np.uint32)
+        z = np.ascontiguousarray(zbuffer, np.float32)
+        out = np.zeros_like(src)
+        vd = abi.view_desc(view)
+        vd.x = vd.y = 0
+        t_in = abi.Target(src.ctypes.data, 4 * w, w, h, z.ctypes.data_as(C.POINTER(C.c_float)))
+        t_out = abi.Target(out.ctypes.data, 4 * w, w, h, None)
+        self._check(self.lib.sgl_dof(self.ctx, C.byref(vd), C.byref(t_in), C.byref(t_out), 0, None))
+        return out
+
+    def server(self, budget_bytes: int = 0, max_batch: int = 0, streams: int = 0, copy_out: bool = True):
+        return Server(self, budget_bytes, max_batch, streams, copy_out)
+
     # per-kernel device timing ----------------------------------------------
     def profile(self, enable: bool = True):
         self._check(self.lib.sgl_profile(self.ctx, 1 if enable else 0))
@@ -198,3 +222,70 @@ class Renderer:
 def _stats_dict(fs: abi.FrameStats) -> dict:
     return {"triangles": fs.triangles, "drawn_triangles": fs.drawn_triangles, "fragments": fs.fragments,
             "pixels": fs.pixels, "kernel_launches": fs.kernel_launches}
+
+
+class Server:
+    """The continuous-batching request loop of the library (sgl_server_*)."""
+
+    def __init__(self, renderer: Renderer, budget_bytes=0, max_batch=0, streams=0, copy_out=True):
+        self.r = renderer
+        self.lib = renderer.lib
+        opts = abi.ServeOpts(budget_bytes, max_batch, streams, 1 if copy_out else 0)
+        h = C.c_void_p()
+        self.r._check(self.lib.sgl_server_create(self.r.ctx, C.byref(opts), C.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, scene_id: int, view, host_pixels: np.ndarray | None = None,
+               host_zbuffer: np.ndarray | None = None) -> int:
+        req = abi.Request()
+        req.scene_id = scene_id
+        req.view = abi.view_desc(view)
+        if host_pixels is not None:
+            req.host_pixels = host_pixels.ctypes.data_as(C.POINTER(C.c_uint32))
+        if host_zbuffer is not None:
+            req.host_zbuffer = host_zbuffer.ctypes.data_as(C.POINTER(C.c_float))
+        t = C.c_uint64()
+        st = self.lib.sgl_server_submit(self.h, C.byref(req), C.byref(t))
+        if st != 0:
+            raise SglError(st, "sgl_server_submit")
+        self._keep[t.value] = (host_pixels, host_zbuffer)
+        return t.value
+
+    def _result(self, res: abi.RequestResult) -> dict:
+        return {"status": res.status, "submit_s": res.submit_s, "start_s": res.start_s, "done_s": res.done_s,
+                "fragments": res.fragments}
+
+    def poll(self, ticket: int):
+        res = abi.RequestResult()
+        st = self.lib.sgl_server_poll(self.h, ticket, C.byref(res))
+        if st == -9:
+            return None
+        if st != 0:
+            raise SglError(st, "sgl_server_poll")
+        self._keep.pop(ticket, None)
+        return self._result(res)
+
+    def wait(self, ticket: int, timeout_s: float = 60.0) -> dict:
+        res = abi.RequestResult()
+        st = self.lib.sgl_server_wait(self.h, ticket, timeout_s, C.byref(res))
+        if st != 0:
+            raise SglError(st, "sgl_server_wait")
+        self._keep.pop(ticket, None)
+        return self._result(res)
+
+    def drain(self, timeout_s: float = 120.0):
+        st = self.lib.sgl_server_drain(self.h, timeout_s)
+        if st != 0:
+            raise SglError(st, "sgl_server_drain")
+
+    def close(self):
+        if self.h:
+            self.lib.sgl_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
