@@ -96,7 +96,9 @@ def test_serving_budget_and_poll(renderer):
     t = srv.submit(sid, S.cube_view(320, 240))
     res = srv.wait(t, 30.0)
     assert res["status"] == 0 and res["fragments"] > 0
-    assert srv.poll(t + 1000) is None or True
+    with pytest.raises(SglError) as e:
+        srv.poll(t + 1000)  # never issued
+    assert e.value.status == -4
     srv.drain(10.0)
     srv.close()
     renderer.release(sid)
