@@ -1,22 +1,34 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 swegl renderer; prints ONE JSON line (rank 0).
 
-Workloads (synthetic, seeded; see swegl_gb300/scenes.py):
-  frame  200 UV spheres (819,200 triangles, 8 value-noise 1024^2 textures,
-         sun + 4 point lights, shininess in [8,128]) at 1920x1080, one frame
-         per step, plain one-frame-per-launch renderer.
+Default workload, `serve` (the metric): 8 device-resident scenes of 200-style
+UV spheres with 10k, 50k, 100k, 250k, 500k, 800k, 1.2M and 2M triangles; a
+seeded request stream (Poisson arrivals at 2000 requests/s, uniform scene,
+camera on a sphere of radius 35, viewport sides log-uniform 64..3840 x
+64..2160, depth of field with probability 0.5) served by the library's
+continuous-batching loop under a 40 GB budget.
 
-Timing: W warm-up steps, then K timed steps, each bracketed by CUDA events on
-the launching stream.  Inputs are larger than L2: four resident copies of the
-scene (about 4 x 100 MB against a 129 MB L2) are rendered in rotation, so each
-step reads its scene cold.  `e2e` renders the same frames through the public
-C ABI with host (pinned) buffers: the frame copy back to the host is inside
-its timed region.  Under torchrun (N > 1) every rank renders its own frames
-(replicas, no collective); rank 0 prints the max-over-ranks timing.
+  value     served frames/s at saturation: each step submits 256 requests of
+            the stream at once and drains them (closed loop).  Timed with
+            CUDA events on the default stream, which the serving streams are
+            ordered with.
+  sequential_frames_per_s  the same requests through the plain
+            one-frame-per-launch renderer, one call after another.
+  latency   p50/p99/p999 with the requests submitted at their Poisson
+            arrival times (open loop) for --duration seconds.
+  e2e       closed-loop steps again, every frame (colour + depth) copied to
+            pinned host memory through the public API.
+  roofline  the plain renderer's 1080p frame of the 200-sphere scene
+            (819,200 triangles): algorithmic bytes / device time, against the
+            measured HBM copy bandwidth; per-stage times from CUDA events.
 
+Inputs are larger than L2: the 8 resident scenes hold ~1.9 GB.  Under
+torchrun (N > 1) every rank serves its own stream (replicas, no collective);
+value sums the frames of all ranks over the max-over-ranks time.
+
+--workload frame times the plain renderer alone on the 1080p frame.
 --impl reference times the reference's CPU algorithm (the oracle's C
-restatement, built from oracle/sgl_oracle.c) on all host threads on the same
-workload.
+restatement, oracle/sgl_oracle.c) on all host threads on the same requests.
 """
 from __future__ import annotations
 
@@ -35,10 +47,13 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
+METRIC = "served frames/s + p50/p99 latency vs one-frame-per-launch, same GPU, <=1 LSB RGB"
+
 
 # ----------------------------------------------------------------- helpers --
 def env_rank():
-    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 def measured_peaks() -> dict:
@@ -51,7 +66,7 @@ def measured_peaks() -> dict:
 
 
 def profile_traffic(name: str):
-    """Per-launch DRAM traffic from the committed ncu summary (profiles/)."""
+    """Per-frame DRAM traffic from the committed ncu summary (profiles/)."""
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
@@ -78,8 +93,7 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except (OSError, FileNotFoundError):
             self.proc = None
         time.sleep(0.3)
@@ -125,24 +139,122 @@ def frame_alg_bytes(scene, w: int, h: int) -> int:
     return 32 * len(scene.positions) + 4 * len(scene.indices) + 4 * texels + 8 * w * h
 
 
-# ---------------------------------------------------------------- workloads --
-def build_frame_workload():
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def device_target(torch, w: int, h: int):
+    from swegl_gb300 import abi
+
+    pix = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+    zb = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+    t = abi.Target()
+    t.pixels = pix.data_ptr()
+    t.pitch = 4 * w
+    t.width, t.height = w, h
+    t.zbuffer = C.cast(C.c_void_p(zb.data_ptr()), C.POINTER(C.c_float))
+    return (pix, zb), t
+
+
+def max_over_ranks(torch, dist, x: float) -> float:
+    if not dist:
+        return x
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(torch, dist, x: float) -> float:
+    if not dist:
+        return x
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------- single-frame stage --
+def frame_measure(r, torch, steps: int, warmup: int, with_e2e: bool):
+    """The plain renderer on the 1080p 200-sphere frame; 4 resident copies of
+    the scene (~400 MB, above the 129 MB L2) rendered in rotation."""
+    from swegl_gb300 import abi
     from swegl_gb300 import scenes as S
 
     scene = S.spheres_scene()
-    view = S.spheres_view(1920, 1080)
-    cfg = {"workload": "spheres200_1080p_frame", "spheres": 200, "triangles": scene.n_triangles,
-           "vertices": int(len(scene.positions)), "viewport": "1920x1080", "textures": "8 x 1024^2 value noise",
-           "lights": "sun + 4 point", "shininess": "U[8,128]",
-           "l2": "inputs larger than L2: 4 resident scene copies rendered in rotation",
-           "renderer": "one frame per launch sequence"}
-    return scene, [view], cfg
+    v = S.spheres_view(1920, 1080)
+    copies = [r.upload(scene) for _ in range(4)]
+    stream = torch.cuda.Stream()
+    _bufs, tgt = device_target(torch, v.w, v.h)
+
+    def step(k):
+        r.render_device(copies[k % len(copies)], [v], [tgt], stream=stream.cuda_stream)
+
+    for k in range(warmup):
+        step(k)
+    torch.cuda.synchronize()
+    stats = r.render_device(copies[0], [v], [tgt], stream=stream.cuda_stream, stats=True)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    r.profile(True)
+    for k in range(steps):
+        starts[k].record(stream)
+        step(k)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    prof = r.profile_read()
+    r.profile(False)
+    frame_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / steps
+    out = {"frame_ms": frame_ms, "stats": stats, "prof": prof, "alg_bytes": frame_alg_bytes(scene, v.w, v.h)}
+    if with_e2e:
+        host_pix = torch.zeros((v.h, v.w), dtype=torch.int32).pin_memory()
+        host_z = torch.zeros((v.h, v.w), dtype=torch.float32).pin_memory()
+        htgt = abi.Target()
+        htgt.pixels = host_pix.data_ptr()
+        htgt.pitch = 4 * v.w
+        htgt.width, htgt.height = v.w, v.h
+        htgt.zbuffer = C.cast(C.c_void_p(host_z.data_ptr()), C.POINTER(C.c_float))
+        vd = (abi.ViewDesc * 1)(abi.view_desc(v))
+        td = (abi.Target * 1)(htgt)
+        for k in range(warmup):
+            r.lib.sgl_render(r.ctx, copies[k % 4], vd, td, 1, 0, None, None)
+        t0 = time.perf_counter()
+        for k in range(steps):
+            st = r.lib.sgl_render(r.ctx, copies[k % 4], vd, td, 1, 0, None, None)
+            if st != 0:
+                raise RuntimeError(f"sgl_render failed: {st}")
+        out["e2e_fps"] = steps / (time.perf_counter() - t0)
+        out["view_bytes"] = C.sizeof(abi.ViewDesc)
+        out["frame_bytes"] = 8 * v.w * v.h
+    for c in copies:
+        r.release(c)
+    out["scene"] = scene
+    out["view"] = v
+    return out
 
 
-def run_ours(args, rank, world, local_rank):
+def roofline_of(fm: dict) -> dict:
+    peaks = measured_peaks()
+    achieved = fm["alg_bytes"] / (fm["frame_ms"] / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": peaks["source"],
+            "unit_of_work": "one 1920x1080 frame of the 819,200-triangle scene (%d algorithmic bytes)"
+                            % fm["alg_bytes"],
+            "frame_us": round(1e3 * fm["frame_ms"], 2),
+            "traffic": profile_traffic("frame_1080p_traffic.md")}
+
+
+def kernels_of(fm: dict) -> dict:
+    return {k: {"avg_us": round(1e3 * d["total_ms"] / max(1, d["launches"]), 2)} for k, d in fm["prof"].items()
+            if d["launches"]}
+
+
+# --------------------------------------------------------------- workloads --
+def run_frame(args, rank, world, local_rank):
     import torch
 
-    from swegl_gb300 import abi
     from swegl_gb300.runtime import Renderer
 
     torch.cuda.set_device(local_rank)
@@ -151,182 +263,302 @@ def run_ours(args, rank, world, local_rank):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    scene, views, cfg = build_frame_workload()
     r = Renderer(local_rank)
-    copies = [r.upload(scene) for _ in range(4)]
-    sid = copies[0]
-    v = views[0]
-    stream = torch.cuda.Stream()
-    pix = torch.zeros((v.h, v.w), dtype=torch.int32, device="cuda")
-    zb = torch.zeros((v.h, v.w), dtype=torch.float32, device="cuda")
-    tgt = abi.Target()
-    tgt.pixels = pix.data_ptr()
-    tgt.pitch = 4 * v.w
-    tgt.width, tgt.height = v.w, v.h
-    tgt.zbuffer = C.cast(C.c_void_p(zb.data_ptr()), C.POINTER(C.c_float))
-    def step(k):
-        r.render_device(copies[k % len(copies)], views, [tgt], stream=stream.cuda_stream)
-
-    with torch.cuda.stream(stream):
-        for k in range(args.warmup):
-            step(k)
-    torch.cuda.synchronize()
-    stats = r.render_device(sid, views, [tgt], stream=stream.cuda_stream, stats=True)
-    torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     if dist:
         dist.barrier()
-    torch.cuda.synchronize()
-    r.profile(True)
     with ClockSampler(local_rank) as clocks:
-        with torch.cuda.stream(stream):
-            for k in range(args.steps):
-                starts[k].record(stream)
-                step(k)
-                ends[k].record(stream)
-        torch.cuda.synchronize()
-    prof = r.profile_read()
-    r.profile(False)
-    if dist:
-        dist.barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    frames_per_s = world * args.steps / (total_ms / 1e3)
-
-    # e2e through the public API with pinned host buffers (copy-out inside)
-    host_pix = torch.zeros((v.h, v.w), dtype=torch.int32).pin_memory()
-    host_z = torch.zeros((v.h, v.w), dtype=torch.float32).pin_memory()
-    htgt = abi.Target()
-    htgt.pixels = host_pix.data_ptr()
-    htgt.pitch = 4 * v.w
-    htgt.width, htgt.height = v.w, v.h
-    htgt.zbuffer = C.cast(C.c_void_p(host_z.data_ptr()), C.POINTER(C.c_float))
-    vd = (abi.ViewDesc * 1)(abi.view_desc(v))
-    td = (abi.Target * 1)(htgt)
-
-    def e2e_step(k):
-        st = r.lib.sgl_render(r.ctx, copies[k % len(copies)], vd, td, 1, 0, None, None)
-        if st != 0:
-            raise RuntimeError(f"sgl_render failed: {st}")
-
-    for k in range(args.warmup):
-        e2e_step(k)
-    e2e_times = []
-    for k in range(args.steps):
-        t0 = time.perf_counter()
-        e2e_step(k)
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_times)
-    if dist:
-        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_fps = world * args.steps / e2e_total
-
-    alg = frame_alg_bytes(scene, v.w, v.h)
-    frame_ms = total_ms / args.steps
-    peaks = measured_peaks()
-    achieved = alg / (frame_ms / 1e3) / 1e9
-    kernels = {k: {"avg_us": round(1e3 * d["total_ms"] / max(1, d["launches"]), 2), "launches": d["launches"]}
-               for k, d in prof.items()}
-    dom = max(prof.items(), key=lambda kv: kv[1]["total_ms"])[0] if prof else None
+        fm = frame_measure(r, torch, args.steps, args.warmup, True)
+    frame_ms = max_over_ranks(torch, dist, fm["frame_ms"])
+    fps = world * 1e3 / frame_ms
+    e2e = sum_over_ranks(torch, dist, fm["e2e_fps"]) if dist else fm["e2e_fps"]
+    prof = fm["prof"]
     out = {
-        "metric": "frames/s (single 1080p frame per launch sequence)",
-        "value": round(frames_per_s, 2),
-        "unit": "frames/s",
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": round(frame_ms, 4),
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "fp32",
-        "data": "synthetic (seeded scenes, see swegl_gb300/scenes.py)",
-        "config": cfg,
-        "gfragments_per_s": round(stats["fragments"] * frames_per_s / 1e9, 3),
-        "fragments_per_frame": stats["fragments"],
-        "kernels": kernels,
-        "dominant_kernel": dom,
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": peaks["source"],
-                     "unit_of_work": "one frame (alg bytes %d)" % alg,
-                     "traffic": profile_traffic("frame_1080p_traffic.md")},
-        "e2e": {"value": round(e2e_fps, 2), "unit": "frames/s", "h2d_bytes_per_step": C.sizeof(abi.ViewDesc),
-                "d2h_bytes_per_step": 8 * v.w * v.h},
-        "gpu_launches": int(stats["kernel_launches"]) * args.steps,
+        "metric": "frames/s (plain renderer, one 1080p frame per launch sequence)",
+        "value": round(fps, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(frame_ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic (seeded scenes, swegl_gb300/scenes.py)",
+        "config": {"workload": "spheres200_1080p_frame", "triangles": fm["scene"].n_triangles,
+                   "viewport": "1920x1080", "l2": "inputs larger than L2: 4 resident scene copies in rotation"},
+        "gfragments_per_s": round(fm["stats"]["fragments"] * fps / 1e9, 3),
+        "kernels": kernels_of(fm),
+        "dominant_kernel": max(prof.items(), key=lambda kv: kv[1]["total_ms"])[0] if prof else None,
+        "roofline": roofline_of(fm),
+        "e2e": {"value": round(e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": fm["view_bytes"],
+                "d2h_bytes_per_step": fm["frame_bytes"]},
+        "gpu_launches": int(fm["stats"]["kernel_launches"]) * args.steps,
         "clocks": clocks.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(scene, views, args)
+        out["cpu_baseline"] = cpu_frame_baseline(fm["scene"], fm["view"], args)
+    r.close()
     if dist:
         dist.destroy_process_group()
-    r.close()
     return out if rank == 0 else None
 
 
-def cpu_threads() -> int:
-    try:
-        return len(os.sched_getaffinity(0))
-    except AttributeError:
-        return os.cpu_count() or 1
-
-
-def cpu_baseline(scene, views, args) -> dict:
-    """The oracle restatement on all host threads, a bounded sample of the workload."""
+def cpu_frame_baseline(scene, view, args) -> dict:
     import oracle
 
     threads = cpu_threads()
     n = max(threads, args.cpu_frames)
-    frame_views = [views[i % len(views)] for i in range(n)]
-    oracle.render_parallel(scene, frame_views[:threads], threads)  # warm-up
+    oracle.render_parallel(scene, [view] * threads, threads)
     t0 = time.perf_counter()
-    oracle.render_parallel(scene, frame_views, threads)
+    oracle.render_parallel(scene, [view] * n, threads)
     dt = time.perf_counter() - t0
     return {"value": round(n / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": f"{n} frames of the same workload on {threads} threads ({dt:.1f} s)"}
+            "sample": f"{n} frames of the 1080p frame on {threads} threads ({dt:.1f} s)"}
 
 
-def run_reference(args, rank, world):
-    """The reference's CPU algorithm (oracle restatement) timed on the host cores."""
-    if rank != 0:
-        return None
-    scene, views, cfg = build_frame_workload()
+def serve_config(args) -> dict:
+    from swegl_gb300 import scenes as S
+
+    return {"workload": "serving: 8 resident scenes, Poisson 2000 req/s, viewports 64^2..3840x2160, DoF p=0.5",
+            "scene_triangles": list(S.SERVE_TRIANGLES), "requests_per_step": args.requests_per_step,
+            "budget_bytes": args.budget, "max_batch": args.max_batch, "streams": args.streams,
+            "latency_duration_s": args.duration, "arrival_rate": 2000,
+            "l2": "inputs larger than L2: 8 resident scenes of ~1.9 GB"}
+
+
+def run_serve(args, rank, world, local_rank):
+    import torch
+
+    from swegl_gb300 import scenes as S
+    from swegl_gb300.runtime import Renderer
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    scenes = S.serving_scenes()
+    r = Renderer(local_rank)
+    sids = [r.upload(sc) for sc in scenes]
+    M = args.requests_per_step
+    reqs = S.serving_requests((args.warmup + args.steps) * M, seed=60 + rank)
+    srv = r.server(budget_bytes=args.budget, max_batch=args.max_batch, streams=args.streams, copy_out=False)
+
+    def serve_chunk(chunk, server):
+        for (_, k, v) in chunk:
+            server.submit(sids[k], v)
+        server.drain(600.0)
+
+    # warm-up: graphs captured, pools grown
+    for s in range(args.warmup):
+        serve_chunk(reqs[s * M:(s + 1) * M], srv)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    b0 = srv.stats()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local_rank) as clocks:
+        for s in range(args.steps):
+            torch.cuda.synchronize()
+            starts[s].record()
+            serve_chunk(reqs[(args.warmup + s) * M:(args.warmup + s + 1) * M], srv)
+            ends[s].record()
+            torch.cuda.synchronize()
+    b1 = srv.stats()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = max_over_ranks(torch, dist, sum(step_ms))
+    value = world * args.steps * M / (total_ms / 1e3)
+    timed = reqs[args.warmup * M:]
+
+    # sequential one-frame-per-launch on the same requests (a bounded prefix)
+    n_seq = min(len(timed), args.seq_requests)
+    big = max(v.w * v.h for (_, _, v) in timed[:n_seq])
+    _bufs, tgt = device_target(torch, 3840, max(1, -(-big // 3840)))
+    stream = torch.cuda.Stream()
+    for (_, k, v) in timed[:8]:
+        t = _retarget(tgt, v)
+        r.render_device(sids[k], [v], [t], stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for (_, k, v) in timed[:n_seq]:
+        r.render_device(sids[k], [v], [_retarget(tgt, v)], stream=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    seq_fps = n_seq / (e0.elapsed_time(e1) / 1e3)
+    # the batched loop on the very same prefix, for a like-for-like ratio
+    torch.cuda.synchronize()
+    e0.record()
+    serve_chunk(timed[:n_seq], srv)
+    e1.record()
+    torch.cuda.synchronize()
+    batched_same_fps = n_seq / (e0.elapsed_time(e1) / 1e3)
+
+    # open-loop latency at the Poisson arrival times
+    lat = latency_run(srv, sids, args.duration, seed=70 + rank)
+
+    # e2e: closed loop with every frame copied to pinned host memory
+    e2e_fps, h2d, d2h = e2e_run(r, torch, sids, timed, M, args)
+    srv.close()
+
+    fm = frame_measure(r, torch, 10, 3, False)
+    gpu_launches = int(b1["kernels"] - b0["kernels"])
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded scenes and request stream, swegl_gb300/scenes.py)",
+        "config": serve_config(args),
+        "sequential_frames_per_s": round(seq_fps, 2),
+        "batched_frames_per_s_same_requests": round(batched_same_fps, 2),
+        "sequential_requests": n_seq,
+        "latency_ms": lat,
+        "batches": int(b1["batches"] - b0["batches"]),
+        "frame_1080p": {"frames_per_s": round(1e3 / fm["frame_ms"], 1), "kernels": kernels_of(fm)},
+        "roofline": roofline_of(fm),
+        "e2e": {"value": round(e2e_fps, 2), "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": gpu_launches,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_serve_baseline(scenes, timed, args)
+    r.close()
+    if dist:
+        dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def _retarget(tgt, v):
+    from swegl_gb300 import abi
+
+    t = abi.Target()
+    t.pixels = tgt.pixels
+    t.pitch = 4 * v.w
+    t.width, t.height = v.w, v.h
+    t.zbuffer = tgt.zbuffer
+    return t
+
+
+def latency_run(srv, sids, duration: float, seed: int) -> dict:
+    from swegl_gb300 import scenes as S
+
+    stream_reqs = S.serving_requests(int(2000 * duration) + 1, seed=seed)
+    stream_reqs = [q for q in stream_reqs if q[0] <= duration]
+    t0 = time.perf_counter()
+    tickets = []
+    for (arrival, k, v) in stream_reqs:
+        while True:
+            dt = arrival - (time.perf_counter() - t0)
+            if dt <= 0:
+                break
+            if dt > 0.0005:
+                time.sleep(dt - 0.0003)
+        tickets.append(srv.submit(sids[k], v))
+    results = [srv.wait(t, 600.0) for t in tickets]
+    wall = time.perf_counter() - t0
+    lats = np.array([1e3 * (x["done_s"] - x["submit_s"]) for x in results])
+    return {"p50": round(float(np.percentile(lats, 50)), 3), "p99": round(float(np.percentile(lats, 99)), 3),
+            "p999": round(float(np.percentile(lats, 99.9)), 3), "mean": round(float(lats.mean()), 3),
+            "requests": len(results), "served_frames_per_s": round(len(results) / wall, 1),
+            "offered_rate": 2000}
+
+
+def e2e_run(r, torch, sids, timed, M: int, args):
+    """Closed-loop steps with copy-out of every frame to pinned host memory."""
+    srv = r.server(budget_bytes=args.budget, max_batch=args.max_batch, streams=args.streams, copy_out=True)
+    steps = max(1, min(args.steps, 3))
+    chunks = [timed[s * M:(s + 1) * M] for s in range(steps)]
+    need = max(sum(8 * v.w * v.h for (_, _, v) in ch) for ch in chunks)
+    pool = torch.empty(need // 4 + 16, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+
+    def run_chunk(ch):
+        off = 0
+        for (_, k, v) in ch:
+            px = v.w * v.h
+            pix = pool[off:off + px].reshape(v.h, v.w)
+            z = pool[off + px:off + 2 * px].view(np.float32).reshape(v.h, v.w)
+            off += 2 * px
+            srv.submit(sids[k], v, pix, z)
+        srv.drain(600.0)
+
+    run_chunk(chunks[0])  # warm-up
+    t0 = time.perf_counter()
+    for ch in chunks:
+        run_chunk(ch)
+    dt = time.perf_counter() - t0
+    srv.close()
+    from swegl_gb300 import abi
+
+    h2d = C.sizeof(abi.Request) * M
+    d2h = int(sum(8 * v.w * v.h for ch in chunks for (_, _, v) in ch) / steps)
+    return steps * M / dt, h2d, d2h
+
+
+def cpu_serve_baseline(scenes, timed, args) -> dict:
+    """The oracle restatement on all host threads over a bounded prefix of the
+    request stream, grouped by scene."""
     import oracle
 
     threads = cpu_threads()
-    per_step = threads
-    frame_views = [views[0]] * per_step
-    for _ in range(max(1, min(args.warmup, 1))):
-        oracle.render_parallel(scene, frame_views, threads)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        oracle.render_parallel(scene, frame_views, threads)
-        times.append(time.perf_counter() - t0)
-    fps = per_step * len(times) / sum(times)
+    sample = timed[:args.cpu_requests]
+    t0 = time.perf_counter()
+    by_scene = {}
+    for (_, k, v) in sample:
+        by_scene.setdefault(k, []).append(v)
+    for k, views in by_scene.items():
+        oracle.render_parallel(scenes[k], views, threads)
+    dt = time.perf_counter() - t0
+    return {"value": round(len(sample) / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"the first {len(sample)} requests of the stream on {threads} threads ({dt:.1f} s)"}
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU algorithm (the oracle restatement) on the host cores,
+    same workload and metric; each step renders a bounded slice of requests."""
+    if rank != 0:
+        return None
+    import oracle
+    from swegl_gb300 import scenes as S
+
+    threads = cpu_threads()
+    if args.workload == "frame":
+        scene = S.spheres_scene()
+        views = [S.spheres_view(1920, 1080)] * threads
+        cfg = {"workload": "spheres200_1080p_frame", "triangles": scene.n_triangles, "viewport": "1920x1080"}
+        metric = "frames/s (plain renderer, one 1080p frame per launch sequence)"
+        oracle.render_parallel(scene, views, threads)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            oracle.render_parallel(scene, views, threads)
+            times.append(time.perf_counter() - t0)
+        n_per_step = len(views)
+    else:
+        scenes = S.serving_scenes()
+        per_step = args.cpu_requests_per_step
+        reqs = S.serving_requests((args.steps + 1) * per_step, seed=60)
+        cfg = serve_config(args)
+        metric = METRIC
+
+        def step(chunk):
+            by_scene = {}
+            for (_, k, v) in chunk:
+                by_scene.setdefault(k, []).append(v)
+            for k, views in by_scene.items():
+                oracle.render_parallel(scenes[k], views, threads)
+
+        step(reqs[:per_step])
+        times = []
+        for s in range(args.steps):
+            t0 = time.perf_counter()
+            step(reqs[(s + 1) * per_step:(s + 2) * per_step])
+            times.append(time.perf_counter() - t0)
+        n_per_step = per_step
+    fps = n_per_step * len(times) / sum(times)
     return {
-        "impl": "reference",
-        "metric": "frames/s (single 1080p frame per launch sequence)",
-        "value": round(fps, 3),
-        "unit": "frames/s",
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": round(1e3 * sum(times) / len(times), 3),
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "fp32",
-        "data": "synthetic (seeded scenes, see swegl_gb300/scenes.py)",
-        "config": cfg,
+        "impl": "reference", "metric": metric, "value": round(fps, 3), "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded scenes and request stream, swegl_gb300/scenes.py)", "config": cfg,
         "cpu_baseline": {"value": round(fps, 3), "unit": "frames/s", "cores": threads, "kind": "port",
-                         "sample": f"{per_step} frames per step on {threads} threads"},
+                         "sample": f"{n_per_step} requests per step on {threads} threads"},
         "e2e": {"value": round(fps, 3), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -334,18 +566,29 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["serve", "frame"], default="serve")
+    ap.add_argument("--requests-per-step", type=int, default=256)
+    ap.add_argument("--seq-requests", type=int, default=512)
+    ap.add_argument("--duration", type=float, default=10.0, help="open-loop latency run, seconds")
+    ap.add_argument("--budget", type=int, default=40 << 30)
+    ap.add_argument("--max-batch", type=int, default=64)
+    ap.add_argument("--streams", type=int, default=3)
     ap.add_argument("--cpu-frames", type=int, default=32)
+    ap.add_argument("--cpu-requests", type=int, default=48)
+    ap.add_argument("--cpu-requests-per-step", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local_rank = env_rank()
     if args.impl == "reference":
         out = run_reference(args, rank, world)
+    elif args.workload == "frame":
+        out = run_frame(args, rank, world, local_rank)
     else:
-        out = run_ours(args, rank, world, local_rank)
+        out = run_serve(args, rank, world, local_rank)
     if out is not None:
         print(json.dumps(out), flush=True)
 

@@ -291,6 +291,8 @@ SGL_API sgl_status sgl_server_poll(sgl_server *srv, uint64_t ticket, sgl_request
 SGL_API sgl_status sgl_server_wait(sgl_server *srv, uint64_t ticket, double timeout_s, sgl_request_result *result);
 /* Wait until every submitted request is done (SGL_ERR_TIMEOUT otherwise). */
 SGL_API sgl_status sgl_server_drain(sgl_server *srv, double timeout_s);
+/* Batches and kernels launched, requests completed so far. */
+SGL_API sgl_status sgl_server_stats(sgl_server *srv, uint64_t *batches, uint64_t *kernels, uint64_t *completed);
 SGL_API void       sgl_server_destroy(sgl_server *srv);
 
 /* Per-kernel device timing (CUDA events on the launching stream around each

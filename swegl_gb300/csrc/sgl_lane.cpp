@@ -64,7 +64,7 @@ Lane::~Lane()
         cudaStreamDestroy(capture_stream);
 }
 
-sgl_status Lane::init(Ctx *ctx, int max_items_, cudaStream_t external)
+sgl_status Lane::init(Ctx *ctx, int max_items_, cudaStream_t external, bool blocking)
 {
     max_items = max_items_;
     CUDA_TRY(init_device_constants());
@@ -72,7 +72,7 @@ sgl_status Lane::init(Ctx *ctx, int max_items_, cudaStream_t external)
         stream = external;
         own_stream = false;
     } else {
-        CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        CUDA_TRY(cudaStreamCreateWithFlags(&stream, blocking ? cudaStreamDefault : cudaStreamNonBlocking));
         own_stream = true;
     }
     for (auto &sl : slots) {
@@ -244,8 +244,9 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
                 CUDA_TRY(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking));
             cudaGraph_t graph = nullptr;
             CUDA_TRY(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal));
-            int dummy = 0;
-            cudaError_t le = launch_batch(db, tile, sl.any_dof, capture_stream, &dummy, nullptr);
+            int kernels = 0;
+            cudaError_t le = launch_batch(db, tile, sl.any_dof, capture_stream, &kernels, nullptr);
+            sl.graph_kernels[tile_index(tile)][sl.any_dof ? 1 : 0] = kernels;
             cudaError_t ce = cudaStreamEndCapture(capture_stream, &graph);
             CUDA_TRY(le);
             CUDA_TRY(ce);
@@ -255,7 +256,7 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
         }
         CUDA_TRY(cudaGraphLaunch(g, stream));
         if (launches)
-            *launches += 1;
+            *launches += sl.graph_kernels[tile_index(tile)][sl.any_dof ? 1 : 0];
     } else {
         CUDA_TRY(launch_batch(db, tile, sl.any_dof, stream, launches, prof));
     }

@@ -97,6 +97,7 @@ struct Lane {
         cudaEvent_t done = nullptr;   // launch sequence of this slot done
         bool used = false;
         cudaGraphExec_t graph[3][2] = {}; // per tile 8/16/32, without / with depth of field
+        int graph_kernels[3][2] = {};     // kernels in each graph
         int n_items = 0;
         bool any_dof = false;
     } slots[kSlots];
@@ -104,7 +105,8 @@ struct Lane {
     DevBuf list, clip, clippx, spans, ndc, yes, key, prec, doftmp, dofz;
     ~Lane();
 
-    sgl_status init(Ctx *ctx, int max_items, cudaStream_t external);
+    // external == nullptr: own stream, blocking (ordered with the legacy default stream) or not
+    sgl_status init(Ctx *ctx, int max_items, cudaStream_t external, bool blocking = false);
     // Stage and copy the descriptors of a batch into a free slot; returns its index.
     sgl_status prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inline_span, uint8_t *slot_flags,
                        int *slot_out);

@@ -57,6 +57,7 @@ struct Server {
     std::unordered_map<uint64_t, sgl_request_result> done;
     uint64_t next_ticket = 1;
     uint64_t submitted = 0, completed = 0;
+    uint64_t batches = 0, kernels = 0; // launched by the worker
     size_t in_flight_bytes = 0;
     bool stop = false;
     std::thread worker;
@@ -101,8 +102,14 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
     const double t0 = now_s();
     if (st == SGL_OK)
         st = ls.lane->prepare(c, entries.data(), (int)entries.size(), tile, span_bin, nullptr, &ls.slot);
+    int kernels_launched = 0;
     if (st == SGL_OK)
-        st = ls.lane->launch(c, ls.slot, tile, true, nullptr, nullptr);
+        st = ls.lane->launch(c, ls.slot, tile, true, &kernels_launched, nullptr);
+    {
+        std::lock_guard<std::mutex> g(mu);
+        batches++;
+        kernels += (uint64_t)kernels_launched;
+    }
     if (st == SGL_OK && opts.copy_out) {
         for (size_t i = 0; i < jobs.size() && st == SGL_OK; i++) {
             const size_t px = (size_t)jobs[i].req.view.w * jobs[i].req.view.h;
@@ -240,7 +247,9 @@ SGL_API sgl_status sgl_server_create(sgl_ctx *c, const sgl_serve_opts *opts, sgl
         srv->lanes.push_back(std::make_unique<Server::LaneState>());
         Server::LaneState &ls = *srv->lanes.back();
         ls.lane = std::make_unique<Lane>();
-        sgl_status st = ls.lane->init(&srv->errors, srv->opts.max_batch, nullptr);
+        // blocking streams: work on the legacy default stream (a caller's timing
+        // events) is ordered with every batch
+        sgl_status st = ls.lane->init(&srv->errors, srv->opts.max_batch, nullptr, true);
         if (st != SGL_OK) {
             delete srv;
             return st;
@@ -330,6 +339,21 @@ SGL_API sgl_status sgl_server_drain(sgl_server *s, double timeout_s)
     while (srv->completed < srv->submitted)
         if (srv->cv_done.wait_until(lk, deadline) == std::cv_status::timeout)
             return SGL_ERR_TIMEOUT;
+    return SGL_OK;
+}
+
+SGL_API sgl_status sgl_server_stats(sgl_server *s, uint64_t *batches, uint64_t *kernels, uint64_t *completed)
+{
+    Server *srv = reinterpret_cast<Server *>(s);
+    if (!srv)
+        return SGL_ERR_INVALID;
+    std::lock_guard<std::mutex> g(srv->mu);
+    if (batches)
+        *batches = srv->batches;
+    if (kernels)
+        *kernels = srv->kernels;
+    if (completed)
+        *completed = srv->completed;
     return SGL_OK;
 }
 

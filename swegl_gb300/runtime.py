@@ -64,6 +64,7 @@ def library() -> C.CDLL:
             "sgl_server_wait": ([C.c_void_p, C.c_uint64, C.c_double, P(abi.RequestResult)], C.c_int),
             "sgl_server_drain": ([C.c_void_p, C.c_double], C.c_int),
             "sgl_server_destroy": ([C.c_void_p], None),
+            "sgl_server_stats": ([C.c_void_p, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)], C.c_int),
             "sgl_profile_read": ([C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_uint64)], C.c_int),
         }
         for name, (args, res) in sigs.items():
@@ -278,6 +279,11 @@ class Server:
         st = self.lib.sgl_server_drain(self.h, timeout_s)
         if st != 0:
             raise SglError(st, "sgl_server_drain")
+
+    def stats(self) -> dict:
+        b, k, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self.r._check(self.lib.sgl_server_stats(self.h, C.byref(b), C.byref(k), C.byref(c)))
+        return {"batches": b.value, "kernels": k.value, "completed": c.value}
 
     def close(self):
         if self.h:

@@ -414,15 +414,20 @@ def cube_scene(seed: int = CUBE_SEED, tex_size: int = 256, size: float = 2.0) ->
 
 def spheres_scene(n_spheres: int = 200, seed: int = SPHERES_SEED, n_textures: int = 8, tex_size: int = 1024,
                   slices: int = 64, stacks: int = 32, n_point_lights: int = 4, light_intensity: float = 50.0,
-                  box: float = 20.0, r_min: float = 0.3, r_max: float = 2.0, shininess=(8, 128)) -> Scene:
+                  box: float = 20.0, r_min: float = 0.3, r_max: float = 2.0, shininess=(8, 128),
+                  textures: list | None = None) -> Scene:
     """UV spheres with centres uniform in [-box, box]^3 and radii uniform in
     [r_min, r_max]; value-noise textures, one picked per sphere; per-sphere
     integer shininess uniform in `shininess`; sun plus point lights at
     uniform positions rejected when within 0.5 of a sphere surface."""
     rng = Rng(seed)
     s = Scene()
-    for t in range(n_textures):
-        s.textures.append(texture_value_noise(seed * 1000 + t, tex_size))
+    if textures is not None:  # shared, prebuilt texture set
+        s.textures = list(textures)
+        n_textures = len(textures)
+    else:
+        for t in range(n_textures):
+            s.textures.append(texture_value_noise(seed * 1000 + t, tex_size))
     centres = rng.uniform(-box, box, 3 * n_spheres).reshape(n_spheres, 3).astype(np.float32)
     radii = rng.uniform(r_min, r_max, n_spheres)
     tex_ids = rng.integers(0, n_textures - 1, n_spheres)
@@ -575,3 +580,39 @@ def grid_scene(n: int = 40, extent: float = 10.0, seed: int = 6) -> Scene:
     s.add_primitive(node, TRIANGLES, 0, pos, nrm, uv, np.asarray(idx, np.uint32))
     s.point_lights = [(0.0, 1.0, -3.0, 2.0)]
     return s.finalize()
+
+
+SERVE_TRIANGLES = (10_000, 50_000, 100_000, 250_000, 500_000, 800_000, 1_200_000, 2_000_000)
+
+
+def serving_scenes(seed: int = 50, tex_size: int = 1024):
+    """Eight scenes built like the 200-sphere scene with ceil(T / 4096) spheres
+    for T in SERVE_TRIANGLES; they share one set of 8 value-noise textures."""
+    textures = [texture_value_noise(seed * 1000 + t, tex_size) for t in range(8)]
+    out = []
+    for k, t in enumerate(SERVE_TRIANGLES):
+        n = -(-t // 4096)
+        out.append(spheres_scene(n_spheres=n, seed=seed + 1 + k, textures=textures))
+    return out
+
+
+def serving_requests(n: int, seed: int = 60, rate: float = 2000.0, n_scenes: int = 8, radius: float = 35.0,
+                     min_wh=(64, 64), max_wh=(3840, 2160), dof_p: float = 0.5):
+    """A seeded request stream: Poisson arrivals at `rate`/s, a uniform scene,
+    a camera on a sphere of `radius`, viewport sides log-uniform between
+    min_wh and max_wh, depth of field with probability dof_p (focus 20,
+    aperture 0.05, at most 16 px).  Returns [(arrival_s, scene_index, View)]."""
+    rng = Rng(seed)
+    t = 0.0
+    out = []
+    for _ in range(n):
+        u = rng.uniform(0.0, 1.0, 1)[0]
+        t += -math.log(1.0 - u) / rate
+        k = int(rng.integers(0, n_scenes - 1, 1)[0])
+        w = log_uniform_int(rng, min_wh[0], max_wh[0])
+        h = log_uniform_int(rng, min_wh[1], max_wh[1])
+        m, c = camera_on_sphere(rng, radius)
+        v = view_for(w, h, m, c)
+        v.dof = bool(rng.uniform(0.0, 1.0, 1)[0] < dof_p)
+        out.append((t, k, v))
+    return out
