@@ -203,6 +203,20 @@ SGL_API sgl_status sgl_scene_info(sgl_ctx *ctx, int scene_id, uint64_t *n_triang
 SGL_API sgl_status sgl_render(sgl_ctx *ctx, int scene_id, const sgl_view *views, const sgl_target *targets,
                               int n_views, int device_buffers, void *stream, sgl_frame_stats *stats);
 
+/* sgl_render for one view, for callers that must not allocate: a real-time
+ * frame callback with a fixed memory plan, or a host that forbids the library
+ * from growing its footprint or from taking the device-wide synchronisation
+ * of cudaMalloc / cudaFree.  No counterpart in the reference (its render call
+ * allocates nothing on a GPU because it has none).  All scratch comes from one
+ * 64 MiB static device array that every GPU loading the library keeps until
+ * exit; views needing more are refused with SGL_ERR_BUDGET.  Targets are
+ * device buffers; asynchronous on `stream`.  The array is shared: calls that
+ * overlap on the GPU race, so order them.  The first call on a device looks
+ * up the array's address (cudaGetSymbolAddress); make it before any stream
+ * capture. */
+SGL_API sgl_status sgl_render_noalloc(sgl_ctx *ctx, int scene_id, const sgl_view *view, const sgl_target *target,
+                                      void *stream);
+
 /* Debug variant of one view: writes the per-pixel winner slot
  * (2 * draw-order triangle index + clip sub-triangle, 0xFFFFFFFF = none) and
  * the per-slot "reached scanline setup" flags, used to check depth-test

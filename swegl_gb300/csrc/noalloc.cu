@@ -1,0 +1,205 @@
+// noalloc.cu — sgl_render_noalloc: the plain renderer for callers that must
+// not allocate memory.
+//
+// Who needs it: code that runs where allocation is not allowed or not safe —
+// a real-time frame callback with a fixed memory plan, a host application that
+// hands the renderer a pre-sized device buffer and forbids the library from
+// growing its footprint, or code that must not take the allocator's implicit
+// device-wide synchronisation (cudaMalloc / cudaFree stall every stream).
+// Such a caller cannot use sgl_render, whose per-view scratch (depth keys,
+// winner records, triangle lists, span bins, descriptors) lives in
+// library-owned buffers that grow on demand.
+//
+// Here all of that scratch comes from one file-scope device array of
+// kNoAllocScratchBytes (64 MiB).  Every GPU that loads the library holds it
+// until the process exits.  Views whose scratch does not fit are refused with
+// SGL_ERR_BUDGET and a message giving the bytes needed.  The call makes no
+// cudaMalloc, cudaFree or other allocating call; its descriptors are built on
+// the host stack and copied into the array.
+//
+// The array is shared by every call on a device and keeps the last call's
+// contents; the counters that must start at zero are cleared by each call
+// (the depth keys and visibility flags are cleared by the kernels).  Calls
+// that overlap on the GPU — on different streams, or from different contexts
+// of the same device — race on the array: the caller must order them.
+//
+// Set-up: the first call on a device, with that device current, looks up the
+// array's device address with cudaGetSymbolAddress (the array's name is only
+// a host-side stand-in) and caches it for that device.  Make that first call
+// before any stream capture.
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include <cuda_runtime.h>
+
+#include "sgl.h"
+#include "sgl_internal.h"
+#include "sgl_runtime.h"
+
+namespace sgl {
+
+constexpr size_t kNoAllocScratchBytes = 64ull << 20;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_addr[kNoAllocMaxDevices];
+
+// The device address of the scratch array on `device` (which must be current).
+static cudaError_t noalloc_scratch(int device, unsigned char **out)
+{
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return e;
+        g_noalloc_addr[device] = p;
+    }
+    *out = (unsigned char *)g_noalloc_addr[device];
+    return cudaSuccess;
+}
+
+static size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+} // namespace sgl
+
+using namespace sgl;
+
+extern "C" {
+
+SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *view, const sgl_target *target,
+                                      void *stream)
+{
+    Ctx *ctx = reinterpret_cast<Ctx *>(c);
+    if (!ctx || !view || !target)
+        return SGL_ERR_INVALID;
+    Scene *s = ctx->find(scene_id);
+    if (!s) {
+        ctx->fail("unknown scene %d", scene_id);
+        return SGL_ERR_NOT_FOUND;
+    }
+    sgl_status r = check_view(ctx, *view, *target);
+    if (r != SGL_OK)
+        return r;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) {
+        ctx->fail("cudaSetDevice(%d) failed", ctx->device);
+        return SGL_ERR_CUDA;
+    }
+    const sgl_view &v = *view;
+    const size_t px = (size_t)v.w * v.h;
+    const size_t nv = s->n_vertices, nt = s->n_triangles;
+    const bool dof = v.dof.enabled != 0;
+    const int tile = ctx->tile;
+    const size_t tiles = (size_t)((v.w + tile - 1) / tile) * (size_t)((v.h + tile - 1) / tile);
+    // layout of the scratch array
+    size_t off = 0;
+    const size_t o_batch = off;
+    off += up256(sizeof(BatchDev));
+    const size_t o_item = off;
+    off += up256(sizeof(ItemDev));
+    const size_t o_bases = off;
+    off += up256(8 * sizeof(uint32_t));
+    const size_t o_counters = off;
+    off += up256(kCounterWords * sizeof(unsigned long long));
+    const size_t o_item_counters = off;
+    off += up256(2 * sizeof(unsigned long long));
+    const size_t o_ndc = off;
+    off += up256(16 * nv);
+    const size_t o_yes = off;
+    off += up256(nv);
+    const size_t o_key = off;
+    off += up256(8 * px);
+    const size_t o_prec = off;
+    off += up256(16 * px);
+    const size_t o_clippx = off;
+    off += up256(8 * px);
+    const size_t o_list = off;
+    off += up256(8 * (nt ? nt : 1));
+    const size_t o_dof = off;
+    off += dof ? up256(8 * px) : 0;
+    const size_t o_spans = off;
+    const size_t min_spans = 4096;
+    const size_t need = o_spans + min_spans * sizeof(SpanRec);
+    if (need > kNoAllocScratchBytes || px >= (1ull << 32) || tiles >= (1ull << 32)) {
+        ctx->fail("sgl_render_noalloc: this view of scene %d needs %zu bytes of scratch; the static scratch "
+                  "holds %zu bytes (use sgl_render, or a smaller view or scene)",
+                  scene_id, need, kNoAllocScratchBytes);
+        return SGL_ERR_BUDGET;
+    }
+    unsigned char *base = nullptr;
+    cudaError_t e = noalloc_scratch(ctx->device, &base);
+    if (e != cudaSuccess) {
+        ctx->fail("sgl_render_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        return SGL_ERR_CUDA;
+    }
+    const uint32_t span_cap = (uint32_t)((kNoAllocScratchBytes - o_spans) / sizeof(SpanRec));
+    ItemDev it{};
+    it.s = s->dev;
+    it.v = make_view(v);
+    it.ndc = (float4 *)(base + o_ndc);
+    it.yes = base + o_yes;
+    it.key = (unsigned long long *)(base + o_key);
+    it.prec = (float4 *)(base + o_prec);
+    it.pixels = (uint32_t *)target->pixels + (size_t)v.y * (target->pitch / 4) + v.x;
+    it.pitch_px = target->pitch / 4;
+    it.zbuf = target->zbuffer;
+    it.tiles_x = (v.w + tile - 1) / tile;
+    it.tile_base = 0;
+    if (dof) {
+        const sgl_dof_desc &d = v.dof;
+        it.dof = 1;
+        it.dof_out = it.pixels;
+        it.dof_pitch = it.pitch_px;
+        it.pixels = (uint32_t *)(base + o_dof);
+        it.pitch_px = v.w;
+        if (!it.zbuf)
+            it.zbuf = (float *)(base + o_dof + 4 * px);
+        const float k = d.px_scale > 0.0f ? d.px_scale : (v.proj[5] * (float)v.h) / 2.0f;
+        it.dof_focus = d.focus;
+        it.dof_ka = k * d.aperture;
+        it.dof_rmax = d.max_radius;
+        it.p22 = v.proj[10];
+        it.p23 = v.proj[11];
+    }
+    const uint32_t bases[8] = {0u, (uint32_t)nv, 0u, (uint32_t)nt, 0u, (uint32_t)px, 0u, (uint32_t)tiles};
+    BatchDev b{};
+    b.items = (const ItemDev *)(base + o_item);
+    b.vtx_base = (const uint32_t *)(base + o_bases);
+    b.tri_base = b.vtx_base + 2;
+    b.px_base = b.vtx_base + 4;
+    b.tile_base = b.vtx_base + 6;
+    b.n_items = 1;
+    b.inline_span = ctx->inline_span;
+    b.total_vtx = (uint32_t)nv;
+    b.total_tri = (uint32_t)nt;
+    b.total_px = (uint32_t)px;
+    b.total_tiles = (uint32_t)tiles;
+    b.list = (uint2 *)(base + o_list);
+    b.list_cap = (uint32_t)(nt ? nt : 1);
+    b.clip = b.list;
+    b.clip_cap = b.list_cap;
+    b.clippx = (uint2 *)(base + o_clippx);
+    b.clippx_cap = (uint32_t)(px ? px : 1);
+    b.spans = (SpanRec *)(base + o_spans);
+    b.span_cap = span_cap;
+    b.counters = (unsigned long long *)(base + o_counters);
+    b.item_counters = (unsigned long long *)(base + o_item_counters);
+    b.slot_flags = nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    // descriptors from the host stack (pageable copies return once staged)
+    CUDA_TRY(cudaMemcpyAsync(base + o_item, &it, sizeof it, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(base + o_bases, bases, sizeof bases, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(base + o_batch, &b, sizeof b, cudaMemcpyHostToDevice, st));
+    // the counters must start at zero on every call
+    CUDA_TRY(cudaMemsetAsync(base + o_counters, 0, kCounterWords * sizeof(unsigned long long), st));
+    CUDA_TRY(cudaMemsetAsync(base + o_item_counters, 0, 2 * sizeof(unsigned long long), st));
+    CUDA_TRY(launch_batch((const BatchDev *)(base + o_batch), tile, dof, st, nullptr, nullptr));
+    return SGL_OK;
+}
+
+} // extern "C"

@@ -58,6 +58,7 @@ def library() -> C.CDLL:
                                   P(abi.FrameStats)], C.c_int),
             "sgl_autotune": ([C.c_void_p, P(abi.BatchItem), C.c_int, P(abi.BatchOpts)], C.c_int),
             "sgl_dof": ([C.c_void_p, P(abi.ViewDesc), P(abi.Target), P(abi.Target), C.c_int, C.c_void_p], C.c_int),
+            "sgl_render_noalloc": ([C.c_void_p, C.c_int, P(abi.ViewDesc), P(abi.Target), C.c_void_p], C.c_int),
             "sgl_server_create": ([C.c_void_p, P(abi.ServeOpts), P(C.c_void_p)], C.c_int),
             "sgl_server_submit": ([C.c_void_p, P(abi.Request), P(C.c_uint64)], C.c_int),
             "sgl_server_poll": ([C.c_void_p, C.c_uint64, P(abi.RequestResult)], C.c_int),
