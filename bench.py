@@ -159,20 +159,27 @@ def device_target(torch, w: int, h: int):
     return (pix, zb), t
 
 
-def max_over_ranks(torch, dist, x: float) -> float:
+def max_over_ranks(torch, dist, x: float, device: str = "cuda") -> float:
+    """Replicas: the job's time is the slowest rank's."""
     if not dist:
         return x
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    t = torch.tensor([x], device=device, dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
 
-def sum_over_ranks(torch, dist, x: float) -> float:
+def sum_over_ranks(torch, dist, x: float, device: str = "cuda") -> float:
     if not dist:
         return x
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    t = torch.tensor([x], device=device, dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def replica_throughput(frames_per_rank: int, world: int, max_ms: float) -> float:
+    """Whole-job frames/s of independent replicas: all ranks' frames over the
+    slowest rank's time."""
+    return world * frames_per_rank / (max_ms / 1e3)
 
 
 # ------------------------------------------------------- single-frame stage --
@@ -362,7 +369,7 @@ def run_serve(args, rank, world, local_rank):
     b1 = srv.stats()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = max_over_ranks(torch, dist, sum(step_ms))
-    value = world * args.steps * M / (total_ms / 1e3)
+    value = replica_throughput(args.steps * M, world, total_ms)
     timed = reqs[args.warmup * M:]
 
     # sequential one-frame-per-launch on the same requests (a bounded prefix)
