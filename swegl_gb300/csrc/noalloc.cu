@@ -18,8 +18,9 @@
 // the host stack and copied into the array.
 //
 // The array is shared by every call on a device and keeps the last call's
-// contents; the counters that must start at zero are cleared by each call
-// (the depth keys and visibility flags are cleared by the kernels).  Calls
+// contents; each call clears what must start cleared (the counters, and the
+// depth keys to all ones) with cudaMemsetAsync; the visibility flags are
+// cleared by the kernels.  Calls
 // that overlap on the GPU — on different streams, or from different contexts
 // of the same device — race on the array: the caller must order them.
 //
@@ -116,10 +117,12 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     off += up256(8 * px);
     const size_t o_prec = off;
     off += up256(16 * px);
-    const size_t o_clippx = off;
-    off += up256(8 * px);
     const size_t o_list = off;
     off += up256(8 * (nt ? nt : 1));
+    const size_t o_recs = off;
+    off += up256(sizeof(TriRec) * (nt ? nt : 1));
+    const size_t o_recmap = off;
+    off += up256(4 * (nt ? nt : 1));
     const size_t o_dof = off;
     off += dof ? up256(8 * px) : 0;
     const size_t o_spans = off;
@@ -183,8 +186,9 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     b.list_cap = (uint32_t)(nt ? nt : 1);
     b.clip = b.list;
     b.clip_cap = b.list_cap;
-    b.clippx = (uint2 *)(base + o_clippx);
-    b.clippx_cap = (uint32_t)(px ? px : 1);
+    b.recs = (TriRec *)(base + o_recs);
+    b.recmap = (uint32_t *)(base + o_recmap);
+    b.keep_keys = 0;
     b.spans = (SpanRec *)(base + o_spans);
     b.span_cap = span_cap;
     b.counters = (unsigned long long *)(base + o_counters);
@@ -198,6 +202,8 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     // the counters must start at zero on every call
     CUDA_TRY(cudaMemsetAsync(base + o_counters, 0, kCounterWords * sizeof(unsigned long long), st));
     CUDA_TRY(cudaMemsetAsync(base + o_item_counters, 0, 2 * sizeof(unsigned long long), st));
+    CUDA_TRY(cudaMemsetAsync(base + o_key, 0xFF, 8 * px, st)); // kEmptyKey
+
     CUDA_TRY(launch_batch((const BatchDev *)(base + o_batch), tile, dof, st, nullptr, nullptr));
     return SGL_OK;
 }

@@ -5,17 +5,17 @@
 // totals from device memory, so one launch sequence (and one CUDA graph)
 // serves any batch.  The plain one-frame-per-launch renderer is a batch of one.
 //
-//   k_clear       per pixel: depth key cleared (viewport_t::clear, viewport.cpp:88-113)
 //   k_vertex      world -> view -> projection, |z'| divide      (vertex_shaders.hpp:35-52)
 //   k_flags       visibility flags of triangles                  (renderer.cpp:86-185)
-//   k_compact     drawable triangles -> one list grouped by row class / near-clip list
-//   k_walk        depth walk: fragment keys folded with atomicMin
+//   k_compact     drawable triangles -> the walk list / the near-clip list
+//   k_walk        per triangle set-up (TriRec), rows dealt across each warp's
+//                 lanes, fragment keys folded with atomicMin
 //   k_walk_clip   the same for triangles crossing the near plane (rare)
 //   k_spans<0>    long spans binned by the walk, one warp each
 //   k_spans<1>, k_walk_clip<1>   winner records for binned spans and clipped triangles
 //   k_walk_winner winner records of every span, only after a bin overflow
-//   k_shade       per pixel: background or the winner's colour, and depth
-//   k_shade_clip  winners that belong to near-clipped triangles (rare)
+//   k_shade       per pixel: background or the winner's colour, and depth;
+//                 winners are queued so that shading runs on full warps
 //   k_dof         depth-of-field gather of the items that ask for it
 //
 // Depth test.  The reference draws triangles in order and keeps a fragment
@@ -24,9 +24,11 @@
 // key (float bits of z << 32 | draw slot) into its pixel with atomicMin: z is
 // above 0.001, so its bits order like the floats, and the draw slot
 // (2 * draw-order triangle + clip sub-triangle) breaks ties in draw order.
-// The shade kernel then replays the winner's row and pixel steps to recover
-// the progress values the reference shaded with; spans too long to replay
-// cheaply have them recorded by the span kernels instead.
+// The shade kernel then replays the winner's row and pixel steps from the
+// triangle's set-up record to recover the progress values the reference
+// shaded with; spans too long to replay cheaply have them recorded by the
+// span kernels instead.  The depth keys start every launch sequence empty:
+// new key pools are filled once and the shade kernel empties what it reads.
 #include <cstdint>
 
 #include "sgl_device.cuh"
@@ -91,28 +93,43 @@ __global__ void k_world(SceneDev s)
     s.uv[g] = make_float2(p.w, q.w);
 }
 
-__global__ void __launch_bounds__(256) k_clear(const BatchDev *b)
-{
-    for_each_in_items(b, b->px_base, b->total_px,
-                      [&](int item, uint32_t i) { b->items[item].key[i] = kEmptyKey; });
-}
-
 // world_to_camera_or_frustum (vertex_shaders.hpp:35-52): view, projection
-// (rows 0-2), x and y divided by |z'|; also clears the visibility flag.
+// (rows 0-2), x and y divided by |z'|; also clears the visibility flag.  The
+// item's matrices stay in registers while the grid-stride index is inside it.
 __global__ void __launch_bounds__(256) k_vertex(const BatchDev *b)
 {
-    for_each_in_items(b, b->vtx_base, b->total_vtx, [&](int item, uint32_t g) {
-        const ItemDev &it = b->items[item];
-        const float4 w = it.s.wpos[g];
-        V3 p = transform3(mk3(w.x, w.y, w.z), it.v.view);
-        p = transform3(p, it.v.proj);
+    uint32_t lo = 0, hi = 0;
+    float m[24];
+    const float4 *wpos = nullptr;
+    float4 *ndc = nullptr;
+    uint8_t *yes = nullptr;
+    const uint32_t total = b->total_vtx;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        if (g < lo || g >= hi) {
+            const int item = find_item(b->vtx_base, b->n_items, g);
+            lo = __ldg(b->vtx_base + item);
+            hi = __ldg(b->vtx_base + item + 1);
+            const ItemDev &it = b->items[item];
+#pragma unroll
+            for (int k = 0; k < 12; k++) {
+                m[k] = it.v.view[k];
+                m[12 + k] = it.v.proj[k];
+            }
+            wpos = it.s.wpos;
+            ndc = it.ndc;
+            yes = it.yes;
+        }
+        const uint32_t l = g - lo;
+        const float4 w = wpos[l];
+        V3 p = transform3(mk3(w.x, w.y, w.z), m);
+        p = transform3(p, m + 12);
         if (p.z != 0.0f) {
             p.x = p.x / fabsf(p.z);
             p.y = p.y / fabsf(p.z);
         }
-        it.ndc[g] = make_float4(p.x, p.y, p.z, 0.0f);
-        it.yes[g] = 0;
-    });
+        ndc[l] = make_float4(p.x, p.y, p.z, 0.0f);
+        yes[l] = 0;
+    }
 }
 
 // inside_camera_frustum (src/render/renderer.cpp:58-70)
@@ -134,20 +151,39 @@ __device__ __forceinline__ V3 ld3(const float4 *a, uint32_t i)
 // or front facing, front_face_visible :72-75, on the draw-order triple).
 __global__ void __launch_bounds__(256) k_flags(const BatchDev *b)
 {
-    for_each_in_items(b, b->tri_base, b->total_tri, [&](int item, uint32_t t) {
-        const ItemDev &it = b->items[item];
-        const uint4 tri = it.s.tris[t];
-        const V3 a = ld3(it.ndc, tri.x), c1 = ld3(it.ndc, tri.y), c2 = ld3(it.ndc, tri.z);
-        if (!inside_frustum(a, c1, c2))
-            return;
-        const int m = it.s.prims[tri.w].material;
-        const int ds = (m >= 0 && m < it.s.n_mats) ? it.s.mats[m].double_sided : 0;
-        if (ds || cross_n_z(sub3(c1, a), sub3(c2, a)) > 0.0f) {
-            it.yes[tri.x] = 1;
-            it.yes[tri.y] = 1;
-            it.yes[tri.z] = 1;
+    uint32_t lo = 0, hi = 0;
+    const uint4 *tris = nullptr;
+    const float4 *ndc = nullptr;
+    uint8_t *yes = nullptr;
+    const PrimDesc *prims = nullptr;
+    const MatDesc *mats = nullptr;
+    int n_mats = 0;
+    const uint32_t total = b->total_tri;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        if (g < lo || g >= hi) {
+            const int item = find_item(b->tri_base, b->n_items, g);
+            lo = __ldg(b->tri_base + item);
+            hi = __ldg(b->tri_base + item + 1);
+            const ItemDev &it = b->items[item];
+            tris = it.s.tris;
+            ndc = it.ndc;
+            yes = it.yes;
+            prims = it.s.prims;
+            mats = it.s.mats;
+            n_mats = it.s.n_mats;
         }
-    });
+        const uint4 tri = tris[g - lo];
+        const V3 a = ld3(ndc, tri.x), c1 = ld3(ndc, tri.y), c2 = ld3(ndc, tri.z);
+        if (!inside_frustum(a, c1, c2))
+            continue;
+        const int m = prims[tri.w].material;
+        const int ds = (m >= 0 && m < n_mats) ? mats[m].double_sided : 0;
+        if (ds || cross_n_z(sub3(c1, a), sub3(c2, a)) > 0.0f) {
+            yes[tri.x] = 1;
+            yes[tri.y] = 1;
+            yes[tri.z] = 1;
+        }
+    }
 }
 
 // frustum_to_viewport (viewport.cpp:123-129) of a flagged vertex
@@ -157,38 +193,24 @@ __device__ __forceinline__ V3 load_vp(const ItemDev &it, uint32_t g)
     return mk3(it.v.vm00 * n.x + it.v.vm03, it.v.vm11 * n.y + it.v.vm13, n.z);
 }
 
-// Rows of fill_triangle_2's scanline range from the three screen y values:
-// ceil(max y) - ceil(min y) (renderer.cpp:390-394).  The compaction uses it to
-// class triangles, and the shade kernel to know which triangles had every
-// span binned; both evaluate it the same way.
-__device__ __forceinline__ int row_extent(float ya, float yb, float yc)
-{
-    const float lo = fminf(ya, fminf(yb, yc)), hi = fmaxf(ya, fmaxf(yb, yc));
-    const int a = f2i(ceilf(lo)), b = f2i(ceilf(hi));
-    return (b - a) < 0 ? 0x7FFFFFFF : (b - a);
-}
-
-__device__ __forceinline__ int row_class(int rows)
-{
-    return rows <= 2 ? 0 : rows <= 4 ? 1 : rows <= 8 ? 2 : rows <= kTallRows ? 3 : 4;
-}
-
 // Drawable triangles (all three vertices flagged, renderer.cpp:248-253) into
-// one list, each block's entries grouped by row class so that a warp of the
-// walk gets triangles of similar size; triangles crossing the near plane go to
-// their own list.  One global atomic per list per block.
+// the walk list; triangles crossing the near plane go to their own list and
+// are marked in the record map.  One global atomic per list per block.
 constexpr int kCompactBlock = 512;
 __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
 {
-    __shared__ uint32_t cnt[kClasses + 1], cls_off[kClasses], base[2];
+    __shared__ uint32_t cnt[2], base[2];
     const int lane = threadIdx.x & 31;
     int item = -1;
     uint32_t lo = 0, hi = 0;
+    const uint4 *tris = nullptr;
+    const float4 *ndc = nullptr;
+    const uint8_t *yes = nullptr;
     const uint32_t total = b->total_tri;
     // every thread of the block runs the same number of iterations (barriers inside)
-    const uint32_t span = gridDim.x * blockDim.x;
-    for (uint32_t g0 = blockIdx.x * blockDim.x; g0 < total; g0 += span) {
-        if (threadIdx.x < kClasses + 1)
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t g0 = blockIdx.x * blockDim.x; g0 < total; g0 += stride) {
+        if (threadIdx.x < 2)
             cnt[threadIdx.x] = 0;
         __syncthreads();
         const uint32_t g = g0 + threadIdx.x;
@@ -199,23 +221,22 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
                 item = find_item(b->tri_base, b->n_items, g);
                 lo = __ldg(b->tri_base + item);
                 hi = __ldg(b->tri_base + item + 1);
+                const ItemDev &it = b->items[item];
+                tris = it.s.tris;
+                ndc = it.ndc;
+                yes = it.yes;
             }
             t = g - lo;
-            const ItemDev &it = b->items[item];
-            const uint4 tri = it.s.tris[t];
-            if (it.yes[tri.x] && it.yes[tri.y] && it.yes[tri.z]) {
-                const float4 a = it.ndc[tri.x], c1 = it.ndc[tri.y], c2 = it.ndc[tri.z];
+            const uint4 tri = tris[t];
+            if (yes[tri.x] && yes[tri.y] && yes[tri.z]) {
                 // fill_triangle's cases (renderer.cpp:281-318): the smallest z' decides
-                if (below_near(a.z) || below_near(c1.z) || below_near(c2.z))
-                    list = kClasses;
-                else
-                    list = row_class(row_extent(it.v.vm11 * a.y + it.v.vm13, it.v.vm11 * c1.y + it.v.vm13,
-                                                it.v.vm11 * c2.y + it.v.vm13));
+                const float za = ndc[tri.x].z, zb = ndc[tri.y].z, zc = ndc[tri.z].z;
+                list = (below_near(za) || below_near(zb) || below_near(zc)) ? 1 : 0;
             }
         }
         uint32_t pos = 0;
 #pragma unroll
-        for (int k = 0; k <= kClasses; k++) {
+        for (int k = 0; k < 2; k++) {
             const unsigned m = __ballot_sync(0xFFFFFFFFu, list == k);
             if (!m)
                 continue;
@@ -228,24 +249,20 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            uint32_t run = 0;
-            for (int k = 0; k < kClasses; k++) {
-                cls_off[k] = run;
-                run += cnt[k];
-            }
             uint32_t *c32 = reinterpret_cast<uint32_t *>(b->counters);
-            base[0] = run ? atomicAdd(&c32[C_LIST], run) : 0u;
-            base[1] = cnt[kClasses] ? atomicAdd(&c32[C_CLIP], cnt[kClasses]) : 0u;
+            base[0] = cnt[0] ? atomicAdd(&c32[C_LIST], cnt[0]) : 0u;
+            base[1] = cnt[1] ? atomicAdd(&c32[C_CLIP], cnt[1]) : 0u;
         }
         __syncthreads();
-        if (list == kClasses) {
+        if (list == 1) {
             const uint32_t j = base[1] + pos;
             if (j < b->clip_cap)
                 b->clip[b->clip_cap - 1 - j] = make_uint2(t, (uint32_t)item); // filled from the end
-        } else if (list >= 0) {
-            const uint32_t j = base[0] + cls_off[list] + pos;
+            b->recmap[g] = kRecClip;
+        } else if (list == 0) {
+            const uint32_t j = base[0] + pos;
             if (j < b->list_cap)
-                b->list[j] = make_uint2(t, (uint32_t)item | ((uint32_t)list << 24));
+                b->list[j] = make_uint2(t, (uint32_t)item);
         }
         __syncthreads();
     }
@@ -471,36 +488,6 @@ struct WinnerVisitor {
     }
 };
 
-// Replays one triangle's walk up to pixel (tx, ty) to recover the progress
-// values the reference had there: the edge progress of the row and the qpixel
-// progress after (tx - x1) steps (renderer.cpp:474-493).  Spans wider than
-// the inline limit were recorded by the span kernels instead (use_prec).
-struct ReplayVisitor {
-    int tx, ty;
-    int inline_span;
-    bool found, use_prec;
-    float4 rec;
-
-    __device__ __forceinline__ bool active() const { return !found && !use_prec; }
-    __device__ __forceinline__ void drawn() {}
-    __device__ __forceinline__ void span(int y, int x1, int x2, const Side &Ls, const Side &Rs, uint32_t bits)
-    {
-        if (y != ty || tx < x1 || tx >= x2)
-            return;
-        if (x2 - x1 > inline_span) {
-            use_prec = true;
-            return;
-        }
-        Interp q;
-        q.init_self(Rs.x - Ls.x, Ls.it.value(), Rs.it.value());
-        q.displace((float)x1 - Ls.x);
-        for (int x = x1; x < tx; x++)
-            q.step();
-        rec = make_float4(q.alpha, Ls.it.alpha, Rs.it.alpha, __uint_as_float(bits));
-        found = true;
-    }
-};
-
 // Per-item counters of a warp: lanes grouped by item, one atomic per group.
 __device__ __forceinline__ void item_add(unsigned long long *dst, uint32_t item, unsigned long long v, bool valid)
 {
@@ -523,33 +510,455 @@ __device__ __forceinline__ void warp_add(unsigned long long *dst, unsigned long 
         atomicAdd(dst, v);
 }
 
-// Depth walk of the drawable triangles wholly in front of the near plane:
-// fill_triangle's normal case (renderer.cpp:281-285), one sub-triangle, slot 2t.
-__global__ void __launch_bounds__(128, 8) k_walk(const BatchDev *b)
+// ------------------------------------------------------- row-parallel walk --
+//
+// The walk of fill_triangle_2 is serial only along its edges: row k needs the
+// edges after k steps (x += ratio, top += tstep, bottom += bstep, renderer.cpp
+// :553-556), and each span needs the qpixel chain from its left end.  The
+// steps are float additions, so any thread can reach row k by repeating them
+// from the set-up; the divisions of a row (edge progress, span set-up) and of
+// its pixels then run wherever that row is.  A warp takes 32 triangles, each
+// lane makes its triangle's set-up (the TriRec), and the warp's rows are
+// dealt out across the lanes.  Triangles with more than kTallRows rows are
+// walked by the whole warp, 32 rows at a time, and every one of their spans
+// goes to the long-span kernels.
+
+constexpr int kWalkWarps = 4;
+// Per-warp shared copy of the lanes' set-ups, sm[field][lane]: fields 0-31 are
+// the words of TriRec in order, so the warp can store whole records; the row
+// is padded to 33 words so that both the per-lane and the per-record accesses
+// are free of bank conflicts.
+enum {
+    F_LX, F_LT, F_LB, F_LR, F_LTS, F_LBS, // long edge: x, top, bottom, ratio, tstep, bstep
+    F_UX, F_UT, F_UB, F_UR, F_UTS, F_UBS, // upper short edge
+    F_DX, F_DT, F_DB, F_DR, F_DTS, F_DBS, // lower short edge
+    F_Z0, F_Z1, F_Z2, F_YS, F_YL, F_NU, F_ND, F_FLAGS, F_SLOT, F_ITEM, F_G0, F_G1, F_G2, F_PRIM,
+    F_FRAGS, kWalkFields
+};
+constexpr int kWalkPitch = 33;
+static_assert(F_PRIM == 31 && sizeof(TriRec) == 32 * sizeof(uint32_t), "shared set-up fields follow TriRec");
+
+// interpolator_g<1>::InitSelf then DisplaceStartingPoint (interpolator.hpp:
+// 60-84), with 1/z1 and 1/z2 passed in (the same divisions, made once per
+// vertex).  The progress of the displaced state is not formed here: every
+// reader divides top by bottom itself, as step() would have.
+__device__ __forceinline__ void edge_init(float dist, float rz1, float rz2, float move, float &top, float &bot,
+                                          float &ts, float &bs)
 {
+    const float alphastep = 1.0f / dist;
+    bot = rz1;
+    top = 0.0f;
+    top = top * bot;
+    ts = (1.0f * rz2 - top) * alphastep;
+    bs = (rz2 - bot) * alphastep;
+    top = top + ts * move;
+    bot = bot + bs * move;
+}
+
+// The inputs of one walked row: both edges at the half's first row with
+// their constants, the steps to take, the row and its span bits.
+struct RowIn {
+    float lx, lt, lb, lr, lts, lbs, lz, ldv; // long edge; value() = lz + ldv * progress
+    float sx, st, sb, sr, sts, sbs, sz, sdv; // short edge of the row's half
+    int y, ls, ss;
+    bool llr;
+    uint32_t bits;
+};
+
+// Row k of a set-up (k < n_u: upper half): `lg` is the long edge (x, top,
+// bottom, ratio, tstep, bstep), `sh` the short edge of the row's half.
+__device__ __forceinline__ void row_in(RowIn &r, int k, const float lg[6], const float sh[6], float z0, float z1,
+                                       float z2, int y_s, int y_l, int n_u, uint32_t flags)
+{
+    r.lx = lg[0]; r.lt = lg[1]; r.lb = lg[2]; r.lr = lg[3]; r.lts = lg[4]; r.lbs = lg[5];
+    r.sx = sh[0]; r.st = sh[1]; r.sb = sh[2]; r.sr = sh[3]; r.sts = sh[4]; r.sbs = sh[5];
+    r.lz = z0;
+    r.ldv = z2 - z0;
+    r.ls = k;
+    if (k < n_u) {
+        r.sz = z0;
+        r.sdv = z1 - z0;
+        r.y = y_s + k;
+        r.ss = k;
+        r.llr = (flags & kRecLLRUpper) != 0u;
+        r.bits = r.llr ? kBitLLR : 0u;
+    } else {
+        r.sz = z1;
+        r.sdv = z2 - z1;
+        r.y = y_l + (k - n_u);
+        r.ss = k - n_u;
+        r.llr = (flags & kRecLLRLower) != 0u;
+        r.bits = kBitLower | (r.llr ? kBitLLR : 0u);
+    }
+}
+
+// A row after its steps: the span [x1, x2) clipped to the viewport
+// (renderer.cpp:466-472) and the left and right edge (Ls, Rs).
+struct RowSpan {
+    int x1, x2;
+    float Lx, Lt, Lb, Lz, Ldv, Rx, Rt, Rb, Rz, Rdv;
+};
+
+__device__ __forceinline__ void row_span(RowIn &r, const ViewDev &v, RowSpan &o)
+{
+    for (int k = 0; k < r.ls; k++) {
+        r.lx = r.lx + r.lr;
+        r.lt = r.lt + r.lts;
+        r.lb = r.lb + r.lbs;
+    }
+    for (int k = 0; k < r.ss; k++) {
+        r.sx = r.sx + r.sr;
+        r.st = r.st + r.sts;
+        r.sb = r.sb + r.sbs;
+    }
+    if (r.llr) {
+        o.Lx = r.sx; o.Lt = r.st; o.Lb = r.sb; o.Lz = r.sz; o.Ldv = r.sdv;
+        o.Rx = r.lx; o.Rt = r.lt; o.Rb = r.lb; o.Rz = r.lz; o.Rdv = r.ldv;
+    } else {
+        o.Lx = r.lx; o.Lt = r.lt; o.Lb = r.lb; o.Lz = r.lz; o.Ldv = r.ldv;
+        o.Rx = r.sx; o.Rt = r.st; o.Rb = r.sb; o.Rz = r.sz; o.Rdv = r.sdv;
+    }
+    o.x1 = f2i(ceilf(o.Lx));
+    if (o.x1 < v.x)
+        o.x1 = v.x;
+    o.x2 = f2i(ceilf(o.Rx));
+    if (o.x2 > v.x + v.w)
+        o.x2 = v.x + v.w;
+}
+
+// The qpixel interpolator of a span after its displacement to x1, and the
+// progress of both edges (renderer.cpp:474-480, prepare_for_scanline).
+__device__ __forceinline__ void span_interp(const RowSpan &o, Interp &q, float &pl, float &pr)
+{
+    pl = o.Lt / o.Lb;
+    pr = o.Rt / o.Rb;
+    q.init_self(o.Rx - o.Lx, o.Lz + o.Ldv * pl, o.Rz + o.Rdv * pr);
+    q.displace((float)o.x1 - o.Lx);
+}
+
+// Bins the spans of the lanes that ask for it (one atomic per warp).  Every
+// lane of the warp calls it; returns whether this lane's span was binned.
+__device__ __forceinline__ bool bin_span_warp(const BatchDev *b, bool want, uint32_t item, uint32_t slot, int y,
+                                              const RowSpan &o, const Interp &q, float pl, float pr, uint32_t bits)
+{
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, want);
+    if (!m)
+        return false;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader)
+        base = atomicAdd(counter32(b, C_SPANS), (uint32_t)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (!want)
+        return false;
+    const uint32_t i = base + __popc(m & ((1u << lane) - 1u));
+    if (i >= b->span_cap) {
+        atomicExch(counter32(b, C_OVERFLOW), 1u);
+        return false;
+    }
+    SpanRec r;
+    r.slot = slot;
+    r.y_bits = (uint32_t)y | bits;
+    r.x1 = o.x1;
+    r.x2 = o.x2;
+    r.top = q.top;
+    r.tstep = q.tstep;
+    r.bottom = q.bottom;
+    r.bstep = q.bstep;
+    r.v0 = q.v0;
+    r.dv = q.dv;
+    r.progL = pl;
+    r.progR = pr;
+    r.item = item;
+    b->spans[i] = r;
+    return true;
+}
+
+// One span's pixels into the depth keys (the opaque branch of
+// fill_half_triangle, renderer.cpp:484-499, as a key reduction).
+__device__ __forceinline__ void span_depth(const ItemDev &it, int y, uint32_t slot, int x1, int x2, Interp q)
+{
+    const ViewDev &v = it.v;
+    unsigned long long *row = it.key + ((long long)(y - v.y) * v.w - v.x);
+    for (int x = x1; x < x2; x++, q.step()) {
+        const float z = q.value();
+        if (below_near(z) || __float_as_uint(z) >= kMaxZBits)
+            continue;
+        atomicMin(row + x, make_key(z, slot)); // result unused: a reduction
+    }
+}
+
+typedef uint32_t WalkRow[kWalkPitch];
+
+__device__ __forceinline__ float smf(const WalkRow *S, int f, int o) { return __uint_as_float(S[f][o]); }
+
+__device__ __forceinline__ void smem_row_in(RowIn &r, const WalkRow *S, int o, int k)
+{
+    const int n_u = (int)S[F_NU][o];
+    const int sf = k < n_u ? F_UX : F_DX;
+    float lg[6], sh[6];
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+        lg[f] = smf(S, F_LX + f, o);
+        sh[f] = smf(S, sf + f, o);
+    }
+    row_in(r, k, lg, sh, smf(S, F_Z0, o), smf(S, F_Z1, o), smf(S, F_Z2, o), (int)S[F_YS][o], (int)S[F_YL][o], n_u,
+           S[F_FLAGS][o]);
+}
+
+// Set-up of triangle t of `item` (list entry i): fill_triangle's z sort
+// (renderer.cpp:264-279), fill_triangle_2's y sort, edges and halves
+// (:375-460), into this lane's shared fields.  Returns whether the triangle
+// reached scanline set-up (y0 != y2).
+__device__ __forceinline__ bool walk_setup(const BatchDev *b, uint32_t i, uint32_t t, uint32_t item, WalkRow *S,
+                                           int lane, int &rows, bool &tall)
+{
+    const ItemDev &it = b->items[item];
+    const ViewDev &v = it.v;
+    const uint4 tri = it.s.tris[t];
+    V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
+    const bool ffv = cross_n_z(sub3(c1, a), sub3(c2, a)) < 0.0f;
+    int pa = 0, pb = 1, pc = 2;
+    sort_z_desc(a, c1, c2, pa, pb, pc);
+    sort_y_asc(a, c1, c2, pa, pb, pc);
+    const V3 v0 = a, v1 = c1, v2 = c2;
+    const int y0 = f2i(ceilf(v0.y)), y1 = f2i(ceilf(v1.y)), y2 = f2i(ceilf(v2.y));
+    rows = 0;
+    tall = false;
+    if (y0 == y2)
+        return false;
+    const uint32_t slot = 2 * t;
+    if (b->slot_flags)
+        b->slot_flags[slot] = 1;
+    auto put = [&](int f, float x) { S[f][lane] = __float_as_uint(x); };
+    const float rz0 = 1.0f / v0.z, rz1 = 1.0f / v1.z, rz2 = 1.0f / v2.z;
+    const int ys = y0 < v.y ? v.y : y0;
+    float top, bot, ts, bs;
+    const float lmove = (float)ys - v0.y;
+    const float lratio = (v2.x - v0.x) / (v2.y - v0.y);
+    edge_init(v2.y - v0.y, rz0, rz2, lmove, top, bot, ts, bs);
+    put(F_LX, v0.x + lratio * lmove);
+    put(F_LT, top);
+    put(F_LB, bot);
+    put(F_LR, lratio);
+    put(F_LTS, ts);
+    put(F_LBS, bs);
+    uint32_t flags = ffv ? kRecFFV : 0u;
+    int n_u = 0, n_d = 0, y_l = 0;
+    if (y1 >= v.y) {
+        const float ratio = (v1.x - v0.x) / (v1.y - v0.y);
+        const int yend = y1 < v.y + v.h ? y1 : v.y + v.h;
+        edge_init(v1.y - v0.y, rz0, rz1, lmove, top, bot, ts, bs);
+        put(F_UX, v0.x + ratio * lmove);
+        put(F_UT, top);
+        put(F_UB, bot);
+        put(F_UR, ratio);
+        put(F_UTS, ts);
+        put(F_UBS, bs);
+        if (lratio > ratio)
+            flags |= kRecLLRUpper;
+        n_u = yend > ys ? yend - ys : 0;
+    }
+    if (y1 < v.y + v.h) {
+        const float ratio = (v2.x - v1.x) / (v2.y - v1.y);
+        const int y = y1 > v.y ? y1 : v.y;
+        const int yend = y2 < v.y + v.h ? y2 : v.y + v.h;
+        const float move = (float)y - v1.y;
+        edge_init(v2.y - v1.y, rz1, rz2, move, top, bot, ts, bs);
+        put(F_DX, v1.x + ratio * move);
+        put(F_DT, top);
+        put(F_DB, bot);
+        put(F_DR, ratio);
+        put(F_DTS, ts);
+        put(F_DBS, bs);
+        if (lratio < ratio)
+            flags |= kRecLLRLower;
+        y_l = y;
+        n_d = yend > y ? yend - y : 0;
+    }
+    rows = n_u + n_d;
+    tall = rows > kTallRows;
+    if (tall)
+        flags |= kRecTall;
+    put(F_Z0, v0.z);
+    put(F_Z1, v1.z);
+    put(F_Z2, v2.z);
+    S[F_YS][lane] = (uint32_t)ys;
+    S[F_YL][lane] = (uint32_t)y_l;
+    S[F_NU][lane] = (uint32_t)n_u;
+    S[F_ND][lane] = (uint32_t)n_d;
+    S[F_FLAGS][lane] = flags;
+    S[F_SLOT][lane] = slot;
+    S[F_ITEM][lane] = item;
+    S[F_G0][lane] = pa == 0 ? tri.x : (pa == 1 ? tri.y : tri.z);
+    S[F_G1][lane] = pb == 0 ? tri.x : (pb == 1 ? tri.y : tri.z);
+    S[F_G2][lane] = pc == 0 ? tri.x : (pc == 1 ? tri.y : tri.z);
+    S[F_PRIM][lane] = tri.w;
+    b->recmap[__ldg(b->tri_base + item) + t] = i;
+    return true;
+}
+
+// One row of lane o's triangle, on this lane; every lane of the warp calls it
+// (act = this lane has a row).  Spans wider than the inline limit, and every
+// span of a tall triangle, go to the long-span kernels.
+__device__ __forceinline__ void walk_row(const BatchDev *b, WalkRow *S, int o, RowIn &r, bool act,
+                                         bool bin_all)
+{
+    const uint32_t item = act ? S[F_ITEM][o] : 0u;
+    const ItemDev &it = b->items[item];
+    RowSpan sp;
+    sp.x1 = sp.x2 = 0;
+    if (act)
+        row_span(r, it.v, sp);
+    const bool has = act && sp.x1 < sp.x2;
+    Interp q;
+    float pl = 0.0f, pr = 0.0f;
+    if (has) {
+        atomicAdd(&S[F_FRAGS][o], (uint32_t)(sp.x2 - sp.x1));
+        span_interp(sp, q, pl, pr);
+    }
+    const uint32_t slot = S[F_SLOT][o];
+    const bool want = has && (bin_all || sp.x2 - sp.x1 > b->inline_span);
+    if (bin_span_warp(b, want, item, slot, r.y, sp, q, pl, pr, r.bits))
+        return;
+    if (has)
+        span_depth(it, r.y, slot, sp.x1, sp.x2, q);
+}
+
+// A tall triangle (lane o's), walked by the whole warp: for each 32 rows
+// every lane runs the 32 edge steps and keeps the state of its own row, so
+// no lane repeats more than 32 steps per row it walks.
+__device__ __noinline__ void walk_tall(const BatchDev *b, WalkRow *S, int o)
+{
+    const int lane = threadIdx.x & 31;
+    float lg[6], up[6], dn[6];
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+        lg[f] = smf(S, F_LX + f, o);
+        up[f] = smf(S, F_UX + f, o);
+        dn[f] = smf(S, F_DX + f, o);
+    }
+    const float z0 = smf(S, F_Z0, o), z1 = smf(S, F_Z1, o), z2 = smf(S, F_Z2, o);
+    const int y_s = (int)S[F_YS][o], y_l = (int)S[F_YL][o], n_u = (int)S[F_NU][o], n_d = (int)S[F_ND][o];
+    const uint32_t flags = S[F_FLAGS][o];
+    const int n = n_u + n_d;
+    float lx = lg[0], lt = lg[1], lb = lg[2];
+    float sx = up[0], st = up[1], sb = up[2];
+    for (int r0 = 0; r0 < n; r0 += 32) {
+        float mlx = 0.0f, mlt = 0.0f, mlb = 0.0f, msx = 0.0f, mst = 0.0f, msb = 0.0f;
+        for (int k = 0; k < 32; k++) {
+            const int rr = r0 + k;
+            if (rr == n_u) { // the lower half starts on its own short edge
+                sx = dn[0];
+                st = dn[1];
+                sb = dn[2];
+            }
+            if (k == lane) {
+                mlx = lx; mlt = lt; mlb = lb;
+                msx = sx; mst = st; msb = sb;
+            }
+            lx = lx + lg[3];
+            lt = lt + lg[4];
+            lb = lb + lg[5];
+            if (rr < n_u) {
+                sx = sx + up[3];
+                st = st + up[4];
+                sb = sb + up[5];
+            } else {
+                sx = sx + dn[3];
+                st = st + dn[4];
+                sb = sb + dn[5];
+            }
+        }
+        const int k = r0 + lane;
+        const bool act = k < n;
+        RowIn r;
+        row_in(r, act ? k : 0, lg, (act && k >= n_u) ? dn : up, z0, z1, z2, y_s, y_l, n_u, flags);
+        r.lx = mlx; r.lt = mlt; r.lb = mlb; // already stepped to the row
+        r.sx = msx; r.st = mst; r.sb = msb;
+        r.ls = 0;
+        r.ss = 0;
+        walk_row(b, S, o, r, act, true);
+    }
+}
+
+// Depth walk of the drawable triangles wholly in front of the near plane
+// (fill_triangle's normal case, renderer.cpp:281-285: one sub-triangle, slot
+// 2t).  Warps take 32 list entries at a time from a shared counter.
+__global__ void __launch_bounds__(kWalkWarps * 32, 8) k_walk(const BatchDev *b)
+{
+    __shared__ WalkRow sm[kWalkWarps][kWalkFields];
+    const int lane = threadIdx.x & 31;
+    WalkRow *S = sm[threadIdx.x >> 5];
     const uint32_t n_raw = *counter32(b, C_LIST);
     const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
     unsigned long long drawn_all = 0, frags_all = 0;
-    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
-        const uint32_t i = i0 + threadIdx.x;
-        DepthVisitor vis{b, nullptr, 0u, 0u, b->inline_span, false, 0ull, 0ull};
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0)
+            base = atomicAdd(counter32(b, C_WORK), 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n)
+            break;
+        const uint32_t i = base + lane;
         const bool valid = i < n;
+        int rows = 0;
+        bool tall = false, drawn = false;
+        uint32_t item = 0;
+        S[F_FRAGS][lane] = 0;
         if (valid) {
             const uint2 e = b->list[i];
-            vis.item = e.y & 0xFFFFFFu;
-            vis.it = &b->items[vis.item];
-            vis.bin_all = (e.y >> 24) == (uint32_t)(kClasses - 1);
-            const uint4 tri = vis.it->s.tris[e.x];
-            V3 a = load_vp(*vis.it, tri.x), c1 = load_vp(*vis.it, tri.y), c2 = load_vp(*vis.it, tri.z);
-            int pa = 0, pb = 1, pc = 2;
-            sort_z_desc(a, c1, c2, pa, pb, pc);
-            vis.slot = 2 * e.x;
-            walk_sub(vis.it->v, a, c1, c2, vis);
+            item = e.y;
+            drawn = walk_setup(b, i, e.x, item, S, lane, rows, tall);
         }
-        item_add(b->item_counters, vis.item, vis.drawn_n, valid);
-        item_add(b->item_counters + 1, vis.item, vis.fragments, valid);
-        drawn_all += vis.drawn_n;
-        frags_all += vis.fragments;
+        __syncwarp();
+        // the warp stores the set-ups (32 lanes = the 32 words of a record)
+        for (unsigned dm = __ballot_sync(0xFFFFFFFFu, drawn); dm; dm &= dm - 1) {
+            const int j = __ffs(dm) - 1;
+            reinterpret_cast<uint32_t *>(b->recs + base + j)[lane] = S[lane][j];
+        }
+        // deal the rows of the non-tall triangles across the lanes
+        const int mine = tall ? 0 : rows;
+        int incl = mine;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int u = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= d)
+                incl += u;
+        }
+        const int excl = incl - mine;
+        const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        for (int p0 = 0; p0 < total; p0 += 32) {
+            const int p = p0 + lane;
+            int o = 0;
+#pragma unroll
+            for (int s = 16; s >= 1; s >>= 1) {
+                const int c = __shfl_sync(0xFFFFFFFFu, incl, o + s - 1);
+                if (c <= p)
+                    o += s;
+            }
+            o = o > 31 ? 31 : o;
+            const int ex = __shfl_sync(0xFFFFFFFFu, excl, o);
+            const bool act = p < total;
+            RowIn r;
+            if (act)
+                smem_row_in(r, S, o, p - ex);
+            walk_row(b, S, o, r, act, false);
+        }
+        unsigned tm = __ballot_sync(0xFFFFFFFFu, tall);
+        while (tm) {
+            const int o = __ffs(tm) - 1;
+            tm &= tm - 1;
+            walk_tall(b, S, o);
+        }
+        __syncwarp();
+        const unsigned long long fr = valid ? (unsigned long long)S[F_FRAGS][lane] : 0ull;
+        item_add(b->item_counters, item, drawn ? 1ull : 0ull, valid);
+        item_add(b->item_counters + 1, item, fr, valid);
+        drawn_all += drawn ? 1ull : 0ull;
+        frags_all += fr;
+        __syncwarp();
     }
     warp_add(&b->counters[C_DRAWN], drawn_all);
     warp_add(&b->counters[C_FRAGMENTS], frags_all);
@@ -798,65 +1207,115 @@ __device__ __forceinline__ uint32_t shade_winner(Shader &sh, const LightsDev &L,
     return sh_shade(sh, L, v, rec.x);
 }
 
-// One pixel (x, y relative to the viewport) of item `item`: the background of
-// viewport_t::clear (viewport.cpp:88-113) or the colour of the winning
-// fragment, and its depth.  Winners of near-clipped triangles are passed on
-// to k_shade_clip.
-__device__ __forceinline__ void shade_pixel(const BatchDev *b, uint32_t item, const ItemDev &it, int x, int y)
+// A winner of a near-clipped triangle: the clip vertices are rebuilt exactly
+// as fill_triangle makes them; the progress values were recorded by the
+// near-clip winner walk.  Rare, so kept out of line.
+__device__ __noinline__ uint32_t shade_clip_px(const ItemDev &it, uint32_t i, uint32_t slot)
 {
-    const ViewDev &v = it.v;
-    const uint32_t i = (uint32_t)y * (uint32_t)v.w + (uint32_t)x;
-    const unsigned long long k = it.key[i];
-    uint32_t *px = it.pixels + (long long)y * it.pitch_px + x;
-    if (k == kEmptyKey) {
-        *px = 0u;
-        if (it.zbuf)
-            it.zbuf[i] = __uint_as_float(kMaxZBits);
-        return;
-    }
-    if (it.zbuf)
-        it.zbuf[i] = __uint_as_float((uint32_t)(k >> 32));
-    const uint32_t slot = (uint32_t)k;
-    const uint4 tri = it.s.tris[slot >> 1];
-    V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
-    if (below_near(a.z) || below_near(c1.z) || below_near(c2.z)) {
-        const uint32_t j = atomicAdd(counter32(b, C_CLIPPX), 1u);
-        if (j < b->clippx_cap)
-            b->clippx[j] = make_uint2(i, item);
-        return;
-    }
-    // fill_triangle: front_face_visible, then the z sort; fill_triangle_2: the y sort
-    const bool ffv = cross_n_z(sub3(c1, a), sub3(c2, a)) < 0.0f;
-    int pa = 0, pb = 1, pc = 2;
-    sort_z_desc(a, c1, c2, pa, pb, pc);
-    float4 rec;
-    if (*counter32(b, C_OVERFLOW) || row_extent(a.y, c1.y, c2.y) > kTallRows) {
-        rec = it.prec[i]; // recorded by the span kernels (or the overflow winner walk)
-    } else {
-        ReplayVisitor rv{x + v.x, y + v.y, b->inline_span, false, false, make_float4(0.f, 0.f, 0.f, 0.f)};
-        walk_sub(v, a, c1, c2, rv);
-        rec = rv.found ? rv.rec : it.prec[i];
-    }
-    sort_y_asc(a, c1, c2, pa, pb, pc);
-    const uint32_t g0 = pa == 0 ? tri.x : (pa == 1 ? tri.y : tri.z);
-    const uint32_t g1 = pb == 0 ? tri.x : (pb == 1 ? tri.y : tri.z);
-    const uint32_t g2 = pc == 0 ? tri.x : (pc == 1 ? tri.y : tri.z);
+    const float4 rec = it.prec[i];
     Shader sh;
-    bind_material(it.s, tri.w, sh);
-    const float4 w0 = it.s.wpos[g0], w1 = it.s.wpos[g1], w2 = it.s.wpos[g2];
-    const float4 n0 = it.s.wnrm[g0], n1 = it.s.wnrm[g1], n2 = it.s.wnrm[g2];
-    const float2 u0 = it.s.uv[g0], u1 = it.s.uv[g1], u2 = it.s.uv[g2];
+    bool done = false;
+    auto emit = [&](uint32_t sl, const TV &a, const TV &c1, const TV &c2, bool ffv) {
+        if (sl != slot || done)
+            return;
+        const TV *p0 = &a, *p1 = &c1, *p2 = &c2, *t;
+        if (p1->vp.y < p0->vp.y) { t = p0; p0 = p1; p1 = t; }
+        if (p2->vp.y < p1->vp.y) { t = p1; p1 = p2; p2 = t; }
+        if (p1->vp.y < p0->vp.y) { t = p0; p0 = p1; p1 = t; }
+        const V3 sw[3] = {p0->world, p1->world, p2->world};
+        const V3 sn[3] = {p0->nworld, p1->nworld, p2->nworld};
+        const V2 su[3] = {p0->uv, p1->uv, p2->uv};
+        bind_material(it.s, it.s.tris[slot >> 1].w, sh);
+        sh_prepare_triangle(sh, sw, sn, su, !ffv);
+        done = true;
+    };
+    clip_triangle(it, slot >> 1, emit);
+    return done ? shade_winner(sh, *it.s.lights, it.v, rec) : 0u;
+}
+
+// The progress values of pixel (X, Y) (surface coordinates) from its winning
+// triangle's set-up: the row's edges after their steps, the span and the
+// qpixel chain up to X (renderer.cpp:474-493).  False when the span was wide
+// enough to be binned (its winners were recorded by the span kernels).
+__device__ __forceinline__ bool rec_replay(const TriRec *rp, const ViewDev &v, int inline_span, int X, int Y,
+                                           float4 &out)
+{
+    const float4 *q = reinterpret_cast<const float4 *>(rp);
+    const float4 q5 = q[5], q6 = q[6];
+    const int y_s = __float_as_int(q5.y), y_l = __float_as_int(q5.z), n_u = __float_as_int(q5.w);
+    const uint32_t flags = __float_as_uint(q6.y);
+    const int k = (Y >= y_s && Y < y_s + n_u) ? Y - y_s : n_u + (Y - y_l);
+    const float4 q0 = q[0], q1 = q[1], q4 = q[4];
+    const float lg[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+    float sh[6];
+    if (k < n_u) {
+        const float4 q2 = q[2];
+        sh[0] = q1.z; sh[1] = q1.w; sh[2] = q2.x; sh[3] = q2.y; sh[4] = q2.z; sh[5] = q2.w;
+    } else {
+        const float4 q3 = q[3];
+        sh[0] = q3.x; sh[1] = q3.y; sh[2] = q3.z; sh[3] = q3.w; sh[4] = q4.x; sh[5] = q4.y;
+    }
+    RowIn r;
+    row_in(r, k, lg, sh, q4.z, q4.w, q5.x, y_s, y_l, n_u, flags);
+    RowSpan sp;
+    row_span(r, v, sp);
+    if (sp.x2 - sp.x1 > inline_span)
+        return false;
+    Interp it;
+    float pl, pr;
+    span_interp(sp, it, pl, pr);
+    for (int x = sp.x1; x < X; x++)
+        it.step();
+    out = make_float4(it.alpha, pl, pr, __uint_as_float(r.bits));
+    return true;
+}
+
+// The colour of one winning fragment: pixel i of item `item`, won by `slot`.
+__device__ __forceinline__ uint32_t shade_winner_px(const BatchDev *b, uint32_t item, uint32_t i, uint32_t slot,
+                                                   bool overflow)
+{
+    const ItemDev &it = b->items[item];
+    const ViewDev &v = it.v;
+    const uint32_t ri = b->recmap[__ldg(b->tri_base + item) + (slot >> 1)];
+    if (ri == kRecClip)
+        return shade_clip_px(it, i, slot);
+    const TriRec *rp = b->recs + ri;
+    const uint4 q6 = reinterpret_cast<const uint4 *>(rp)[6];
+    const uint4 q7 = reinterpret_cast<const uint4 *>(rp)[7];
+    const uint32_t flags = q6.y;
+    const int y = (int)(i / (uint32_t)v.w), x = (int)(i - (uint32_t)y * (uint32_t)v.w);
+    float4 rec;
+    if (overflow || (flags & kRecTall) || !rec_replay(rp, v, b->inline_span, x + v.x, y + v.y, rec))
+        rec = it.prec[i]; // recorded by the span kernels (or the overflow winner walk)
+    Shader sh;
+    bind_material(it.s, q7.w, sh);
+    const float4 w0 = it.s.wpos[q7.x], w1 = it.s.wpos[q7.y], w2 = it.s.wpos[q7.z];
+    const float4 n0 = it.s.wnrm[q7.x], n1 = it.s.wnrm[q7.y], n2 = it.s.wnrm[q7.z];
+    const float2 u0 = it.s.uv[q7.x], u1 = it.s.uv[q7.y], u2 = it.s.uv[q7.z];
     const V3 sw[3] = {mk3(w0.x, w0.y, w0.z), mk3(w1.x, w1.y, w1.z), mk3(w2.x, w2.y, w2.z)};
     const V3 sn[3] = {mk3(n0.x, n0.y, n0.z), mk3(n1.x, n1.y, n1.z), mk3(n2.x, n2.y, n2.z)};
     const V2 su[3] = {mk2(u0.x, u0.y), mk2(u1.x, u1.y), mk2(u2.x, u2.y)};
-    sh_prepare_triangle(sh, sw, sn, su, !ffv);
-    *px = shade_winner(sh, *it.s.lights, v, rec);
+    sh_prepare_triangle(sh, sw, sn, su, (flags & kRecFFV) == 0u);
+    return shade_winner(sh, *it.s.lights, v, rec);
 }
 
-// Square tiles of TILE x TILE pixels, one block of TILE*TILE threads per tile.
+// Per pixel: the background of viewport_t::clear (viewport.cpp:88-113) or the
+// colour of the winning fragment, and its depth.  A block takes TILE x TILE
+// tiles; background pixels are written at once and winners are queued in
+// shared memory, so that the shading runs on full warps.  The depth keys read
+// are reset to empty for the next launch sequence (unless kept for debug).
+constexpr int kShadeThreads = 256;
 template <int TILE>
-__global__ void __launch_bounds__(TILE *TILE) k_shade(const BatchDev *b)
+__global__ void __launch_bounds__(kShadeThreads, 3) k_shade(const BatchDev *b)
 {
+    __shared__ uint4 queue[2 * kShadeThreads];
+    __shared__ int qn;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0)
+        qn = 0;
+    __syncthreads();
+    const bool overflow = *counter32(b, C_OVERFLOW) != 0u;
+    const bool keep = b->keep_keys != 0;
     int item = -1;
     uint32_t lo = 0, hi = 0;
     for (uint32_t tg = blockIdx.x; tg < b->total_tiles; tg += gridDim.x) {
@@ -868,45 +1327,59 @@ __global__ void __launch_bounds__(TILE *TILE) k_shade(const BatchDev *b)
         const ItemDev &it = b->items[item];
         const uint32_t tl = tg - lo;
         const int tx = (int)(tl % (uint32_t)it.tiles_x), ty = (int)(tl / (uint32_t)it.tiles_x);
-        const int x = tx * TILE + (int)(threadIdx.x % TILE), y = ty * TILE + (int)(threadIdx.x / TILE);
-        if (x < it.v.w && y < it.v.h)
-            shade_pixel(b, (uint32_t)item, it, x, y);
+        for (int p0 = 0; p0 < TILE * TILE; p0 += kShadeThreads) {
+            const int p = p0 + (int)threadIdx.x;
+            const int x = tx * TILE + p % TILE, y = ty * TILE + p / TILE;
+            bool win = false;
+            uint32_t i = 0;
+            unsigned long long k = kEmptyKey;
+            if (p < TILE * TILE && x < it.v.w && y < it.v.h) {
+                i = (uint32_t)y * (uint32_t)it.v.w + (uint32_t)x;
+                k = it.key[i];
+                if (k == kEmptyKey) {
+                    it.pixels[(long long)y * it.pitch_px + x] = 0u;
+                    if (it.zbuf)
+                        it.zbuf[i] = __uint_as_float(kMaxZBits);
+                } else {
+                    win = true;
+                    if (it.zbuf)
+                        it.zbuf[i] = __uint_as_float((uint32_t)(k >> 32));
+                    if (!keep)
+                        it.key[i] = kEmptyKey;
+                }
+            }
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, win);
+            int wb = 0;
+            if (lane == 0 && m)
+                wb = atomicAdd(&qn, __popc(m));
+            wb = __shfl_sync(0xFFFFFFFFu, wb, 0);
+            if (win)
+                queue[wb + __popc(m & ((1u << lane) - 1u))] = make_uint4(i, (uint32_t)item, (uint32_t)k, 0u);
+            __syncthreads();
+            const int have = qn;
+            if (have >= kShadeThreads) {
+                const uint4 e = queue[threadIdx.x];
+                const ItemDev &ie = b->items[e.y];
+                const ViewDev &ve = ie.v;
+                const uint32_t c = shade_winner_px(b, e.y, e.x, e.z, overflow);
+                const int yy = (int)(e.x / (uint32_t)ve.w), xx = (int)(e.x - (uint32_t)yy * (uint32_t)ve.w);
+                ie.pixels[(long long)yy * ie.pitch_px + xx] = c;
+                __syncthreads();
+                if ((int)threadIdx.x < have - kShadeThreads)
+                    queue[threadIdx.x] = queue[kShadeThreads + threadIdx.x];
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    qn = have - kShadeThreads;
+            }
+            __syncthreads();
+        }
     }
-}
-
-// Winners that belong to near-clipped triangles: the clip vertices are rebuilt
-// exactly as fill_triangle makes them; the progress values were recorded by
-// the near-clip winner walk.
-__global__ void __launch_bounds__(128) k_shade_clip(const BatchDev *b)
-{
-    const uint32_t n_raw = *counter32(b, C_CLIPPX);
-    const uint32_t n = n_raw < b->clippx_cap ? n_raw : b->clippx_cap;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint2 e = b->clippx[j];
-        const ItemDev &it = b->items[e.y];
-        const uint32_t i = e.x;
-        const int y = (int)(i / (uint32_t)it.v.w), x = (int)(i - (uint32_t)y * (uint32_t)it.v.w);
-        const uint32_t slot = (uint32_t)it.key[i];
-        const float4 rec = it.prec[i];
-        Shader sh;
-        bool done = false;
-        auto emit = [&](uint32_t sl, const TV &a, const TV &c1, const TV &c2, bool ffv) {
-            if (sl != slot || done)
-                return;
-            const TV *p0 = &a, *p1 = &c1, *p2 = &c2, *t;
-            if (p1->vp.y < p0->vp.y) { t = p0; p0 = p1; p1 = t; }
-            if (p2->vp.y < p1->vp.y) { t = p1; p1 = p2; p2 = t; }
-            if (p1->vp.y < p0->vp.y) { t = p0; p0 = p1; p1 = t; }
-            const V3 sw[3] = {p0->world, p1->world, p2->world};
-            const V3 sn[3] = {p0->nworld, p1->nworld, p2->nworld};
-            const V2 su[3] = {p0->uv, p1->uv, p2->uv};
-            bind_material(it.s, it.s.tris[slot >> 1].w, sh);
-            sh_prepare_triangle(sh, sw, sn, su, !ffv);
-            done = true;
-        };
-        clip_triangle(it, slot >> 1, emit);
-        if (done)
-            it.pixels[(long long)y * it.pitch_px + x] = shade_winner(sh, *it.s.lights, it.v, rec);
+    if ((int)threadIdx.x < qn) {
+        const uint4 e = queue[threadIdx.x];
+        const ItemDev &ie = b->items[e.y];
+        const uint32_t c = shade_winner_px(b, e.y, e.x, e.z, overflow);
+        const int yy = (int)(e.x / (uint32_t)ie.v.w), xx = (int)(e.x - (uint32_t)yy * (uint32_t)ie.v.w);
+        ie.pixels[(long long)yy * ie.pitch_px + xx] = c;
     }
 }
 
@@ -979,9 +1452,8 @@ cudaError_t launch_world(const SceneDev &s, cudaStream_t st)
 
 const char *prof_kernel_name(int k)
 {
-    static const char *names[kProfKernels] = {"k_clear",  "k_vertex",       "k_flags",
-                                              "k_compact", "k_walk+clip",   "k_spans",
-                                              "winner records", "k_shade", "k_dof"};
+    static const char *names[kProfKernels] = {"k_vertex", "k_flags",        "k_compact", "k_walk+clip",
+                                              "k_spans",  "winner records", "k_shade",   "k_dof"};
     return (k >= 0 && k < kProfKernels) ? names[k] : "?";
 }
 
@@ -1038,9 +1510,6 @@ cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t
     };
     const int sms = sm_count();
     int n = 0;
-    mark(PK_CLEAR);
-    k_clear<<<sms * 8, 256, 0, st>>>(b);
-    n++;
     mark(PK_VERTEX);
     k_vertex<<<sms * 8, 256, 0, st>>>(b);
     n++;
@@ -1051,7 +1520,7 @@ cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t
     k_compact<<<sms * 4, kCompactBlock, 0, st>>>(b);
     n++;
     mark(PK_DEPTH);
-    k_walk<<<sms * 8, 128, 0, st>>>(b);
+    k_walk<<<sms * 8, kWalkWarps * 32, 0, st>>>(b);
     k_walk_clip<0><<<sms, 128, 0, st>>>(b);
     n += 2;
     mark(PK_SPANS);
@@ -1064,13 +1533,12 @@ cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t
     n += 3;
     mark(PK_SHADE);
     if (tile == 8)
-        k_shade<8><<<sms * 16, 64, 0, st>>>(b);
+        k_shade<8><<<sms * 3, kShadeThreads, 0, st>>>(b);
     else if (tile == 32)
-        k_shade<32><<<sms * 2, 1024, 0, st>>>(b);
+        k_shade<32><<<sms * 3, kShadeThreads, 0, st>>>(b);
     else
-        k_shade<16><<<sms * 8, 256, 0, st>>>(b);
-    k_shade_clip<<<sms, 128, 0, st>>>(b);
-    n += 2;
+        k_shade<16><<<sms * 3, kShadeThreads, 0, st>>>(b);
+    n++;
     mark(PK_DOF);
     if (any_dof) {
         k_dof<<<sms * 8, 256, 0, st>>>(b);

@@ -101,12 +101,40 @@ static_assert(sizeof(SpanRec) == 52, "SpanRec layout");
 constexpr uint32_t kBitLower = 1u << 30; // span of the lower half-triangle
 constexpr uint32_t kBitLLR = 1u << 31;   // long_line_on_right
 constexpr uint32_t kYMask = (1u << 30) - 1u;
-constexpr int kClasses = 5;   // drawable triangles by rows: <=2, <=4, <=8, <=kTallRows, taller
-constexpr int kTallRows = 16; // taller triangles queue every span
+constexpr int kTallRows = 16; // triangles walking more rows bin every span
+
+// The scanline set-up of one drawable triangle (fill_triangle_2,
+// src/render/renderer.cpp:361-460), written by the walk and read back by the
+// shade kernel, which replays a winner's row and pixel steps from it instead
+// of repeating the set-up.  Vertices are in fill_triangle_2's y order
+// (v0, v1, v2).  Each edge is an interpolator_g<1> with its x, after the
+// displacement to the first row the walk visits: the long edge v0 -> v2 and
+// the upper short edge v0 -> v1 at row y_s, the lower short edge v1 -> v2 at
+// row y_l.  Row k of the walk (k < n_u: upper half, else lower half) sees the
+// long edge after k steps and its short edge after k (or k - n_u) steps.
+struct __align__(16) TriRec {
+    float lx, ltop, lbot, lratio;  // long edge
+    float ltstep, lbstep, ux, utop; // ... upper short edge
+    float ubot, uratio, utstep, ubstep;
+    float dx, dtop, dbot, dratio;   // lower short edge
+    float dtstep, dbstep, z0, z1;   // z' of v0, v1, v2
+    float z2;
+    int y_s, y_l, n_u;
+    int n_d;
+    uint32_t flags;                 // kRecLLRUpper | kRecLLRLower | kRecFFV | kRecTall
+    uint32_t slot, item;
+    uint32_t g0, g1, g2, prim;      // vertices of v0, v1, v2; draw-order primitive
+};
+static_assert(sizeof(TriRec) == 128, "TriRec layout");
+constexpr uint32_t kRecLLRUpper = 1u; // long_line_on_right in the upper half
+constexpr uint32_t kRecLLRLower = 2u; // ... in the lower half
+constexpr uint32_t kRecFFV = 4u;      // front_face_visible
+constexpr uint32_t kRecTall = 8u;     // every span was binned (winners recorded in prec)
+constexpr uint32_t kRecClip = 0xFFFFFFFFu; // recmap entry of a near-clipped triangle
 
 // Batch counters: 64-bit [C_DRAWN], [C_FRAGMENTS]; 32-bit words from index 4.
 enum { C_DRAWN = 0, C_FRAGMENTS = 1 };
-enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_CLIPPX = 8 };
+enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_WORK = 8 };
 constexpr int kCounterWords = 8; // 64-bit words
 
 // A batch of views rendered by one launch sequence (lives in device memory).
@@ -119,12 +147,13 @@ struct BatchDev {
     int n_items;
     int inline_span;           // spans wider than this go to the long-span bins
     uint32_t total_vtx, total_tri, total_px, total_tiles;
-    uint2 *list;               // drawable triangles {t, item | class << 24}
+    uint2 *list;               // drawable triangles {t, item}
     uint32_t list_cap;
     uint2 *clip;               // drawable triangles crossing the near plane {t, item}: entry j at clip[clip_cap - 1 - j]
     uint32_t clip_cap;
-    uint2 *clippx;             // pixels won by near-clipped triangles {pixel, item}
-    uint32_t clippx_cap;
+    TriRec *recs;              // scanline set-up of list entry i (list_cap entries)
+    uint32_t *recmap;          // per batch triangle (tri_base[item] + t): its list entry, or kRecClip
+    int keep_keys;             // leave the depth keys for the caller (debug); else the shade resets them
     SpanRec *spans;            // long-span bins
     uint32_t span_cap;
     unsigned long long *counters;      // kCounterWords words
@@ -134,8 +163,8 @@ struct BatchDev {
 
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each stage of a launch sequence (enabled with sgl_profile).
-constexpr int kProfKernels = 9;
-enum ProfKernel { PK_CLEAR = 0, PK_VERTEX, PK_FLAGS, PK_COMPACT, PK_DEPTH, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF };
+constexpr int kProfKernels = 8;
+enum ProfKernel { PK_VERTEX = 0, PK_FLAGS, PK_COMPACT, PK_DEPTH, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF };
 struct Profiler {
     bool enabled = false;
     cudaEvent_t ev[kProfKernels + 1] = {};
@@ -149,7 +178,8 @@ void prof_flush(Profiler *p);
 // kernel launchers (raster.cu)
 cudaError_t launch_world(const SceneDev &s, cudaStream_t st);
 // The launch sequence of a batch whose BatchDev lives at `b` (device memory).
-// `any_dof` adds the depth-of-field gather.
+// `any_dof` adds the depth-of-field gather.  The depth keys must hold
+// kEmptyKey on entry; the shade kernel leaves them so (unless keep_keys).
 cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t st, int *launches, Profiler *prof);
 // The depth-of-field gather alone (items prepared by the caller).
 cudaError_t launch_dof(const BatchDev *b, cudaStream_t st);

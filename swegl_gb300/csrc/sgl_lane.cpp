@@ -42,7 +42,7 @@ size_t view_scratch_bytes(uint32_t n_vertices, uint32_t n_triangles, int w, int 
 {
     const size_t px = (size_t)w * h;
     return align_up(16 * (size_t)n_vertices, 256) + align_up(n_vertices, 256) + 8 * px + 16 * px  // ndc yes key prec
-           + 8 * (size_t)n_triangles + 8 * px + sizeof(SpanRec) * (px / 8 + 64)                    // lists, bins
+           + (8 + sizeof(TriRec) + 4) * (size_t)n_triangles + sizeof(SpanRec) * (px / 8 + 64)      // lists, set-ups, bins
            + 8 * px;                                                                               // dof colour, depth
 }
 
@@ -144,10 +144,17 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     const size_t span_cap = std::max<size_t>(65536, tp / 8);
     CUDA_TRY(ndc.ensure(sizeof(float4) * std::max<size_t>(ndc_off, 1)));
     CUDA_TRY(yes.ensure(std::max<size_t>(yes_off, 1)));
+    const void *key_was = key.ptr;
     CUDA_TRY(key.ensure(sizeof(unsigned long long) * std::max<uint64_t>(tp, 1)));
+    if (key.ptr != key_was || keys_dirty) {
+        // a new pool, or one a debug render or a failed launch left dirty
+        CUDA_TRY(cudaMemsetAsync(key.ptr, 0xFF, key.bytes, stream)); // kEmptyKey is all ones
+        keys_dirty = false;
+    }
     CUDA_TRY(prec.ensure(sizeof(float4) * std::max<uint64_t>(tp, 1)));
     CUDA_TRY(list.ensure(sizeof(uint2) * std::max<uint64_t>(tt, 1)));
-    CUDA_TRY(clippx.ensure(sizeof(uint2) * std::max<uint64_t>(tp, 1)));
+    CUDA_TRY(recs.ensure(sizeof(TriRec) * std::max<uint64_t>(tt, 1)));
+    CUDA_TRY(recmap.ensure(sizeof(uint32_t) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(spans.ensure(sizeof(SpanRec) * span_cap));
     if (dof_px) {
         CUDA_TRY(doftmp.ensure(4 * dof_px));
@@ -208,8 +215,10 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.list_cap = (uint32_t)std::max<uint64_t>(tt, 1);
     bd.clip = (uint2 *)list.ptr; // shares the list buffer, filled from its end
     bd.clip_cap = bd.list_cap;
-    bd.clippx = (uint2 *)clippx.ptr;
-    bd.clippx_cap = (uint32_t)std::max<uint64_t>(tp, 1);
+    bd.recs = (TriRec *)recs.ptr;
+    bd.recmap = (uint32_t *)recmap.ptr;
+    bd.keep_keys = slot_flags != nullptr; // debug renders read the keys back
+    sl.keep_keys = bd.keep_keys != 0;
     bd.spans = (SpanRec *)spans.ptr;
     bd.span_cap = (uint32_t)std::min<size_t>(spans.bytes / sizeof(SpanRec), 0xFFFFFFFFu);
     bd.counters = (unsigned long long *)sl.d_counters.ptr;
@@ -235,6 +244,7 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
 {
     Slot &sl = slots[si];
     const BatchDev *db = (const BatchDev *)sl.d_batch.ptr;
+    keys_dirty = true; // until the sequence is enqueued: its shade kernel empties the keys
     if (use_graph) {
         cudaGraphExec_t &g = sl.graph[tile_index(tile)][sl.any_dof ? 1 : 0];
         if (!g) {
@@ -260,6 +270,7 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
     } else {
         CUDA_TRY(launch_batch(db, tile, sl.any_dof, stream, launches, prof));
     }
+    keys_dirty = sl.keep_keys;
     unsigned long long *hc = (unsigned long long *)sl.h_counters.ptr;
     CUDA_TRY(cudaMemcpyAsync(hc, sl.d_counters.ptr, sizeof(unsigned long long) * kCounterWords,
                              cudaMemcpyDeviceToHost, stream));

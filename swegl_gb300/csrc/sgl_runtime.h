@@ -100,9 +100,11 @@ struct Lane {
         int graph_kernels[3][2] = {};     // kernels in each graph
         int n_items = 0;
         bool any_dof = false;
+        bool keep_keys = false;
     } slots[kSlots];
     int next = 0;
-    DevBuf list, clip, clippx, spans, ndc, yes, key, prec, doftmp, dofz;
+    DevBuf list, recs, recmap, spans, ndc, yes, key, prec, doftmp, dofz;
+    bool keys_dirty = false; // the key pool may hold other than kEmptyKey (debug, failed launch)
     ~Lane();
 
     // external == nullptr: own stream, blocking (ordered with the legacy default stream) or not
