@@ -123,6 +123,8 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     off += up256(sizeof(TriRec) * (nt ? nt : 1));
     const size_t o_recmap = off;
     off += up256(4 * (nt ? nt : 1));
+    const size_t o_tall = off;
+    off += up256(4 * (nt ? nt : 1));
     const size_t o_dof = off;
     off += dof ? up256(8 * px) : 0;
     const size_t o_spans = off;
@@ -188,6 +190,7 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     b.clip_cap = b.list_cap;
     b.recs = (TriRec *)(base + o_recs);
     b.recmap = (uint32_t *)(base + o_recmap);
+    b.tall = (uint32_t *)(base + o_tall);
     b.keep_keys = 0;
     b.spans = (SpanRec *)(base + o_spans);
     b.span_cap = span_cap;

@@ -10,7 +10,8 @@
 //   k_compact     drawable triangles -> the walk list / the near-clip list
 //   k_walk        per triangle set-up (TriRec), rows dealt across each warp's
 //                 lanes, fragment keys folded with atomicMin
-//   k_walk_clip   the same for triangles crossing the near plane (rare)
+//   k_setup       per drawable triangle: its scanline set-up (TriRec)
+//   k_walk_clip   triangles crossing the near plane, and tall triangles (rare)
 //   k_spans<0>    long spans binned by the walk, one warp each
 //   k_spans<1>, k_walk_clip<1>   winner records for binned spans and clipped triangles
 //   k_walk_winner winner records of every span, only after a bin overflow
@@ -70,6 +71,23 @@ __device__ __forceinline__ void for_each_in_items(const BatchDev *b, const uint3
         fn(item, g - lo);
     }
 }
+
+// Depth-key reduction without a return value (red.global.min.u64): the
+// 64-bit atomicMin() returns the old key, and a warp would wait for that round
+// trip on every fragment.
+__device__ __forceinline__ void key_min(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("red.global.min.u64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
+}
+
+// Asynchronous 4-byte global -> shared copies (cp.async), committed as groups.
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // ---------------------------------------------------------------- vertices --
 
@@ -454,7 +472,7 @@ struct DepthVisitor {
         unsigned long long *row = it->key + ((long long)(y - v.y) * v.w - v.x);
         const uint32_t sl = slot;
         auto op = [&](int x, float z, float) {
-            atomicMin(row + x, make_key(z, sl)); // result unused: a reduction, no round trip
+            key_min(row + x, make_key(z, sl));
         };
         span_pixels(x1, x2, Ls, Rs, op);
     }
@@ -510,6 +528,47 @@ __device__ __forceinline__ void warp_add(unsigned long long *dst, unsigned long 
         atomicAdd(dst, v);
 }
 
+// Per-item counters (drawn triangles, fragments) of a warp, summed in
+// registers while all of the warp's lanes work on one item and added to the
+// item's counters when the item changes (one atomic per counter then); an
+// iteration whose lanes span several items adds per item at once.  Every
+// lane of the warp calls add() and flush().
+struct ItemAcc {
+    uint32_t item = 0xFFFFFFFFu;
+    unsigned long long v0 = 0, v1 = 0;
+
+    __device__ __forceinline__ void flush(const BatchDev *b)
+    {
+        if (item != 0xFFFFFFFFu) {
+            warp_add(b->item_counters + 2 * (size_t)item, v0);
+            warp_add(b->item_counters + 2 * (size_t)item + 1, v1);
+        }
+        item = 0xFFFFFFFFu;
+        v0 = v1 = 0;
+    }
+    __device__ __forceinline__ void add(const BatchDev *b, uint32_t it, unsigned long long a0, unsigned long long a1,
+                                        bool valid)
+    {
+        const unsigned act = __ballot_sync(0xFFFFFFFFu, valid);
+        if (!act)
+            return;
+        const uint32_t first = __shfl_sync(0xFFFFFFFFu, it, __ffs(act) - 1);
+        if (__all_sync(0xFFFFFFFFu, !valid || it == first)) {
+            if (first != item) {
+                flush(b);
+                item = first;
+            }
+            if (valid) {
+                v0 += a0;
+                v1 += a1;
+            }
+        } else {
+            item_add(b->item_counters, it, a0, valid);
+            item_add(b->item_counters + 1, it, a1, valid);
+        }
+    }
+};
+
 // ------------------------------------------------------- row-parallel walk --
 //
 // The walk of fill_triangle_2 is serial only along its edges: row k needs the
@@ -524,6 +583,9 @@ __device__ __forceinline__ void warp_add(unsigned long long *dst, unsigned long 
 // goes to the long-span kernels.
 
 constexpr int kWalkWarps = 4;
+#ifndef SGL_WALK_MIN_BLOCKS
+#define SGL_WALK_MIN_BLOCKS 6 // resident blocks per SM the walk is compiled for (caps its registers)
+#endif
 // Per-warp shared copy of the lanes' set-ups, sm[field][lane]: fields 0-31 are
 // the words of TriRec in order, so the warp can store whole records; the row
 // is padded to 33 words so that both the per-lane and the per-record accesses
@@ -533,7 +595,9 @@ enum {
     F_UX, F_UT, F_UB, F_UR, F_UTS, F_UBS, // upper short edge
     F_DX, F_DT, F_DB, F_DR, F_DTS, F_DBS, // lower short edge
     F_Z0, F_Z1, F_Z2, F_YS, F_YL, F_NU, F_ND, F_FLAGS, F_SLOT, F_ITEM, F_G0, F_G1, F_G2, F_PRIM,
-    F_FRAGS, kWalkFields
+    F_FRAGS, // fragments of the lane's triangle (shared atomics of the lanes walking its rows)
+    F_INCL,  // inclusive prefix of the rows dealt out, per lane
+    kWalkFields
 };
 constexpr int kWalkPitch = 33;
 static_assert(F_PRIM == 31 && sizeof(TriRec) == 32 * sizeof(uint32_t), "shared set-up fields follow TriRec");
@@ -599,7 +663,7 @@ struct RowSpan {
     float Lx, Lt, Lb, Lz, Ldv, Rx, Rt, Rb, Rz, Rdv;
 };
 
-__device__ __forceinline__ void row_span(RowIn &r, const ViewDev &v, RowSpan &o)
+__device__ __forceinline__ void row_span(RowIn &r, int vx, int vw, RowSpan &o)
 {
     for (int k = 0; k < r.ls; k++) {
         r.lx = r.lx + r.lr;
@@ -619,11 +683,11 @@ __device__ __forceinline__ void row_span(RowIn &r, const ViewDev &v, RowSpan &o)
         o.Rx = r.sx; o.Rt = r.st; o.Rb = r.sb; o.Rz = r.sz; o.Rdv = r.sdv;
     }
     o.x1 = f2i(ceilf(o.Lx));
-    if (o.x1 < v.x)
-        o.x1 = v.x;
+    if (o.x1 < vx)
+        o.x1 = vx;
     o.x2 = f2i(ceilf(o.Rx));
-    if (o.x2 > v.x + v.w)
-        o.x2 = v.x + v.w;
+    if (o.x2 > vx + vw)
+        o.x2 = vx + vw;
 }
 
 // The qpixel interpolator of a span after its displacement to x1, and the
@@ -677,15 +741,31 @@ __device__ __forceinline__ bool bin_span_warp(const BatchDev *b, bool want, uint
 
 // One span's pixels into the depth keys (the opaque branch of
 // fill_half_triangle, renderer.cpp:484-499, as a key reduction).
-__device__ __forceinline__ void span_depth(const ItemDev &it, int y, uint32_t slot, int x1, int x2, Interp q)
+// The view fields the walk needs, kept in registers while the item stays.
+struct WalkView {
+    uint32_t item;
+    int x, y, w;
+    unsigned long long *key;
+    int inline_span;
+    __device__ __forceinline__ void load(const BatchDev *b, uint32_t i)
+    {
+        const ItemDev &it = b->items[i];
+        item = i;
+        x = it.v.x;
+        y = it.v.y;
+        w = it.v.w;
+        key = it.key;
+    }
+};
+
+__device__ __forceinline__ void span_depth(const WalkView &v, int y, uint32_t slot, int x1, int x2, Interp q)
 {
-    const ViewDev &v = it.v;
-    unsigned long long *row = it.key + ((long long)(y - v.y) * v.w - v.x);
+    unsigned long long *row = v.key + ((long long)(y - v.y) * v.w - v.x);
     for (int x = x1; x < x2; x++, q.step()) {
         const float z = q.value();
         if (below_near(z) || __float_as_uint(z) >= kMaxZBits)
             continue;
-        atomicMin(row + x, make_key(z, slot)); // result unused: a reduction
+        key_min(row + x, make_key(z, slot));
     }
 }
 
@@ -709,11 +789,12 @@ __device__ __forceinline__ void smem_row_in(RowIn &r, const WalkRow *S, int o, i
 
 // Set-up of triangle t of `item` (list entry i): fill_triangle's z sort
 // (renderer.cpp:264-279), fill_triangle_2's y sort, edges and halves
-// (:375-460), into this lane's shared fields.  Returns whether the triangle
-// reached scanline set-up (y0 != y2).
-__device__ __forceinline__ bool walk_setup(const BatchDev *b, uint32_t i, uint32_t t, uint32_t item, WalkRow *S,
-                                           int lane, int &rows, bool &tall)
+// (:375-460), into the TriRec of the entry.  Returns whether the triangle
+// reached scanline set-up (y0 != y2); the record of one that did not has no
+// rows.
+__device__ __forceinline__ bool tri_setup(const BatchDev *b, uint32_t i, uint32_t t, uint32_t item, bool &tall)
 {
+    tall = false;
     const ItemDev &it = b->items[item];
     const ViewDev &v = it.v;
     const uint4 tri = it.s.tris[t];
@@ -724,125 +805,145 @@ __device__ __forceinline__ bool walk_setup(const BatchDev *b, uint32_t i, uint32
     sort_y_asc(a, c1, c2, pa, pb, pc);
     const V3 v0 = a, v1 = c1, v2 = c2;
     const int y0 = f2i(ceilf(v0.y)), y1 = f2i(ceilf(v1.y)), y2 = f2i(ceilf(v2.y));
-    rows = 0;
-    tall = false;
-    if (y0 == y2)
+    float4 *dst = reinterpret_cast<float4 *>(b->recs + i);
+    if (y0 == y2) {
+        // no rows: n_u = n_d = 0
+        dst[5] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0));
+        dst[6] = make_float4(__int_as_float(0), 0.0f, 0.0f, __uint_as_float(item));
         return false;
+    }
     const uint32_t slot = 2 * t;
     if (b->slot_flags)
         b->slot_flags[slot] = 1;
-    auto put = [&](int f, float x) { S[f][lane] = __float_as_uint(x); };
     const float rz0 = 1.0f / v0.z, rz1 = 1.0f / v1.z, rz2 = 1.0f / v2.z;
     const int ys = y0 < v.y ? v.y : y0;
-    float top, bot, ts, bs;
+    float ltop, lbot, lts, lbs;
     const float lmove = (float)ys - v0.y;
     const float lratio = (v2.x - v0.x) / (v2.y - v0.y);
-    edge_init(v2.y - v0.y, rz0, rz2, lmove, top, bot, ts, bs);
-    put(F_LX, v0.x + lratio * lmove);
-    put(F_LT, top);
-    put(F_LB, bot);
-    put(F_LR, lratio);
-    put(F_LTS, ts);
-    put(F_LBS, bs);
+    edge_init(v2.y - v0.y, rz0, rz2, lmove, ltop, lbot, lts, lbs);
+    const float lx = v0.x + lratio * lmove;
     uint32_t flags = ffv ? kRecFFV : 0u;
     int n_u = 0, n_d = 0, y_l = 0;
+    float ux = 0.0f, utop = 0.0f, ubot = 0.0f, uratio = 0.0f, uts = 0.0f, ubs = 0.0f;
+    float dx = 0.0f, dtop = 0.0f, dbot = 0.0f, dratio = 0.0f, dts = 0.0f, dbs = 0.0f;
     if (y1 >= v.y) {
-        const float ratio = (v1.x - v0.x) / (v1.y - v0.y);
+        uratio = (v1.x - v0.x) / (v1.y - v0.y);
         const int yend = y1 < v.y + v.h ? y1 : v.y + v.h;
-        edge_init(v1.y - v0.y, rz0, rz1, lmove, top, bot, ts, bs);
-        put(F_UX, v0.x + ratio * lmove);
-        put(F_UT, top);
-        put(F_UB, bot);
-        put(F_UR, ratio);
-        put(F_UTS, ts);
-        put(F_UBS, bs);
-        if (lratio > ratio)
+        edge_init(v1.y - v0.y, rz0, rz1, lmove, utop, ubot, uts, ubs);
+        ux = v0.x + uratio * lmove;
+        if (lratio > uratio)
             flags |= kRecLLRUpper;
         n_u = yend > ys ? yend - ys : 0;
     }
     if (y1 < v.y + v.h) {
-        const float ratio = (v2.x - v1.x) / (v2.y - v1.y);
+        dratio = (v2.x - v1.x) / (v2.y - v1.y);
         const int y = y1 > v.y ? y1 : v.y;
         const int yend = y2 < v.y + v.h ? y2 : v.y + v.h;
         const float move = (float)y - v1.y;
-        edge_init(v2.y - v1.y, rz1, rz2, move, top, bot, ts, bs);
-        put(F_DX, v1.x + ratio * move);
-        put(F_DT, top);
-        put(F_DB, bot);
-        put(F_DR, ratio);
-        put(F_DTS, ts);
-        put(F_DBS, bs);
-        if (lratio < ratio)
+        edge_init(v2.y - v1.y, rz1, rz2, move, dtop, dbot, dts, dbs);
+        dx = v1.x + dratio * move;
+        if (lratio < dratio)
             flags |= kRecLLRLower;
         y_l = y;
         n_d = yend > y ? yend - y : 0;
     }
-    rows = n_u + n_d;
-    tall = rows > kTallRows;
-    if (tall)
+    if (n_u + n_d > kTallRows) {
         flags |= kRecTall;
-    put(F_Z0, v0.z);
-    put(F_Z1, v1.z);
-    put(F_Z2, v2.z);
-    S[F_YS][lane] = (uint32_t)ys;
-    S[F_YL][lane] = (uint32_t)y_l;
-    S[F_NU][lane] = (uint32_t)n_u;
-    S[F_ND][lane] = (uint32_t)n_d;
-    S[F_FLAGS][lane] = flags;
-    S[F_SLOT][lane] = slot;
-    S[F_ITEM][lane] = item;
-    S[F_G0][lane] = pa == 0 ? tri.x : (pa == 1 ? tri.y : tri.z);
-    S[F_G1][lane] = pb == 0 ? tri.x : (pb == 1 ? tri.y : tri.z);
-    S[F_G2][lane] = pc == 0 ? tri.x : (pc == 1 ? tri.y : tri.z);
-    S[F_PRIM][lane] = tri.w;
+        tall = true;
+    }
+    const uint32_t g0 = pa == 0 ? tri.x : (pa == 1 ? tri.y : tri.z);
+    const uint32_t g1 = pb == 0 ? tri.x : (pb == 1 ? tri.y : tri.z);
+    const uint32_t g2 = pc == 0 ? tri.x : (pc == 1 ? tri.y : tri.z);
+    dst[0] = make_float4(lx, ltop, lbot, lratio);
+    dst[1] = make_float4(lts, lbs, ux, utop);
+    dst[2] = make_float4(ubot, uratio, uts, ubs);
+    dst[3] = make_float4(dx, dtop, dbot, dratio);
+    dst[4] = make_float4(dts, dbs, v0.z, v1.z);
+    dst[5] = make_float4(v2.z, __int_as_float(ys), __int_as_float(y_l), __int_as_float(n_u));
+    dst[6] = make_float4(__int_as_float(n_d), __uint_as_float(flags), __uint_as_float(slot), __uint_as_float(item));
+    dst[7] = make_float4(__uint_as_float(g0), __uint_as_float(g1), __uint_as_float(g2), __uint_as_float(tri.w));
     b->recmap[__ldg(b->tri_base + item) + t] = i;
     return true;
 }
 
-// One row of lane o's triangle, on this lane; every lane of the warp calls it
-// (act = this lane has a row).  Spans wider than the inline limit, and every
-// span of a tall triangle, go to the long-span kernels.
-__device__ __forceinline__ void walk_row(const BatchDev *b, WalkRow *S, int o, RowIn &r, bool act,
-                                         bool bin_all)
+// Set-up of every walk list entry, one thread each.
+__global__ void __launch_bounds__(256) k_setup(const BatchDev *b)
 {
-    const uint32_t item = act ? S[F_ITEM][o] : 0u;
-    const ItemDev &it = b->items[item];
+    const uint32_t n_raw = *counter32(b, C_LIST);
+    const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
+    ItemAcc acc;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // the loop runs the same number of times on every lane of a warp
+    for (uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; i0 < n; i0 += stride) {
+        const uint32_t i = i0 + (threadIdx.x & 31);
+        bool drawn = false, tall = false;
+        uint32_t item = 0;
+        if (i < n) {
+            const uint2 e = b->list[i];
+            item = e.y;
+            drawn = tri_setup(b, i, e.x, item, tall);
+        }
+        // tall triangles are walked by a whole warp each, in k_walk_rare
+        const unsigned tm = __ballot_sync(0xFFFFFFFFu, tall);
+        if (tm) {
+            const int lane = threadIdx.x & 31, leader = __ffs(tm) - 1;
+            uint32_t tb = 0;
+            if (lane == leader)
+                tb = atomicAdd(counter32(b, C_TALL), (uint32_t)__popc(tm));
+            tb = __shfl_sync(0xFFFFFFFFu, tb, leader);
+            if (tall)
+                b->tall[tb + __popc(tm & ((1u << lane) - 1u))] = i;
+        }
+        acc.add(b, item, drawn ? 1ull : 0ull, 0ull, i < n);
+    }
+    acc.flush(b);
+}
+
+// One row of triangle `slot` of `item` on this lane; every lane of the warp
+// calls it (act = this lane has a row).  Spans wider than the inline limit,
+// and every span of a tall triangle, go to the long-span kernels.  Returns the
+// row's fragments.  `v` caches the item's view (reloaded when it changes).
+__device__ __forceinline__ int walk_row(const BatchDev *b, WalkView &v, uint32_t item, uint32_t slot, RowIn &r,
+                                        bool act, bool bin_all)
+{
+    if (act && item != v.item)
+        v.load(b, item);
     RowSpan sp;
     sp.x1 = sp.x2 = 0;
     if (act)
-        row_span(r, it.v, sp);
+        row_span(r, v.x, v.w, sp);
     const bool has = act && sp.x1 < sp.x2;
     Interp q;
     float pl = 0.0f, pr = 0.0f;
-    if (has) {
-        atomicAdd(&S[F_FRAGS][o], (uint32_t)(sp.x2 - sp.x1));
-        span_interp(sp, q, pl, pr);
-    }
-    const uint32_t slot = S[F_SLOT][o];
-    const bool want = has && (bin_all || sp.x2 - sp.x1 > b->inline_span);
-    if (bin_span_warp(b, want, item, slot, r.y, sp, q, pl, pr, r.bits))
-        return;
     if (has)
-        span_depth(it, r.y, slot, sp.x1, sp.x2, q);
+        span_interp(sp, q, pl, pr);
+    const bool want = has && (bin_all || sp.x2 - sp.x1 > v.inline_span);
+    if (!bin_span_warp(b, want, item, slot, r.y, sp, q, pl, pr, r.bits) && has)
+        span_depth(v, r.y, slot, sp.x1, sp.x2, q);
+    return has ? sp.x2 - sp.x1 : 0;
 }
 
-// A tall triangle (lane o's), walked by the whole warp: for each 32 rows
+// A tall triangle (list entry i), walked by the whole warp: for each 32 rows
 // every lane runs the 32 edge steps and keeps the state of its own row, so
-// no lane repeats more than 32 steps per row it walks.
-__device__ __noinline__ void walk_tall(const BatchDev *b, WalkRow *S, int o)
+// no lane repeats more than 32 steps per row it walks.  Every span is binned.
+// Returns this lane's fragments.
+__device__ __forceinline__ uint32_t walk_tall(const BatchDev *b, uint32_t i)
 {
     const int lane = threadIdx.x & 31;
-    float lg[6], up[6], dn[6];
-#pragma unroll
-    for (int f = 0; f < 6; f++) {
-        lg[f] = smf(S, F_LX + f, o);
-        up[f] = smf(S, F_UX + f, o);
-        dn[f] = smf(S, F_DX + f, o);
-    }
-    const float z0 = smf(S, F_Z0, o), z1 = smf(S, F_Z1, o), z2 = smf(S, F_Z2, o);
-    const int y_s = (int)S[F_YS][o], y_l = (int)S[F_YL][o], n_u = (int)S[F_NU][o], n_d = (int)S[F_ND][o];
-    const uint32_t flags = S[F_FLAGS][o];
+    const float4 *q = reinterpret_cast<const float4 *>(b->recs + i);
+    const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3], q4 = q[4], q5 = q[5], q6 = q[6];
+    const float lg[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+    const float up[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+    const float dn[6] = {q3.x, q3.y, q3.z, q3.w, q4.x, q4.y};
+    const float z0 = q4.z, z1 = q4.w, z2 = q5.x;
+    const int y_s = __float_as_int(q5.y), y_l = __float_as_int(q5.z), n_u = __float_as_int(q5.w);
+    const int n_d = __float_as_int(q6.x);
+    const uint32_t flags = __float_as_uint(q6.y), slot = __float_as_uint(q6.z), item = __float_as_uint(q6.w);
     const int n = n_u + n_d;
+    uint32_t frags = 0;
+    WalkView v;
+    v.load(b, item);
+    v.inline_span = b->inline_span;
     float lx = lg[0], lt = lg[1], lb = lg[2];
     float sx = up[0], st = up[1], sb = up[2];
     for (int r0 = 0; r0 < n; r0 += 32) {
@@ -879,89 +980,101 @@ __device__ __noinline__ void walk_tall(const BatchDev *b, WalkRow *S, int o)
         r.sx = msx; r.st = mst; r.sb = msb;
         r.ls = 0;
         r.ss = 0;
-        walk_row(b, S, o, r, act, true);
+        frags += (uint32_t)walk_row(b, v, item, slot, r, act, true);
     }
+    return frags;
 }
 
 // Depth walk of the drawable triangles wholly in front of the near plane
 // (fill_triangle's normal case, renderer.cpp:281-285: one sub-triangle, slot
-// 2t).  Warps take 32 list entries at a time from a shared counter.
-__global__ void __launch_bounds__(kWalkWarps * 32, 8) k_walk(const BatchDev *b)
+// 2t).  Each warp takes groups of 32 list entries (warp-strided), loads their
+// set-ups into shared memory (one 128-byte record per load) and deals their
+// rows across its lanes.
+__global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(const BatchDev *b)
 {
-    __shared__ WalkRow sm[kWalkWarps][kWalkFields];
+    __shared__ WalkRow sm[kWalkWarps][2][kWalkFields];
     const int lane = threadIdx.x & 31;
-    WalkRow *S = sm[threadIdx.x >> 5];
     const uint32_t n_raw = *counter32(b, C_LIST);
     const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
-    unsigned long long drawn_all = 0, frags_all = 0;
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0)
-            base = atomicAdd(counter32(b, C_WORK), 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n)
-            break;
-        const uint32_t i = base + lane;
-        const bool valid = i < n;
-        int rows = 0;
-        bool tall = false, drawn = false;
-        uint32_t item = 0;
+    const uint32_t n_groups = (n + 31) / 32;
+    // record j of group g -> word `lane` of field row `lane`, column j
+    auto fetch = [&](uint32_t g, WalkRow *D) {
+        if (g < n_groups) {
+            const uint32_t base = 32 * g, cnt = n - base < 32u ? n - base : 32u;
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(b->recs + base) + lane;
+#pragma unroll 8
+            for (uint32_t j = 0; j < cnt; j++)
+                cp_async4(&D[lane][j], src + 32 * j);
+        }
+        cp_async_commit();
+    };
+    ItemAcc acc;
+    WalkView view;
+    view.item = 0xFFFFFFFFu;
+    view.inline_span = b->inline_span;
+    // Groups come from a shared counter.  While group g is walked, the
+    // records of the next group are copied in and the index of the one after
+    // is on its way, so neither wait is on the critical path.
+    uint32_t gi = 0, gj = 0;
+    if (lane == 0) {
+        gi = atomicAdd(counter32(b, C_WALK_NEXT), 1u);
+        gj = atomicAdd(counter32(b, C_WALK_NEXT), 1u);
+    }
+    uint32_t g = __shfl_sync(0xFFFFFFFFu, gi, 0);
+    uint32_t g_next = __shfl_sync(0xFFFFFFFFu, gj, 0);
+    int buf = 0;
+    fetch(g, sm[threadIdx.x >> 5][0]);
+    while (g < n_groups) {
+        fetch(g_next, sm[threadIdx.x >> 5][buf ^ 1]);
+        if (lane == 0 && g_next < n_groups)
+            gi = atomicAdd(counter32(b, C_WALK_NEXT), 1u);
+        cp_async_wait<1>(); // this group's copies are done
+        WalkRow *S = sm[threadIdx.x >> 5][buf];
+        const uint32_t base = 32 * g;
+        const uint32_t cnt = n - base < 32u ? n - base : 32u;
         S[F_FRAGS][lane] = 0;
-        if (valid) {
-            const uint2 e = b->list[i];
-            item = e.y;
-            drawn = walk_setup(b, i, e.x, item, S, lane, rows, tall);
-        }
         __syncwarp();
-        // the warp stores the set-ups (32 lanes = the 32 words of a record)
-        for (unsigned dm = __ballot_sync(0xFFFFFFFFu, drawn); dm; dm &= dm - 1) {
-            const int j = __ffs(dm) - 1;
-            reinterpret_cast<uint32_t *>(b->recs + base + j)[lane] = S[lane][j];
-        }
-        // deal the rows of the non-tall triangles across the lanes
-        const int mine = tall ? 0 : rows;
-        int incl = mine;
+        const bool valid = (uint32_t)lane < cnt;
+        const int n_u = valid ? (int)S[F_NU][lane] : 0, n_d = valid ? (int)S[F_ND][lane] : 0;
+        const bool tall = valid && (S[F_FLAGS][lane] & kRecTall) != 0u; // walked by k_walk_rare
+        // rows of the non-tall triangles, dealt across the lanes
+        int incl = tall ? 0 : n_u + n_d;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const int u = __shfl_up_sync(0xFFFFFFFFu, incl, d);
             if (lane >= d)
                 incl += u;
         }
-        const int excl = incl - mine;
-        const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        S[F_INCL][lane] = (uint32_t)incl;
+        __syncwarp();
+        const int total = (int)S[F_INCL][31];
         for (int p0 = 0; p0 < total; p0 += 32) {
             const int p = p0 + lane;
             int o = 0;
 #pragma unroll
-            for (int s = 16; s >= 1; s >>= 1) {
-                const int c = __shfl_sync(0xFFFFFFFFu, incl, o + s - 1);
-                if (c <= p)
-                    o += s;
-            }
+            for (int st = 16; st >= 1; st >>= 1)
+                if ((int)S[F_INCL][o + st - 1] <= p)
+                    o += st;
             o = o > 31 ? 31 : o;
-            const int ex = __shfl_sync(0xFFFFFFFFu, excl, o);
             const bool act = p < total;
             RowIn r;
-            if (act)
+            if (act) {
+                const int ex = o > 0 ? (int)S[F_INCL][o - 1] : 0;
                 smem_row_in(r, S, o, p - ex);
-            walk_row(b, S, o, r, act, false);
-        }
-        unsigned tm = __ballot_sync(0xFFFFFFFFu, tall);
-        while (tm) {
-            const int o = __ffs(tm) - 1;
-            tm &= tm - 1;
-            walk_tall(b, S, o);
+            }
+            const int fr = walk_row(b, view, S[F_ITEM][o], S[F_SLOT][o], r, act, false);
+            if (fr)
+                atomicAdd(&S[F_FRAGS][o], (uint32_t)fr);
         }
         __syncwarp();
-        const unsigned long long fr = valid ? (unsigned long long)S[F_FRAGS][lane] : 0ull;
-        item_add(b->item_counters, item, drawn ? 1ull : 0ull, valid);
-        item_add(b->item_counters + 1, item, fr, valid);
-        drawn_all += drawn ? 1ull : 0ull;
-        frags_all += fr;
+        acc.add(b, valid ? S[F_ITEM][lane] : 0u, 0ull, valid ? (unsigned long long)S[F_FRAGS][lane] : 0ull, valid);
         __syncwarp();
+        g = g_next;
+        g_next = g < n_groups ? __shfl_sync(0xFFFFFFFFu, gi, 0) : n_groups;
+        buf ^= 1;
     }
-    warp_add(&b->counters[C_DRAWN], drawn_all);
-    warp_add(&b->counters[C_FRAGMENTS], frags_all);
+    cp_async_wait<0>();
+    acc.flush(b);
 }
 
 // Winner records of every simple triangle's spans: runs only when the bins
@@ -1083,13 +1196,15 @@ __device__ __forceinline__ void clip_triangle(const ItemDev &it, uint32_t t, Emi
     }
 }
 
+// The rare walks: triangles crossing the near plane (fill_triangle's clip
+// cases) and, in the depth pass, the tall triangles (one warp each).
 template <int WINNER>
 __global__ void __launch_bounds__(128) k_walk_clip(const BatchDev *b)
 {
     const uint32_t n_raw = *counter32(b, C_CLIP);
     const uint32_t n = n_raw < b->clip_cap ? n_raw : b->clip_cap;
     const bool overflow = *counter32(b, C_OVERFLOW) != 0u;
-    unsigned long long drawn_all = 0, frags_all = 0;
+    ItemAcc acc;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
         const uint32_t i = i0 + threadIdx.x;
         const bool valid = i < n;
@@ -1111,16 +1226,20 @@ __global__ void __launch_bounds__(128) k_walk_clip(const BatchDev *b)
             };
             clip_triangle(it, e.x, emit);
         }
-        if (!WINNER) {
-            item_add(b->item_counters, dvis.item, dvis.drawn_n, valid);
-            item_add(b->item_counters + 1, dvis.item, dvis.fragments, valid);
-            drawn_all += dvis.drawn_n;
-            frags_all += dvis.fragments;
-        }
+        if (!WINNER)
+            acc.add(b, dvis.item, dvis.drawn_n, dvis.fragments, valid);
     }
     if (!WINNER) {
-        warp_add(&b->counters[C_DRAWN], drawn_all);
-        warp_add(&b->counters[C_FRAGMENTS], frags_all);
+        // tall triangles, one warp each
+        const uint32_t nt_raw = *counter32(b, C_TALL);
+        const uint32_t nt = nt_raw < b->list_cap ? nt_raw : b->list_cap;
+        const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
+        for (uint32_t k = gw; k < nt; k += n_warps) {
+            const uint32_t i = b->tall[k];
+            const uint32_t fr = walk_tall(b, i);
+            acc.add(b, b->recs[i].item, 0ull, fr, true);
+        }
+        acc.flush(b);
     }
 }
 
@@ -1167,7 +1286,7 @@ __global__ void __launch_bounds__(256) k_spans(const BatchDev *b)
             const unsigned long long key = make_key(z, r.slot);
             unsigned long long *kp = it.key + base + x;
             if (!WINNER)
-                atomicMin(kp, key);
+                key_min(kp, key);
             else if (*kp == key)
                 it.prec[base + x] = make_float4(alpha, r.progL, r.progR, __uint_as_float(r.y_bits & ~kYMask));
         }
@@ -1258,7 +1377,7 @@ __device__ __forceinline__ bool rec_replay(const TriRec *rp, const ViewDev &v, i
     RowIn r;
     row_in(r, k, lg, sh, q4.z, q4.w, q5.x, y_s, y_l, n_u, flags);
     RowSpan sp;
-    row_span(r, v, sp);
+    row_span(r, v.x, v.w, sp);
     if (sp.x2 - sp.x1 > inline_span)
         return false;
     Interp it;
@@ -1305,8 +1424,11 @@ __device__ __forceinline__ uint32_t shade_winner_px(const BatchDev *b, uint32_t 
 // shared memory, so that the shading runs on full warps.  The depth keys read
 // are reset to empty for the next launch sequence (unless kept for debug).
 constexpr int kShadeThreads = 256;
+#ifndef SGL_SHADE_MIN_BLOCKS
+#define SGL_SHADE_MIN_BLOCKS 4 // resident blocks per SM the shade is compiled for
+#endif
 template <int TILE>
-__global__ void __launch_bounds__(kShadeThreads, 3) k_shade(const BatchDev *b)
+__global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(const BatchDev *b)
 {
     __shared__ uint4 queue[2 * kShadeThreads];
     __shared__ int qn;
@@ -1314,11 +1436,23 @@ __global__ void __launch_bounds__(kShadeThreads, 3) k_shade(const BatchDev *b)
     if (threadIdx.x == 0)
         qn = 0;
     __syncthreads();
+    __shared__ uint32_t tile_next;
     const bool overflow = *counter32(b, C_OVERFLOW) != 0u;
     const bool keep = b->keep_keys != 0;
     int item = -1;
     uint32_t lo = 0, hi = 0;
-    for (uint32_t tg = blockIdx.x; tg < b->total_tiles; tg += gridDim.x) {
+    // tiles are taken from a shared counter; the next one is fetched while
+    // this one is shaded (the barriers of the loop order the exchange)
+    if (threadIdx.x == 0)
+        tile_next = atomicAdd(counter32(b, C_SHADE_NEXT), 1u);
+    __syncthreads();
+    for (;;) {
+        const uint32_t tg = tile_next;
+        if (tg >= b->total_tiles)
+            break;
+        __syncthreads(); // every thread has read tile_next
+        if (threadIdx.x == 0)
+            tile_next = atomicAdd(counter32(b, C_SHADE_NEXT), 1u);
         if (tg < lo || tg >= hi) {
             item = find_item(b->tile_base, b->n_items, tg);
             lo = __ldg(b->tile_base + item);
@@ -1452,8 +1586,9 @@ cudaError_t launch_world(const SceneDev &s, cudaStream_t st)
 
 const char *prof_kernel_name(int k)
 {
-    static const char *names[kProfKernels] = {"k_vertex", "k_flags",        "k_compact", "k_walk+clip",
-                                              "k_spans",  "winner records", "k_shade",   "k_dof"};
+    static const char *names[kProfKernels] = {"k_vertex", "k_flags",          "k_compact", "k_setup",
+                                              "k_walk",   "k_walk_clip+tall", "k_spans",   "winner records",
+                                              "k_shade",  "k_dof"};
     return (k >= 0 && k < kProfKernels) ? names[k] : "?";
 }
 
@@ -1519,10 +1654,13 @@ cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t
     mark(PK_COMPACT);
     k_compact<<<sms * 4, kCompactBlock, 0, st>>>(b);
     n++;
-    mark(PK_DEPTH);
-    k_walk<<<sms * 8, kWalkWarps * 32, 0, st>>>(b);
+    mark(PK_SETUP);
+    k_setup<<<sms * 8, 256, 0, st>>>(b);
+    mark(PK_WALK);
+    k_walk<<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
+    mark(PK_RARE);
     k_walk_clip<0><<<sms, 128, 0, st>>>(b);
-    n += 2;
+    n += 3;
     mark(PK_SPANS);
     k_spans<0><<<sms * 4, 256, 0, st>>>(b);
     n++;
@@ -1533,11 +1671,11 @@ cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t
     n += 3;
     mark(PK_SHADE);
     if (tile == 8)
-        k_shade<8><<<sms * 3, kShadeThreads, 0, st>>>(b);
+        k_shade<8><<<sms * SGL_SHADE_MIN_BLOCKS, kShadeThreads, 0, st>>>(b);
     else if (tile == 32)
-        k_shade<32><<<sms * 3, kShadeThreads, 0, st>>>(b);
+        k_shade<32><<<sms * SGL_SHADE_MIN_BLOCKS, kShadeThreads, 0, st>>>(b);
     else
-        k_shade<16><<<sms * 3, kShadeThreads, 0, st>>>(b);
+        k_shade<16><<<sms * SGL_SHADE_MIN_BLOCKS, kShadeThreads, 0, st>>>(b);
     n++;
     mark(PK_DOF);
     if (any_dof) {

@@ -132,9 +132,9 @@ constexpr uint32_t kRecFFV = 4u;      // front_face_visible
 constexpr uint32_t kRecTall = 8u;     // every span was binned (winners recorded in prec)
 constexpr uint32_t kRecClip = 0xFFFFFFFFu; // recmap entry of a near-clipped triangle
 
-// Batch counters: 64-bit [C_DRAWN], [C_FRAGMENTS]; 32-bit words from index 4.
-enum { C_DRAWN = 0, C_FRAGMENTS = 1 };
-enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_WORK = 8 };
+// Batch counters (32-bit words); the drawn-triangle and fragment counts are
+// kept per item (item_counters) and summed by the host.
+enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_WALK_NEXT = 8, C_SHADE_NEXT = 9, C_TALL = 10 };
 constexpr int kCounterWords = 8; // 64-bit words
 
 // A batch of views rendered by one launch sequence (lives in device memory).
@@ -153,6 +153,7 @@ struct BatchDev {
     uint32_t clip_cap;
     TriRec *recs;              // scanline set-up of list entry i (list_cap entries)
     uint32_t *recmap;          // per batch triangle (tri_base[item] + t): its list entry, or kRecClip
+    uint32_t *tall;            // list entries of the tall triangles (list_cap entries)
     int keep_keys;             // leave the depth keys for the caller (debug); else the shade resets them
     SpanRec *spans;            // long-span bins
     uint32_t span_cap;
@@ -163,8 +164,10 @@ struct BatchDev {
 
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each stage of a launch sequence (enabled with sgl_profile).
-constexpr int kProfKernels = 8;
-enum ProfKernel { PK_VERTEX = 0, PK_FLAGS, PK_COMPACT, PK_DEPTH, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF };
+constexpr int kProfKernels = 10;
+enum ProfKernel {
+    PK_VERTEX = 0, PK_FLAGS, PK_COMPACT, PK_SETUP, PK_WALK, PK_RARE, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF
+};
 struct Profiler {
     bool enabled = false;
     cudaEvent_t ev[kProfKernels + 1] = {};

@@ -42,7 +42,7 @@ size_t view_scratch_bytes(uint32_t n_vertices, uint32_t n_triangles, int w, int 
 {
     const size_t px = (size_t)w * h;
     return align_up(16 * (size_t)n_vertices, 256) + align_up(n_vertices, 256) + 8 * px + 16 * px  // ndc yes key prec
-           + (8 + sizeof(TriRec) + 4) * (size_t)n_triangles + sizeof(SpanRec) * (px / 8 + 64)      // lists, set-ups, bins
+           + (8 + sizeof(TriRec) + 8) * (size_t)n_triangles + sizeof(SpanRec) * (px / 8 + 64)      // lists, set-ups, bins
            + 8 * px;                                                                               // dof colour, depth
 }
 
@@ -155,6 +155,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     CUDA_TRY(list.ensure(sizeof(uint2) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(recs.ensure(sizeof(TriRec) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(recmap.ensure(sizeof(uint32_t) * std::max<uint64_t>(tt, 1)));
+    CUDA_TRY(tall.ensure(sizeof(uint32_t) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(spans.ensure(sizeof(SpanRec) * span_cap));
     if (dof_px) {
         CUDA_TRY(doftmp.ensure(4 * dof_px));
@@ -217,6 +218,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.clip_cap = bd.list_cap;
     bd.recs = (TriRec *)recs.ptr;
     bd.recmap = (uint32_t *)recmap.ptr;
+    bd.tall = (uint32_t *)tall.ptr;
     bd.keep_keys = slot_flags != nullptr; // debug renders read the keys back
     sl.keep_keys = bd.keep_keys != 0;
     bd.spans = (SpanRec *)spans.ptr;
@@ -286,10 +288,16 @@ sgl_status Lane::read_counters(Ctx *ctx, int si, unsigned long long *drawn, unsi
     Slot &sl = slots[si];
     CUDA_TRY(cudaEventSynchronize(sl.done));
     const unsigned long long *hc = (const unsigned long long *)sl.h_counters.ptr;
+    const unsigned long long *ic = hc + kCounterWords; // per item: drawn, fragments
+    unsigned long long d = 0, f = 0;
+    for (int i = 0; i < sl.n_items; i++) {
+        d += ic[2 * i];
+        f += ic[2 * i + 1];
+    }
     if (drawn)
-        *drawn = hc[C_DRAWN];
+        *drawn = d;
     if (fragments)
-        *fragments = hc[C_FRAGMENTS];
+        *fragments = f;
     if (per_item)
         per_item->assign(hc + kCounterWords, hc + kCounterWords + 2 * sl.n_items);
     return SGL_OK;

@@ -103,7 +103,7 @@ struct Lane {
         bool keep_keys = false;
     } slots[kSlots];
     int next = 0;
-    DevBuf list, recs, recmap, spans, ndc, yes, key, prec, doftmp, dofz;
+    DevBuf list, recs, recmap, tall, spans, ndc, yes, key, prec, doftmp, dofz;
     bool keys_dirty = false; // the key pool may hold other than kEmptyKey (debug, failed launch)
     ~Lane();
 
