@@ -8,13 +8,13 @@
 //   k_vertex      world -> view -> projection, |z'| divide      (vertex_shaders.hpp:35-52)
 //   k_flags       visibility flags of triangles                  (renderer.cpp:86-185)
 //   k_compact     drawable triangles -> the walk list / the near-clip list
-//   k_walk        per triangle set-up (TriRec), rows dealt across each warp's
-//                 lanes, fragment keys folded with atomicMin
-//   k_setup       per drawable triangle: its scanline set-up (TriRec)
-//   k_walk_clip   triangles crossing the near plane, and tall triangles (rare)
-//   k_spans<0>    long spans binned by the walk, one warp each
-//   k_spans<1>, k_walk_clip<1>   winner records for binned spans and clipped triangles
-//   k_walk_winner winner records of every span, only after a bin overflow
+//   k_setup       per walk-list triangle: its scanline set-up (TriRec)
+//   k_walk        rows of each 32 set-ups dealt across a warp's lanes,
+//                 fragment keys folded with an atomic min; then the warp's
+//                 share of the near-clip triangles and of the tall triangles
+//   k_spans       long spans binned by the walk, one warp each
+//   k_winners     winner records of binned spans and near-clip triangles
+//                 (every span after a bin overflow)
 //   k_shade       per pixel: background or the winner's colour, and depth;
 //                 winners are queued so that shading runs on full warps
 //   k_dof         depth-of-field gather of the items that ask for it
@@ -985,6 +985,10 @@ __device__ __forceinline__ uint32_t walk_tall(const BatchDev *b, uint32_t i)
     return frags;
 }
 
+// the rare depth walks, defined with the near-clip code below
+__device__ __noinline__ void walk_clip_depth(const BatchDev *b, ItemAcc &acc);
+__device__ __noinline__ void walk_tall_all(const BatchDev *b, ItemAcc &acc);
+
 // Depth walk of the drawable triangles wholly in front of the near plane
 // (fill_triangle's normal case, renderer.cpp:281-285: one sub-triangle, slot
 // 2t).  Each warp takes groups of 32 list entries (warp-strided), loads their
@@ -1012,22 +1016,16 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
     WalkView view;
     view.item = 0xFFFFFFFFu;
     view.inline_span = b->inline_span;
-    // Groups come from a shared counter.  While group g is walked, the
-    // records of the next group are copied in and the index of the one after
-    // is on its way, so neither wait is on the critical path.
-    uint32_t gi = 0, gj = 0;
-    if (lane == 0) {
-        gi = atomicAdd(counter32(b, C_WALK_NEXT), 1u);
-        gj = atomicAdd(counter32(b, C_WALK_NEXT), 1u);
-    }
-    uint32_t g = __shfl_sync(0xFFFFFFFFu, gi, 0);
-    uint32_t g_next = __shfl_sync(0xFFFFFFFFu, gj, 0);
+    // Warps take groups g, g + W, g + 2W, ... (W warps in the grid; a shared
+    // counter costs more in contention than it saves in balance).  While
+    // group g is walked, the records of the next one are copied in.
+    const uint32_t W = (gridDim.x * blockDim.x) >> 5;
+    uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t g_next = g + W;
     int buf = 0;
     fetch(g, sm[threadIdx.x >> 5][0]);
     while (g < n_groups) {
         fetch(g_next, sm[threadIdx.x >> 5][buf ^ 1]);
-        if (lane == 0 && g_next < n_groups)
-            gi = atomicAdd(counter32(b, C_WALK_NEXT), 1u);
         cp_async_wait<1>(); // this group's copies are done
         WalkRow *S = sm[threadIdx.x >> 5][buf];
         const uint32_t base = 32 * g;
@@ -1070,31 +1068,14 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
         acc.add(b, valid ? S[F_ITEM][lane] : 0u, 0ull, valid ? (unsigned long long)S[F_FRAGS][lane] : 0ull, valid);
         __syncwarp();
         g = g_next;
-        g_next = g < n_groups ? __shfl_sync(0xFFFFFFFFu, gi, 0) : n_groups;
+        g_next = g + W;
         buf ^= 1;
     }
     cp_async_wait<0>();
+    // then this warp's share of the near-clip and the tall triangles
+    walk_clip_depth(b, acc);
+    walk_tall_all(b, acc);
     acc.flush(b);
-}
-
-// Winner records of every simple triangle's spans: runs only when the bins
-// overflowed (the shade kernel replays winners otherwise).
-__global__ void __launch_bounds__(128, 8) k_walk_winner(const BatchDev *b)
-{
-    if (!*counter32(b, C_OVERFLOW))
-        return;
-    const uint32_t n_raw = *counter32(b, C_LIST);
-    const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint2 e = b->list[i];
-        const ItemDev &it = b->items[e.y & 0xFFFFFFu];
-        WinnerVisitor vis{&it, 2 * e.x, b->inline_span, true};
-        const uint4 tri = it.s.tris[e.x];
-        V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
-        int pa = 0, pb = 1, pc = 2;
-        sort_z_desc(a, c1, c2, pa, pb, pc);
-        walk_sub(it.v, a, c1, c2, vis);
-    }
 }
 
 // ------------------------------------------------------------- near clip --
@@ -1196,17 +1177,17 @@ __device__ __forceinline__ void clip_triangle(const ItemDev &it, uint32_t t, Emi
     }
 }
 
-// The rare walks: triangles crossing the near plane (fill_triangle's clip
-// cases) and, in the depth pass, the tall triangles (one warp each).
-template <int WINNER>
-__global__ void __launch_bounds__(128) k_walk_clip(const BatchDev *b)
+// Depth walk of the near-clip triangles (fill_triangle's clip cases), one
+// thread each, over a warp-strided share of the clip list.  Out of line: rare,
+// and its register and stack use stay off the row walk.
+__device__ __noinline__ void walk_clip_depth(const BatchDev *b, ItemAcc &acc)
 {
     const uint32_t n_raw = *counter32(b, C_CLIP);
     const uint32_t n = n_raw < b->clip_cap ? n_raw : b->clip_cap;
-    const bool overflow = *counter32(b, C_OVERFLOW) != 0u;
-    ItemAcc acc;
-    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
-        const uint32_t i = i0 + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i0 = 32 * gw; i0 < n; i0 += 32 * n_warps) {
+        const uint32_t i = i0 + lane;
         const bool valid = i < n;
         DepthVisitor dvis{b, nullptr, 0u, 0u, b->inline_span, false, 0ull, 0ull};
         if (valid) {
@@ -1214,33 +1195,76 @@ __global__ void __launch_bounds__(128) k_walk_clip(const BatchDev *b)
             const ItemDev &it = b->items[e.y];
             dvis.item = e.y;
             dvis.it = &it;
-            WinnerVisitor wvis{&it, 0u, b->inline_span, overflow};
             auto emit = [&](uint32_t slot, const TV &a, const TV &c1, const TV &c2, bool) {
-                if (!WINNER) {
-                    dvis.slot = slot;
-                    walk_sub(it.v, a.vp, c1.vp, c2.vp, dvis);
-                } else {
-                    wvis.slot = slot;
-                    walk_sub(it.v, a.vp, c1.vp, c2.vp, wvis);
-                }
+                dvis.slot = slot;
+                walk_sub(it.v, a.vp, c1.vp, c2.vp, dvis);
             };
             clip_triangle(it, e.x, emit);
         }
-        if (!WINNER)
-            acc.add(b, dvis.item, dvis.drawn_n, dvis.fragments, valid);
+        acc.add(b, dvis.item, dvis.drawn_n, dvis.fragments, valid);
     }
-    if (!WINNER) {
-        // tall triangles, one warp each
-        const uint32_t nt_raw = *counter32(b, C_TALL);
-        const uint32_t nt = nt_raw < b->list_cap ? nt_raw : b->list_cap;
-        const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
-        for (uint32_t k = gw; k < nt; k += n_warps) {
-            const uint32_t i = b->tall[k];
-            const uint32_t fr = walk_tall(b, i);
-            acc.add(b, b->recs[i].item, 0ull, fr, true);
-        }
-        acc.flush(b);
+}
+
+// Depth walk of the tall triangles, one warp each (warp-strided).
+__device__ __noinline__ void walk_tall_all(const BatchDev *b, ItemAcc &acc)
+{
+    const uint32_t nt_raw = *counter32(b, C_TALL);
+    const uint32_t nt = nt_raw < b->list_cap ? nt_raw : b->list_cap;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t k = gw; k < nt; k += n_warps) {
+        const uint32_t i = b->tall[k];
+        const uint32_t fr = walk_tall(b, i);
+        acc.add(b, b->recs[i].item, 0ull, fr, true);
     }
+}
+
+// Winner records of what the shade kernel does not replay, after the depth
+// keys are final: binned spans (one warp each, the qpixel chain as in
+// k_spans), near-clip triangles (one thread each) and, after a bin overflow,
+// every span of the walk list.
+__device__ __forceinline__ void spans_pass(const BatchDev *b, bool winner);
+
+__device__ __noinline__ void winner_clip(const BatchDev *b, bool overflow)
+{
+    const uint32_t n_raw = *counter32(b, C_CLIP);
+    const uint32_t n = n_raw < b->clip_cap ? n_raw : b->clip_cap;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint2 e = b->clip[b->clip_cap - 1 - i];
+        const ItemDev &it = b->items[e.y];
+        WinnerVisitor wvis{&it, 0u, b->inline_span, overflow};
+        auto emit = [&](uint32_t slot, const TV &a, const TV &c1, const TV &c2, bool) {
+            wvis.slot = slot;
+            walk_sub(it.v, a.vp, c1.vp, c2.vp, wvis);
+        };
+        clip_triangle(it, e.x, emit);
+    }
+}
+
+__device__ __noinline__ void winner_overflow(const BatchDev *b)
+{
+    const uint32_t n_raw = *counter32(b, C_LIST);
+    const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint2 e = b->list[i];
+        const ItemDev &it = b->items[e.y];
+        WinnerVisitor vis{&it, 2 * e.x, b->inline_span, true};
+        const uint4 tri = it.s.tris[e.x];
+        V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
+        int pa = 0, pb = 1, pc = 2;
+        sort_z_desc(a, c1, c2, pa, pb, pc);
+        walk_sub(it.v, a, c1, c2, vis);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_winners(const BatchDev *b)
+{
+    const bool overflow = *counter32(b, C_OVERFLOW) != 0u;
+    if (overflow) {
+        winner_overflow(b); // records every span, the binned ones included
+    } else {
+        spans_pass(b, true);
+    }
+    winner_clip(b, overflow);
 }
 
 // ------------------------------------------------------------- long spans --
@@ -1249,13 +1273,10 @@ __global__ void __launch_bounds__(128) k_walk_clip(const BatchDev *b)
 // bstep per pixel, interpolator.hpp:96-100) is serial in floating point, so
 // every lane runs the same 32 steps and keeps the state of its own pixel; the
 // divisions, depth and key work then run on all lanes.
-template <int WINNER>
-__global__ void __launch_bounds__(256) k_spans(const BatchDev *b)
+__device__ __forceinline__ void spans_pass(const BatchDev *b, bool winner)
 {
     const uint32_t n_raw = *counter32(b, C_SPANS);
     const uint32_t n = n_raw < b->span_cap ? n_raw : b->span_cap;
-    if (WINNER && *counter32(b, C_OVERFLOW))
-        return; // the overflow winner walk records every span
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -1285,13 +1306,15 @@ __global__ void __launch_bounds__(256) k_spans(const BatchDev *b)
                 continue;
             const unsigned long long key = make_key(z, r.slot);
             unsigned long long *kp = it.key + base + x;
-            if (!WINNER)
+            if (!winner)
                 key_min(kp, key);
             else if (*kp == key)
                 it.prec[base + x] = make_float4(alpha, r.progL, r.progR, __uint_as_float(r.y_bits & ~kYMask));
         }
     }
 }
+
+__global__ void __launch_bounds__(256) k_spans(const BatchDev *b) { spans_pass(b, false); }
 
 // ------------------------------------------------------------------ shade --
 
@@ -1586,9 +1609,8 @@ cudaError_t launch_world(const SceneDev &s, cudaStream_t st)
 
 const char *prof_kernel_name(int k)
 {
-    static const char *names[kProfKernels] = {"k_vertex", "k_flags",          "k_compact", "k_setup",
-                                              "k_walk",   "k_walk_clip+tall", "k_spans",   "winner records",
-                                              "k_shade",  "k_dof"};
+    static const char *names[kProfKernels] = {"k_vertex", "k_flags",   "k_compact", "k_setup", "k_walk",
+                                              "k_spans",  "k_winners", "k_shade",   "k_dof"};
     return (k >= 0 && k < kProfKernels) ? names[k] : "?";
 }
 
@@ -1656,19 +1678,16 @@ cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t
     n++;
     mark(PK_SETUP);
     k_setup<<<sms * 8, 256, 0, st>>>(b);
+    n++;
     mark(PK_WALK);
     k_walk<<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
-    mark(PK_RARE);
-    k_walk_clip<0><<<sms, 128, 0, st>>>(b);
-    n += 3;
+    n++;
     mark(PK_SPANS);
-    k_spans<0><<<sms * 4, 256, 0, st>>>(b);
+    k_spans<<<sms * 4, 256, 0, st>>>(b);
     n++;
     mark(PK_WINNER);
-    k_spans<1><<<sms * 4, 256, 0, st>>>(b);
-    k_walk_clip<1><<<sms, 128, 0, st>>>(b);
-    k_walk_winner<<<sms * 8, 128, 0, st>>>(b);
-    n += 3;
+    k_winners<<<sms * 4, 256, 0, st>>>(b);
+    n++;
     mark(PK_SHADE);
     if (tile == 8)
         k_shade<8><<<sms * SGL_SHADE_MIN_BLOCKS, kShadeThreads, 0, st>>>(b);

@@ -134,7 +134,7 @@ constexpr uint32_t kRecClip = 0xFFFFFFFFu; // recmap entry of a near-clipped tri
 
 // Batch counters (32-bit words); the drawn-triangle and fragment counts are
 // kept per item (item_counters) and summed by the host.
-enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_WALK_NEXT = 8, C_SHADE_NEXT = 9, C_TALL = 10 };
+enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_SHADE_NEXT = 9, C_TALL = 10 };
 constexpr int kCounterWords = 8; // 64-bit words
 
 // A batch of views rendered by one launch sequence (lives in device memory).
@@ -164,10 +164,8 @@ struct BatchDev {
 
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each stage of a launch sequence (enabled with sgl_profile).
-constexpr int kProfKernels = 10;
-enum ProfKernel {
-    PK_VERTEX = 0, PK_FLAGS, PK_COMPACT, PK_SETUP, PK_WALK, PK_RARE, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF
-};
+constexpr int kProfKernels = 9;
+enum ProfKernel { PK_VERTEX = 0, PK_FLAGS, PK_COMPACT, PK_SETUP, PK_WALK, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF };
 struct Profiler {
     bool enabled = false;
     cudaEvent_t ev[kProfKernels + 1] = {};
