@@ -205,15 +205,19 @@ def frame_measure(r, torch, steps: int, warmup: int, with_e2e: bool):
     torch.cuda.synchronize()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    r.profile(True)
     for k in range(steps):
         starts[k].record(stream)
         step(k)
         ends[k].record(stream)
     torch.cuda.synchronize()
+    frame_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / steps
+    # per-stage times in a separate pass: the stage events add their own gaps
+    r.profile(True)
+    for k in range(steps):
+        step(k)
+    torch.cuda.synchronize()
     prof = r.profile_read()
     r.profile(False)
-    frame_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / steps
     out = {"frame_ms": frame_ms, "stats": stats, "prof": prof, "alg_bytes": frame_alg_bytes(scene, v.w, v.h)}
     if with_e2e:
         host_pix = torch.zeros((v.h, v.w), dtype=torch.int32).pin_memory()
