@@ -1464,10 +1464,13 @@ __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(c
     const bool keep = b->keep_keys != 0;
     int item = -1;
     uint32_t lo = 0, hi = 0;
-    // tiles are taken from a shared counter; the next one is fetched while
-    // this one is shaded (the barriers of the loop order the exchange)
+    // Tiles come from kQueues queues (queue q holds tiles q, q + kQueues,
+    // ...; block b draws from queue b % kQueues); the next tile is fetched
+    // while this one is shaded (the barriers of the loop order the exchange).
+    const uint32_t qb = blockIdx.x % kQueues;
+    uint32_t *tile_q = counter32(b, C_SHADE_Q + 32 * (int)qb);
     if (threadIdx.x == 0)
-        tile_next = atomicAdd(counter32(b, C_SHADE_NEXT), 1u);
+        tile_next = qb + kQueues * atomicAdd(tile_q, 1u);
     __syncthreads();
     for (;;) {
         const uint32_t tg = tile_next;
@@ -1475,7 +1478,7 @@ __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(c
             break;
         __syncthreads(); // every thread has read tile_next
         if (threadIdx.x == 0)
-            tile_next = atomicAdd(counter32(b, C_SHADE_NEXT), 1u);
+            tile_next = qb + kQueues * atomicAdd(tile_q, 1u);
         if (tg < lo || tg >= hi) {
             item = find_item(b->tile_base, b->n_items, tg);
             lo = __ldg(b->tile_base + item);

@@ -134,8 +134,12 @@ constexpr uint32_t kRecClip = 0xFFFFFFFFu; // recmap entry of a near-clipped tri
 
 // Batch counters (32-bit words); the drawn-triangle and fragment counts are
 // kept per item (item_counters) and summed by the host.
-enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_SHADE_NEXT = 9, C_TALL = 10 };
-constexpr int kCounterWords = 8; // 64-bit words
+enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_TALL = 10 };
+// Work queues of the shade kernel's tiles: kQueues counters, one per 128-byte
+// line so that blocks of different queues do not contend.
+constexpr int kQueues = 16;
+constexpr int C_SHADE_Q = 32;                       // 32-bit index of queue q: C_SHADE_Q + 32 q
+constexpr int kCounterWords = (C_SHADE_Q + 32 * kQueues) / 2; // 64-bit words
 
 // A batch of views rendered by one launch sequence (lives in device memory).
 struct BatchDev {

@@ -273,9 +273,7 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
         CUDA_TRY(launch_batch(db, tile, sl.any_dof, stream, launches, prof));
     }
     keys_dirty = sl.keep_keys;
-    unsigned long long *hc = (unsigned long long *)sl.h_counters.ptr;
-    CUDA_TRY(cudaMemcpyAsync(hc, sl.d_counters.ptr, sizeof(unsigned long long) * kCounterWords,
-                             cudaMemcpyDeviceToHost, stream));
+    unsigned long long *hc = (unsigned long long *)sl.h_counters.ptr; // per-item counters only
     CUDA_TRY(cudaMemcpyAsync(hc + kCounterWords, sl.d_item_counters.ptr,
                              2 * sizeof(unsigned long long) * sl.n_items, cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaEventRecord(sl.done, stream));
