@@ -218,7 +218,8 @@ def frame_measure(r, torch, steps: int, warmup: int, with_e2e: bool):
     torch.cuda.synchronize()
     prof = r.profile_read()
     r.profile(False)
-    out = {"frame_ms": frame_ms, "stats": stats, "prof": prof, "alg_bytes": frame_alg_bytes(scene, v.w, v.h)}
+    out = {"frame_ms": frame_ms, "stats": stats, "prof": prof, "alg_bytes": frame_alg_bytes(scene, v.w, v.h),
+           "gpu_frame": (_bufs[0].cpu().numpy().view(np.uint32), _bufs[1].cpu().numpy())}
     if with_e2e:
         host_pix = torch.zeros((v.h, v.w), dtype=torch.int32).pin_memory()
         host_z = torch.zeros((v.h, v.w), dtype=torch.float32).pin_memory()
@@ -300,24 +301,29 @@ def run_frame(args, rank, world, local_rank):
         "clocks": clocks.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_frame_baseline(fm["scene"], fm["view"], args)
+        out["cpu_baseline"] = cpu_frame_baseline(fm["scene"], fm["view"], args, fm["gpu_frame"])
     r.close()
     if dist:
         dist.destroy_process_group()
     return out if rank == 0 else None
 
 
-def cpu_frame_baseline(scene, view, args) -> dict:
+def cpu_frame_baseline(scene, view, args, gpu_frame=None) -> dict:
     import oracle
 
     threads = cpu_threads()
-    n = max(threads, args.cpu_frames)
-    oracle.render_parallel(scene, [view] * threads, threads)
-    t0 = time.perf_counter()
-    oracle.render_parallel(scene, [view] * n, threads)
+    first = oracle.render_parallel(scene, [view] * threads, threads)
+    # about args.cpu_seconds of host work, one frame per thread at a time
+    n, t0 = 0, time.perf_counter()
+    while n < args.cpu_frames and (time.perf_counter() - t0) < args.cpu_seconds:
+        oracle.render_parallel(scene, [view] * threads, threads)
+        n += threads
     dt = time.perf_counter() - t0
-    return {"value": round(n / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": f"{n} frames of the 1080p frame on {threads} threads ({dt:.1f} s)"}
+    out = {"value": round(n / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+           "sample": f"{n} frames of the 1080p frame on {threads} threads ({dt:.1f} s)"}
+    if gpu_frame is not None:
+        out["parity"] = parity_of([gpu_frame], first[:1])
+    return out
 
 
 def serve_config(args) -> dict:
@@ -429,7 +435,8 @@ def run_serve(args, rank, world, local_rank):
         "clocks": clocks.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_serve_baseline(scenes, timed, args)
+        gpu_frames = gpu_sample_frames(r, sids, timed[:args.cpu_requests])
+        out["cpu_baseline"] = cpu_serve_baseline(scenes, timed, args, gpu_frames)
     r.close()
     if dist:
         dist.destroy_process_group()
@@ -502,22 +509,74 @@ def e2e_run(r, torch, sids, timed, M: int, args):
     return steps * M / dt, h2d, d2h
 
 
-def cpu_serve_baseline(scenes, timed, args) -> dict:
+def parity_of(gpu_frames, cpu_frames) -> dict:
+    """Depth bit-exactness and the per-pixel |dRGB| histogram (max over the
+    three channels) of GPU frames against the oracle's frames of the same
+    requests."""
+    hist = np.zeros(4, np.int64)
+    depth_ok = True
+    px = 0
+    for (gp, gz), cf in zip(gpu_frames, cpu_frames):
+        depth_ok &= bool(np.array_equal(gz.view(np.uint32), cf.zbuffer.view(np.uint32)))
+        a = gp.view(np.uint8).reshape(gp.shape + (4,))[..., :3].astype(np.int16)
+        b = cf.pixels.view(np.uint8).reshape(cf.pixels.shape + (4,))[..., :3].astype(np.int16)
+        d = np.abs(a - b).max(axis=-1)
+        hist += np.bincount(np.minimum(d, 3).ravel(), minlength=4)[:4]
+        px += d.size
+    return {"frames": len(gpu_frames), "pixels": int(px), "depth_bit_exact": depth_ok,
+            "rgb_abs_diff_hist_0_1_2_3plus": hist.tolist(),
+            "within_1lsb": round(float(hist[:2].sum()) / max(px, 1), 6), "max_lsb_le_2": bool(hist[3] == 0)}
+
+
+def gpu_sample_frames(r, sids, sample) -> list:
+    """The GPU frames (colour, depth) of a bounded request sample, through the
+    serving loop with copy-out."""
+    srv = r.server(copy_out=True)
+    out = []
+    for (_, k, v) in sample:
+        pix = np.zeros((v.h, v.w), np.uint32)
+        z = np.zeros((v.h, v.w), np.float32)
+        srv.submit(sids[k], v, pix, z)
+        out.append((pix, z))
+    srv.drain(600.0)
+    srv.close()
+    return out
+
+
+def cpu_serve_baseline(scenes, timed, args, gpu_frames=None) -> dict:
     """The oracle restatement on all host threads over a bounded prefix of the
-    request stream, grouped by scene."""
+    request stream, grouped by scene; with the GPU frames of the same requests
+    it also checks them (depth bits, |dRGB| histogram)."""
     import oracle
 
     threads = cpu_threads()
-    sample = timed[:args.cpu_requests]
-    t0 = time.perf_counter()
-    by_scene = {}
-    for (_, k, v) in sample:
-        by_scene.setdefault(k, []).append(v)
-    for k, views in by_scene.items():
-        oracle.render_parallel(scenes[k], views, threads)
+    chunk = args.cpu_requests
+
+    def render_chunk(sample, keep: bool):
+        by_scene = {}
+        for j, (_, k, v) in enumerate(sample):
+            by_scene.setdefault(k, []).append((j, v))
+        frames_out = [None] * len(sample) if keep else None
+        for k, jv in by_scene.items():
+            frames = oracle.render_parallel(scenes[k], [v for (_, v) in jv], threads)
+            if keep:
+                for (j, _), f in zip(jv, frames):
+                    frames_out[j] = f
+        return frames_out
+
+    # the first chunk is also the parity sample; then about args.cpu_seconds of host work in all
+    n, t0 = 0, time.perf_counter()
+    cpu_frames = render_chunk(timed[:chunk], True)
+    n += len(timed[:chunk])
+    while n + chunk <= len(timed) and (time.perf_counter() - t0) < args.cpu_seconds:
+        render_chunk(timed[n:n + chunk], False)
+        n += chunk
     dt = time.perf_counter() - t0
-    return {"value": round(len(sample) / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": f"the first {len(sample)} requests of the stream on {threads} threads ({dt:.1f} s)"}
+    out = {"value": round(n / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+           "sample": f"the first {n} requests of the stream on {threads} threads ({dt:.1f} s)"}
+    if gpu_frames is not None:
+        out["parity"] = parity_of(gpu_frames, cpu_frames)
+    return out
 
 
 def run_reference(args, rank, world):
@@ -587,7 +646,8 @@ def main():
     ap.add_argument("--budget", type=int, default=40 << 30)
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--streams", type=int, default=3)
-    ap.add_argument("--cpu-frames", type=int, default=32)
+    ap.add_argument("--cpu-frames", type=int, default=4096, help="CPU baseline: at most this many 1080p frames")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline: about this much host work")
     ap.add_argument("--cpu-requests", type=int, default=48)
     ap.add_argument("--cpu-requests-per-step", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
