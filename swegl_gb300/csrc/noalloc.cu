@@ -104,7 +104,7 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     const size_t o_item = off;
     off += up256(sizeof(ItemDev));
     const size_t o_bases = off;
-    off += up256(8 * sizeof(uint32_t));
+    off += up256(10 * sizeof(uint32_t));
     const size_t o_counters = off;
     off += up256(kCounterWords * sizeof(unsigned long long));
     const size_t o_item_counters = off;
@@ -170,20 +170,26 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
         it.dof_rmax = d.max_radius;
         it.p22 = v.proj[10];
         it.p23 = v.proj[11];
+        it.dof_halo = dof_halo_of(d.max_radius);
+        it.dof_tiles_x = (v.w + kDofTile - 1) / kDofTile;
     }
-    const uint32_t bases[8] = {0u, (uint32_t)nv, 0u, (uint32_t)nt, 0u, (uint32_t)px, 0u, (uint32_t)tiles};
+    const uint32_t dof_tiles =
+        dof ? (uint32_t)((v.w + kDofTile - 1) / kDofTile) * (uint32_t)((v.h + kDofTile - 1) / kDofTile) : 0u;
+    const uint32_t bases[10] = {0u, (uint32_t)nv, 0u, (uint32_t)nt, 0u, (uint32_t)px, 0u, (uint32_t)tiles, 0u, dof_tiles};
     BatchDev b{};
     b.items = (const ItemDev *)(base + o_item);
     b.vtx_base = (const uint32_t *)(base + o_bases);
     b.tri_base = b.vtx_base + 2;
     b.px_base = b.vtx_base + 4;
     b.tile_base = b.vtx_base + 6;
+    b.dof_base = b.vtx_base + 8;
     b.n_items = 1;
     b.inline_span = ctx->inline_span;
     b.total_vtx = (uint32_t)nv;
     b.total_tri = (uint32_t)nt;
     b.total_px = (uint32_t)px;
     b.total_tiles = (uint32_t)tiles;
+    b.total_dof_tiles = dof_tiles;
     b.list = (uint2 *)(base + o_list);
     b.list_cap = (uint32_t)(nt ? nt : 1);
     b.clip = b.list;

@@ -1547,6 +1547,22 @@ __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(c
 
 __constant__ float2 c_dof_taps[SGL_DOF_TAPS];
 
+// Circle of confusion of pixel i of a depth-of-field item.
+__device__ __forceinline__ float dof_radius(const ItemDev &it, uint32_t i)
+{
+    const float zp = it.zbuf[i];
+    const float zv = (zp - it.p23) / it.p22;
+    float r = (it.dof_ka * fabsf(zv - it.dof_focus)) / zv;
+    if (!(r >= 0.0f && r <= it.dof_rmax))
+        r = it.dof_rmax;
+    return r;
+}
+
+__device__ __forceinline__ uint32_t dof_average(uint32_t centre, uint32_t sb, uint32_t sg, uint32_t sr)
+{
+    return (centre & 0xFF000000u) | (((sr + 16u) / 32u) << 16) | (((sg + 16u) / 32u) << 8) | ((sb + 16u) / 32u);
+}
+
 // Depth-of-field gather (replaces post_shader_depth_box,
 // swegl/render/post_shaders.hpp:51-132).  Per pixel: view-space depth from the
 // z-buffer, z = (z' - P23) / P22; circle of confusion r = K*A*|z - F| / z
@@ -1554,36 +1570,94 @@ __constant__ float2 c_dof_taps[SGL_DOF_TAPS];
 // pattern (sgl_dof_taps.h) at offsets roundf(r * tap), clamped to the
 // viewport, with integer sums rounded half up.  Every step is exact integer
 // or IEEE float arithmetic, so the CPU oracle gives the same bits.
+//
+// A block takes kDofTile x kDofTile tiles of the items that ask for the
+// gather and stages the tile with its halo (the taps reach at most
+// ceil(max_radius) pixels: every tap component is below 1), clamped to the
+// view as the taps are, in shared memory; the 32 taps of each pixel then read
+// shared memory without further clamping.  Views whose reach exceeds
+// kDofMaxHalo gather from the colour buffer.
 __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
 {
-    for_each_in_items(b, b->px_base, b->total_px, [&](int item, uint32_t i) {
-        const ItemDev &it = b->items[item];
-        if (!it.dof)
-            return;
-        const int w = it.v.w, h = it.v.h;
-        const int y = (int)(i / (uint32_t)w), x = (int)(i - (uint32_t)y * (uint32_t)w);
-        const float zp = it.zbuf[i];
-        const float zv = (zp - it.p23) / it.p22;
-        float r = (it.dof_ka * fabsf(zv - it.dof_focus)) / zv;
-        if (!(r >= 0.0f && r <= it.dof_rmax))
-            r = it.dof_rmax;
-        uint32_t sb = 0, sg = 0, sr = 0;
-#pragma unroll 8
-        for (int k = 0; k < SGL_DOF_TAPS; k++) {
-            const float2 t = c_dof_taps[k];
-            int sx = x + (int)roundf(r * t.x), sy = y + (int)roundf(r * t.y);
-            sx = sx < 0 ? 0 : (sx >= w ? w - 1 : sx);
-            sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
-            const uint32_t c = __ldg(it.pixels + (size_t)sy * it.pitch_px + sx);
-            sb += c & 0xFFu;
-            sg += (c >> 8) & 0xFFu;
-            sr += (c >> 16) & 0xFFu;
+    constexpr int S_MAX = kDofTile + 2 * kDofMaxHalo;
+    __shared__ uint32_t halo[S_MAX * S_MAX];
+    int item = -1;
+    uint32_t lo = 0, hi = 0;
+    for (uint32_t tg = blockIdx.x; tg < b->total_dof_tiles; tg += gridDim.x) {
+        if (tg < lo || tg >= hi) {
+            item = find_item(b->dof_base, b->n_items, tg);
+            lo = __ldg(b->dof_base + item);
+            hi = __ldg(b->dof_base + item + 1);
         }
-        const uint32_t centre = it.pixels[(size_t)y * it.pitch_px + x];
-        const uint32_t out = (centre & 0xFF000000u) | (((sr + 16u) / 32u) << 16) | (((sg + 16u) / 32u) << 8) |
-                             ((sb + 16u) / 32u);
-        it.dof_out[(size_t)y * it.dof_pitch + x] = out;
-    });
+        const ItemDev &it = b->items[item];
+        const int w = it.v.w, h = it.v.h;
+        const uint32_t tl = tg - lo;
+        const int x0 = (int)(tl % (uint32_t)it.dof_tiles_x) * kDofTile;
+        const int y0 = (int)(tl / (uint32_t)it.dof_tiles_x) * kDofTile;
+        const int R = it.dof_halo;
+        const int S = kDofTile + 2 * R;
+        if (R >= 0) {
+            // rows of the halo to warps, columns to lanes (S <= 96: 3 per lane)
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            int c0 = x0 - R + lane, c1 = c0 + 32, c2 = c0 + 64;
+            c0 = c0 < 0 ? 0 : (c0 >= w ? w - 1 : c0);
+            c1 = c1 < 0 ? 0 : (c1 >= w ? w - 1 : c1);
+            c2 = c2 < 0 ? 0 : (c2 >= w ? w - 1 : c2);
+#pragma unroll 4
+            for (int yy = warp; yy < S; yy += 8) {
+                int sy = y0 - R + yy;
+                sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
+                const uint32_t *row = it.pixels + (size_t)sy * it.pitch_px;
+                uint32_t *dst = halo + yy * S;
+                if (lane < S)
+                    dst[lane] = __ldg(row + c0);
+                if (lane + 32 < S)
+                    dst[lane + 32] = __ldg(row + c1);
+                if (lane + 64 < S)
+                    dst[lane + 64] = __ldg(row + c2);
+            }
+            __syncthreads();
+        }
+        for (int p = threadIdx.x; p < kDofTile * kDofTile; p += blockDim.x) {
+            const int x = x0 + (p & (kDofTile - 1)), y = y0 + p / kDofTile;
+            if (x >= w || y >= h)
+                continue;
+            const uint32_t i = (uint32_t)y * (uint32_t)w + (uint32_t)x;
+            const float r = dof_radius(it, i);
+            uint32_t out;
+            if (R >= 0) {
+                // the halo holds the view-clamped pixels, so a tap needs no clamp:
+                // |offset| <= ceil(r) <= R keeps it inside
+                const uint32_t *c = halo + (y - y0 + R) * S + (x - x0 + R);
+                uint32_t br = 0, ga = 0; // two 16-bit lanes each: 32 taps x 255 fit
+#pragma unroll 8
+                for (int k = 0; k < SGL_DOF_TAPS; k++) {
+                    const float2 t = c_dof_taps[k];
+                    const uint32_t v = c[(int)roundf(r * t.y) * S + (int)roundf(r * t.x)];
+                    br += v & 0x00FF00FFu;
+                    ga += (v >> 8) & 0x00FF00FFu;
+                }
+                out = dof_average(c[0], br & 0xFFFFu, ga & 0xFFFFu, br >> 16);
+            } else {
+                uint32_t sb = 0, sg = 0, sr = 0;
+#pragma unroll 8
+                for (int k = 0; k < SGL_DOF_TAPS; k++) {
+                    const float2 t = c_dof_taps[k];
+                    int sx = x + (int)roundf(r * t.x), sy = y + (int)roundf(r * t.y);
+                    sx = sx < 0 ? 0 : (sx >= w ? w - 1 : sx);
+                    sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
+                    const uint32_t v = __ldg(it.pixels + (size_t)sy * it.pitch_px + sx);
+                    sb += v & 0xFFu;
+                    sg += (v >> 8) & 0xFFu;
+                    sr += (v >> 16) & 0xFFu;
+                }
+                out = dof_average(it.pixels[(size_t)y * it.pitch_px + x], sb, sg, sr);
+            }
+            it.dof_out[(size_t)y * it.dof_pitch + x] = out;
+        }
+        if (R >= 0)
+            __syncthreads(); // the halo is reused by the next tile
+    }
 }
 
 // ---------------------------------------------------------------- launches --

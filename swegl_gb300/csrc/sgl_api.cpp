@@ -529,6 +529,9 @@ SGL_API sgl_status sgl_dof(sgl_ctx *c, const sgl_view *view, const sgl_target *i
     it.dof_rmax = v.dof.max_radius;
     it.p22 = v.proj[10];
     it.p23 = v.proj[11];
+    it.dof_halo = dof_halo_of(v.dof.max_radius);
+    it.dof_tiles_x = (v.w + kDofTile - 1) / kDofTile;
+    const uint32_t dof_tiles = (uint32_t)it.dof_tiles_x * (uint32_t)((v.h + kDofTile - 1) / kDofTile);
     CUDA_TRY(ctx->dof_desc.ensure(sizeof(ItemDev) + sizeof(BatchDev) + 4 * sizeof(uint32_t)));
     uint8_t *dd = (uint8_t *)ctx->dof_desc.ptr;
     ItemDev *d_it = (ItemDev *)dd;
@@ -537,9 +540,11 @@ SGL_API sgl_status sgl_dof(sgl_ctx *c, const sgl_view *view, const sgl_target *i
     BatchDev b{};
     b.items = d_it;
     b.px_base = d_base;
+    b.dof_base = d_base + 2;
     b.n_items = 1;
     b.total_px = (uint32_t)px;
-    const uint32_t base[2] = {0u, (uint32_t)px};
+    b.total_dof_tiles = dof_tiles;
+    const uint32_t base[4] = {0u, (uint32_t)px, 0u, dof_tiles};
     CUDA_TRY(cudaMemcpyAsync(d_it, &it, sizeof it, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_b, &b, sizeof b, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_base, base, sizeof base, cudaMemcpyHostToDevice, st));

@@ -84,7 +84,26 @@ struct ItemDev {
     float dof_focus, dof_ka, dof_rmax, p22, p23;
     uint32_t *dof_out;
     int dof_pitch;
+    int dof_halo;    // tap reach in pixels (ceil of max_radius, <= kDofMaxHalo), -1: gather from memory
+    int dof_tiles_x; // kDofTile tiles across the view
 };
+
+// Depth-of-field tiles: kDofTile x kDofTile pixels with a halo of up to
+// kDofMaxHalo pixels staged in shared memory.
+constexpr int kDofTile = 32;
+constexpr int kDofMaxHalo = 32;
+
+// The tap reach of a depth-of-field view: ceil(max_radius) when it fits the
+// staged halo, else -1 (the gather then reads the colour buffer directly).
+inline int dof_halo_of(float max_radius)
+{
+    if (!(max_radius >= 0.0f && max_radius <= (float)kDofMaxHalo))
+        return -1;
+    int h = (int)max_radius;
+    if ((float)h < max_radius)
+        h++;
+    return h;
+}
 
 // A span handed from the triangle walk to the long-span kernels: the qpixel
 // interpolator of fill_half_triangle after its displacement to x1.
@@ -148,9 +167,10 @@ struct BatchDev {
     const uint32_t *tri_base;  // n_items + 1 prefix of triangle counts
     const uint32_t *px_base;   // n_items + 1 prefix of pixel counts
     const uint32_t *tile_base; // n_items + 1 prefix of shade-tile counts
+    const uint32_t *dof_base;  // n_items + 1 prefix of depth-of-field tile counts (0 for items without)
     int n_items;
     int inline_span;           // spans wider than this go to the long-span bins
-    uint32_t total_vtx, total_tri, total_px, total_tiles;
+    uint32_t total_vtx, total_tri, total_px, total_tiles, total_dof_tiles;
     uint2 *list;               // drawable triangles {t, item}
     uint32_t list_cap;
     uint2 *clip;               // drawable triangles crossing the near plane {t, item}: entry j at clip[clip_cap - 1 - j]

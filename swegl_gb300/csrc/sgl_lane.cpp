@@ -77,12 +77,12 @@ sgl_status Lane::init(Ctx *ctx, int max_items_, cudaStream_t external, bool bloc
     }
     for (auto &sl : slots) {
         CUDA_TRY(sl.d_items.ensure(sizeof(ItemDev) * (size_t)max_items));
-        CUDA_TRY(sl.d_bases.ensure(sizeof(uint32_t) * 4 * ((size_t)max_items + 1)));
+        CUDA_TRY(sl.d_bases.ensure(sizeof(uint32_t) * 5 * ((size_t)max_items + 1)));
         CUDA_TRY(sl.d_batch.ensure(sizeof(BatchDev)));
         CUDA_TRY(sl.d_counters.ensure(sizeof(unsigned long long) * kCounterWords));
         CUDA_TRY(sl.d_item_counters.ensure(2 * sizeof(unsigned long long) * (size_t)max_items));
         CUDA_TRY(sl.h_items.ensure(sizeof(ItemDev) * (size_t)max_items));
-        CUDA_TRY(sl.h_bases.ensure(sizeof(uint32_t) * 4 * ((size_t)max_items + 1)));
+        CUDA_TRY(sl.h_bases.ensure(sizeof(uint32_t) * 5 * ((size_t)max_items + 1)));
         CUDA_TRY(sl.h_batch.ensure(sizeof(BatchDev)));
         CUDA_TRY(sl.h_counters.ensure(sizeof(unsigned long long) * (kCounterWords + 2 * (size_t)max_items)));
         CUDA_TRY(cudaEventCreateWithFlags(&sl.staged, cudaEventDisableTiming));
@@ -105,8 +105,8 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         CUDA_TRY(cudaEventSynchronize(sl.done)); // its staging buffers are free again
     // prefixes and pool offsets
     uint32_t *hb = (uint32_t *)sl.h_bases.ptr;
-    uint32_t *vb = hb, *tb = hb + (n + 1), *pb = hb + 2 * (n + 1), *gb = hb + 3 * (n + 1);
-    uint64_t tv = 0, tt = 0, tp = 0, tg = 0, dof_px = 0, dofz_px = 0;
+    uint32_t *vb = hb, *tb = hb + (n + 1), *pb = hb + 2 * (n + 1), *gb = hb + 3 * (n + 1), *fb = hb + 4 * (n + 1);
+    uint64_t tv = 0, tt = 0, tp = 0, tg = 0, tf = 0, dof_px = 0, dofz_px = 0;
     size_t ndc_off = 0, yes_off = 0;
     std::vector<size_t> ndc_at(n), yes_at(n), dof_at(n), dofz_at(n);
     for (int i = 0; i < n; i++) {
@@ -116,10 +116,13 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         tb[i] = (uint32_t)tt;
         pb[i] = (uint32_t)tp;
         gb[i] = (uint32_t)tg;
+        fb[i] = (uint32_t)tf;
         tv += s.n_vertices;
         tt += s.n_triangles;
         tp += (uint64_t)v.w * v.h;
         tg += (uint64_t)((v.w + tile - 1) / tile) * (uint64_t)((v.h + tile - 1) / tile);
+        if (v.dof.enabled)
+            tf += (uint64_t)((v.w + kDofTile - 1) / kDofTile) * (uint64_t)((v.h + kDofTile - 1) / kDofTile);
         ndc_at[i] = ndc_off;
         yes_at[i] = yes_off;
         ndc_off += align_up(s.n_vertices, 16);
@@ -132,7 +135,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
                 dofz_px += align_up((size_t)v.w * v.h, 64);
         }
     }
-    if (tv >= (1ull << 32) || tt >= (1ull << 31) || tp >= (1ull << 32) || tg >= (1ull << 32)) {
+    if (tv >= (1ull << 32) || tt >= (1ull << 31) || tp >= (1ull << 32) || tg >= (1ull << 32) || tf >= (1ull << 32)) {
         ctx->fail("batch too large (%llu vertices, %llu triangles, %llu pixels)", (unsigned long long)tv,
                   (unsigned long long)tt, (unsigned long long)tp);
         return SGL_ERR_UNSUPPORTED;
@@ -141,6 +144,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     tb[n] = (uint32_t)tt;
     pb[n] = (uint32_t)tp;
     gb[n] = (uint32_t)tg;
+    fb[n] = (uint32_t)tf;
     const size_t span_cap = std::max<size_t>(65536, tp / 8);
     CUDA_TRY(ndc.ensure(sizeof(float4) * std::max<size_t>(ndc_off, 1)));
     CUDA_TRY(yes.ensure(std::max<size_t>(yes_off, 1)));
@@ -195,6 +199,8 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
             it.dof_rmax = d.max_radius;
             it.p22 = en.view.proj[10];
             it.p23 = en.view.proj[11];
+            it.dof_halo = dof_halo_of(d.max_radius);
+            it.dof_tiles_x = (en.view.w + kDofTile - 1) / kDofTile;
         }
         hi[i] = it;
     }
@@ -206,12 +212,14 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.tri_base = db + (n + 1);
     bd.px_base = db + 2 * (n + 1);
     bd.tile_base = db + 3 * (n + 1);
+    bd.dof_base = db + 4 * (n + 1);
     bd.n_items = n;
     bd.inline_span = inline_span;
     bd.total_vtx = (uint32_t)tv;
     bd.total_tri = (uint32_t)tt;
     bd.total_px = (uint32_t)tp;
     bd.total_tiles = (uint32_t)tg;
+    bd.total_dof_tiles = (uint32_t)tf;
     bd.list = (uint2 *)list.ptr;
     bd.list_cap = (uint32_t)std::max<uint64_t>(tt, 1);
     bd.clip = (uint2 *)list.ptr; // shares the list buffer, filled from its end
@@ -228,7 +236,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.slot_flags = slot_flags;
     *hbd = bd;
     CUDA_TRY(cudaMemcpyAsync(sl.d_items.ptr, hi, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(sl.d_bases.ptr, hb, sizeof(uint32_t) * 4 * (n + 1), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(sl.d_bases.ptr, hb, sizeof(uint32_t) * 5 * (n + 1), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(sl.d_batch.ptr, hbd, sizeof(BatchDev), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemsetAsync(sl.d_counters.ptr, 0, sizeof(unsigned long long) * kCounterWords, stream));
     CUDA_TRY(cudaMemsetAsync(sl.d_item_counters.ptr, 0, 2 * sizeof(unsigned long long) * n, stream));

@@ -37,6 +37,21 @@ def test_dof_kernel_bit_exact(renderer):
     assert int((got != ref.pixels).sum()) > 1000  # the gather did blur
 
 
+@pytest.mark.parametrize("max_radius,w,h", [(16.0, 480, 270), (5.5, 97, 61), (40.0, 300, 200), (0.0, 64, 48)])
+def test_dof_kernel_radius_and_edges(renderer, max_radius, w, h):
+    """Reaches staged in shared memory (<= 32 px, with tiles cut by the view
+    edge) and larger ones read from memory give the oracle's bits."""
+    sc = G.scene("spheres200")
+    v = S.spheres_view(w, h)
+    v.dof = True
+    v.dof_max_radius = max_radius
+    v.dof_aperture = 0.2
+    ref = oracle.render(sc, [S.spheres_view(w, h)])
+    got = renderer.dof(v, ref.pixels, ref.zbuffer)
+    exp = oracle.dof(v, ref.pixels, ref.zbuffer)
+    assert np.array_equal(got, exp)
+
+
 def test_render_with_dof_matches_oracle(renderer):
     sc = G.scene("spheres200")
     sid = renderer.upload(sc)
