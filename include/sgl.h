@@ -139,6 +139,24 @@ typedef struct sgl_dof_desc {
     float px_scale;     /* pixels per world unit at unit distance; 0 = P11*h/2 */
 } sgl_dof_desc;
 
+/* The viewport's pixel shader (viewport_t::m_pixel_shader, a
+ * pixel_shader_t of swegl/render/pixel_shaders.hpp).  The combinations are
+ * pixel_shader_light_and_texture<L, T> (pixel_shaders.hpp:121-179); the
+ * single shaders write what their shade() returns (for the light shaders,
+ * the light value 65536 * L as the int colour, as the reference does). */
+enum {
+    SGL_SHADER_PHONG_BILINEAR = 0, /* <pixel_shader_lights_phong, pixel_shader_texture_bilinear> */
+    SGL_SHADER_PHONG_NEAREST  = 1, /* <pixel_shader_lights_phong, pixel_shader_texture> */
+    SGL_SHADER_FLAT_BILINEAR  = 2, /* <pixel_shader_lights_flat, pixel_shader_texture_bilinear> */
+    SGL_SHADER_FLAT_NEAREST   = 3, /* <pixel_shader_lights_flat, pixel_shader_texture> */
+    SGL_SHADER_COLOR          = 4, /* pixel_shader_t: the material colour */
+    SGL_SHADER_BILINEAR       = 5, /* pixel_shader_texture_bilinear */
+    SGL_SHADER_NEAREST        = 6, /* pixel_shader_texture */
+    SGL_SHADER_PHONG          = 7, /* pixel_shader_lights_phong */
+    SGL_SHADER_FLAT           = 8, /* pixel_shader_lights_flat */
+    SGL_SHADER_COUNT          = 9
+};
+
 /* viewport_t + camera_t (swegl/render/viewport.hpp:27-62,
  * swegl/projection/camera.hpp:10-24). */
 typedef struct sgl_view {
@@ -147,6 +165,7 @@ typedef struct sgl_view {
     float        proj[16];          /* camera_t::m_projectionmatrix, row-major */
     float        camera_pos[3];     /* camera_t::m_center */
     sgl_dof_desc dof;
+    int          shader;            /* SGL_SHADER_*; 0 = Phong + bilinear */
 } sgl_view;
 
 /* The SDL_Surface fields the reference writes (pixels, pitch, w, h with

@@ -15,9 +15,10 @@
 // call, renders each viewport in order through the C ABI (include/sgl.h) and
 // writes the viewport rectangle of its SDL surface and its z-buffer, as the
 // reference does.  Differences, all explicit:
-//   * only pixel_shader_light_and_texture<pixel_shader_lights_phong,
-//     pixel_shader_texture_bilinear> and opaque viewports (0 transparency
-//     layers) run on the GPU; other shaders and layered viewports throw
+//   * the reference's pixel shaders (pixel_shader_t, the flat and Phong light
+//     shaders, the nearest and bilinear texture shaders and their
+//     pixel_shader_light_and_texture<L, T> combinations) and opaque viewports
+//     (0 transparency layers) run on the GPU; layered viewports throw
 //     swegl::render_error (there is no CPU fallback);
 //   * the scene is not mutated (v_world, v_viewport, normal_world, yes and
 //     the temporary clip vertices of the reference are not written back);
@@ -401,21 +402,37 @@ inline node_t make_sphere(unsigned precision, float radius, int material_idx)
 // ------------------------------------------------------------ shader plug-ins --
 
 // The pixel-shader plug-ins of swegl/render/pixel_shaders.hpp.  On the GPU they
-// are tags: only pixel_shader_light_and_texture<pixel_shader_lights_phong,
-// pixel_shader_texture_bilinear> is implemented.
+// are tags naming one of the shaders of sgl.h (SGL_SHADER_*): the material
+// colour of pixel_shader_t, the two light shaders, the two texture shaders and
+// their pixel_shader_light_and_texture<L, T> combinations.  A shader of the
+// caller's own (another subclass) has no GPU counterpart.
 struct pixel_shader_t {
     virtual ~pixel_shader_t() = default;
-    virtual bool gpu_phong_bilinear() const { return false; }
+    virtual int gpu_shader() const { return SGL_SHADER_COLOR; }
 };
-struct pixel_shader_lights_flat : pixel_shader_t {};
-struct pixel_shader_lights_phong : pixel_shader_t {};
-struct pixel_shader_texture : pixel_shader_t {};
-struct pixel_shader_texture_bilinear : pixel_shader_t {};
+struct pixel_shader_lights_flat : pixel_shader_t {
+    int gpu_shader() const override { return SGL_SHADER_FLAT; }
+};
+struct pixel_shader_lights_phong : pixel_shader_t {
+    int gpu_shader() const override { return SGL_SHADER_PHONG; }
+};
+struct pixel_shader_texture : pixel_shader_t {
+    int gpu_shader() const override { return SGL_SHADER_NEAREST; }
+};
+struct pixel_shader_texture_bilinear : pixel_shader_t {
+    int gpu_shader() const override { return SGL_SHADER_BILINEAR; }
+};
 template <typename L, typename T>
 struct pixel_shader_light_and_texture : pixel_shader_t {
-    bool gpu_phong_bilinear() const override
+    int gpu_shader() const override
     {
-        return std::is_same<L, pixel_shader_lights_phong>::value && std::is_same<T, pixel_shader_texture_bilinear>::value;
+        constexpr bool phong = std::is_same<L, pixel_shader_lights_phong>::value;
+        constexpr bool flat = std::is_same<L, pixel_shader_lights_flat>::value;
+        constexpr bool bil = std::is_same<T, pixel_shader_texture_bilinear>::value;
+        constexpr bool near = std::is_same<T, pixel_shader_texture>::value;
+        static_assert((phong || flat) && (bil || near), "a light shader and a texture shader of swegl");
+        return phong ? (bil ? SGL_SHADER_PHONG_BILINEAR : SGL_SHADER_PHONG_NEAREST)
+                     : (bil ? SGL_SHADER_FLAT_BILINEAR : SGL_SHADER_FLAT_NEAREST);
     }
 };
 
@@ -649,9 +666,8 @@ inline int resident(const scene_t &s)
 
 inline void render_one(int scene_id, viewport_t &vp)
 {
-    if (!vp.m_pixel_shader || !vp.m_pixel_shader->gpu_phong_bilinear())
-        throw render_error(SGL_ERR_UNSUPPORTED, "the GPU path renders pixel_shader_light_and_texture<"
-                                                "pixel_shader_lights_phong, pixel_shader_texture_bilinear> only");
+    if (!vp.m_pixel_shader)
+        throw render_error(SGL_ERR_INVALID, "viewport without a pixel shader");
     if (vp.m_got_transparency)
         throw render_error(SGL_ERR_UNSUPPORTED, "the GPU path renders opaque viewports (0 transparency layers)");
     if (!vp.m_screen || !vp.m_screen->format || vp.m_screen->format->BytesPerPixel != 4)
@@ -667,6 +683,7 @@ inline void render_one(int scene_id, viewport_t &vp)
     v.camera_pos[1] = vp.m_camera.m_center.y();
     v.camera_pos[2] = vp.m_camera.m_center.z();
     v.dof = vp.m_post_shader ? vp.m_post_shader->dof() : sgl_dof_desc{0, 0, 0, 0, 0};
+    v.shader = vp.m_pixel_shader->gpu_shader();
     sgl_target t{vp.m_screen->pixels, vp.m_screen->pitch, vp.m_screen->w, vp.m_screen->h, vp.m_zbuffer.get()};
     check(sgl_render(context(), scene_id, &v, &t, 1, 0, nullptr, nullptr), "sgl_render");
 }

@@ -18,6 +18,8 @@
  *   kind 2  bits of the per-pixel perspective progress
  *   kind 3  the Phong light value (65536 * L, as the int the shader returns)
  *   kind 4  the bilinear texel colour alone
+ * Kind 0 renders with the reference shader the view's `shader` field names
+ * (SGL_SHADER_*, include/sgl.h).
  */
 #include <cstring>
 #include <memory>
@@ -47,16 +49,56 @@ struct progress_shader : swegl::pixel_shader_t {
     }
 };
 
-// Counts prepare_for_triangle calls while forwarding to the full shader.
-struct counting_full_shader
-    : swegl::pixel_shader_light_and_texture<swegl::pixel_shader_lights_phong, swegl::pixel_shader_texture_bilinear> {
+// Counts prepare_for_triangle calls while forwarding to a reference shader.
+struct counting_base {
     uint64_t calls = 0;
+};
+template <class S>
+struct counting : S, counting_base {
     void prepare_for_triangle(swegl::vertex_idx i0, swegl::vertex_idx i1, swegl::vertex_idx i2, bool inv) override
     {
         calls++;
-        pixel_shader_light_and_texture::prepare_for_triangle(i0, i1, i2, inv);
+        S::prepare_for_triangle(i0, i1, i2, inv);
     }
 };
+using counting_full_shader =
+    counting<swegl::pixel_shader_light_and_texture<swegl::pixel_shader_lights_phong, swegl::pixel_shader_texture_bilinear>>;
+
+// The reference's own pixel shader for an SGL_SHADER_* mode (include/sgl.h).
+std::shared_ptr<swegl::pixel_shader_t> shader_for_mode(int mode, counting_base **counter)
+{
+    using namespace swegl;
+    std::shared_ptr<pixel_shader_t> p;
+    counting_base *c = nullptr;
+    auto make = [&](auto tag) {
+        auto q = std::make_shared<counting<typename decltype(tag)::type>>();
+        c = q.get();
+        p = q;
+    };
+    struct phong_bil { using type = pixel_shader_light_and_texture<pixel_shader_lights_phong, pixel_shader_texture_bilinear>; };
+    struct phong_near { using type = pixel_shader_light_and_texture<pixel_shader_lights_phong, pixel_shader_texture>; };
+    struct flat_bil { using type = pixel_shader_light_and_texture<pixel_shader_lights_flat, pixel_shader_texture_bilinear>; };
+    struct flat_near { using type = pixel_shader_light_and_texture<pixel_shader_lights_flat, pixel_shader_texture>; };
+    struct color { using type = pixel_shader_t; };
+    struct bil { using type = pixel_shader_texture_bilinear; };
+    struct near { using type = pixel_shader_texture; };
+    struct phong { using type = pixel_shader_lights_phong; };
+    struct flat { using type = pixel_shader_lights_flat; };
+    switch (mode) {
+    case SGL_SHADER_PHONG_BILINEAR: make(phong_bil{}); break;
+    case SGL_SHADER_PHONG_NEAREST: make(phong_near{}); break;
+    case SGL_SHADER_FLAT_BILINEAR: make(flat_bil{}); break;
+    case SGL_SHADER_FLAT_NEAREST: make(flat_near{}); break;
+    case SGL_SHADER_COLOR: make(color{}); break;
+    case SGL_SHADER_BILINEAR: make(bil{}); break;
+    case SGL_SHADER_NEAREST: make(near{}); break;
+    case SGL_SHADER_PHONG: make(phong{}); break;
+    case SGL_SHADER_FLAT: make(flat{}); break;
+    default: break;
+    }
+    *counter = c;
+    return p;
+}
 
 swegl::matrix44_t to_matrix(const float *m)
 {
@@ -157,13 +199,18 @@ __attribute__((visibility("default"))) int ref_render(const sgl_scene_desc *desc
     std::vector<SDL_PixelFormat> formats(n_views, SDL_PixelFormat{4});
     std::vector<SDL_Surface> surfaces(n_views);
     std::vector<std::shared_ptr<swegl::pixel_shader_t>> shaders(n_views);
+    std::vector<counting_base *> counters(n_views, nullptr);
     std::vector<std::unique_ptr<swegl::viewport_t>> vps;
     swegl::post_shader_t post_null;
     for (int i = 0; i < n_views; i++) {
         surfaces[i] = SDL_Surface{targets[i].width, targets[i].height, targets[i].pitch, targets[i].pixels,
                                   &formats[i]};
         switch (shader_kind) {
-        case 0: shaders[i] = std::make_shared<counting_full_shader>(); break;
+        case 0:
+            shaders[i] = shader_for_mode(views[i].shader, &counters[i]);
+            if (!shaders[i])
+                return -1;
+            break;
         case 1: shaders[i] = std::make_shared<id_shader>(); break;
         case 2: shaders[i] = std::make_shared<progress_shader>(); break;
         case 3: shaders[i] = std::make_shared<swegl::pixel_shader_lights_phong>(); break;
@@ -187,7 +234,7 @@ __attribute__((visibility("default"))) int ref_render(const sgl_scene_desc *desc
             std::memcpy(targets[i].zbuffer, vps[i]->zbuffer(), sizeof(float) * (size_t)views[i].w * views[i].h);
         if (triangle_calls) {
             if (shader_kind == 0)
-                triangle_calls[i] = static_cast<counting_full_shader *>(shaders[i].get())->calls;
+                triangle_calls[i] = counters[i]->calls;
             else if (shader_kind == 1)
                 triangle_calls[i] = (uint64_t) static_cast<id_shader *>(shaders[i].get())->calls;
             else

@@ -278,12 +278,18 @@ typedef struct {
     uint32_t default_bitmap;
     int tw, th;
     int shininess;
+    /* pixel_shader_t::color (pixel_shaders.hpp:20), pixel_shader_lights_flat::light */
+    uint32_t color;
+    int flat_light;
     /* scene / viewport inputs */
     const sgl_scene_desc *d;
     v3 campos;
     int kind;
+    int mode; /* SGL_SHADER_* of the view */
     int calls;
 } shader;
+
+static int mode_flat(int m) { return m == SGL_SHADER_FLAT_BILINEAR || m == SGL_SHADER_FLAT_NEAREST || m == SGL_SHADER_FLAT; }
 
 /* pixel_shader_texture_bilinear::prepare_for_primitive (pixel_shaders.cpp:284-302) */
 static void sh_prepare_primitive(shader *sh, const sgl_primitive_desc *p)
@@ -292,6 +298,7 @@ static void sh_prepare_primitive(shader *sh, const sgl_primitive_desc *p)
     const sgl_material_desc *m = (p->material >= 0 && p->material < d->n_materials) ? &d->materials[p->material]
                                                                                     : &d->default_material;
     sh->shininess = m->shininess;
+    sh->color = m->color; /* pixel_shader_t::prepare_for_primitive (pixel_shaders.cpp:14-31) */
     if (m->texture < 0 || m->texture >= d->n_textures) {
         sh->default_bitmap = m->color;
         sh->tex = &sh->default_bitmap;
@@ -302,6 +309,8 @@ static void sh_prepare_primitive(shader *sh, const sgl_primitive_desc *p)
         sh->th = d->textures[m->texture].height;
     }
 }
+
+static int sh_flat_light(const shader *sh, const tvert *a, const tvert *b, const tvert *c, int inverted);
 
 /* prepare_for_triangle of the phong and the bilinear shaders (pixel_shaders.cpp:88-105,304-318) */
 static void sh_prepare_triangle(shader *sh, const tvert *a, const tvert *b, const tvert *c, int inverted)
@@ -329,6 +338,8 @@ static void sh_prepare_triangle(shader *sh, const tvert *a, const tvert *b, cons
     sh->t2.x *= (float)sh->tw;
     sh->t2.y *= (float)sh->th;
     sh->side_long_t_dir = sub2(sh->t2, sh->t0);
+    if (sh->kind == 0 && mode_flat(sh->mode))
+        sh->flat_light = sh_flat_light(sh, a, b, c, inverted);
 }
 
 /* pixel_shaders.cpp:106-126 and 320-325 */
@@ -400,13 +411,11 @@ static void sh_prepare_scanline(shader *sh, float pl, float pr)
     }
 }
 
-/* pixel_shader_lights_phong::shade (src/render/pixel_shaders.cpp:159-205) */
-static int sh_phong(const shader *sh, float progress)
+/* The sun and point-light sum of the Phong and the flat light shaders
+ * (pixel_shaders.cpp:159-205 per pixel, :33-84 per triangle): both evaluate
+ * the same expressions at a point with a normal. */
+static float light_sum(const sgl_scene_desc *d, v3 center, v3 normal, v3 camvec, int shininess)
 {
-    const sgl_scene_desc *d = sh->d;
-    v3 center = add3(sh->v, mul3(sh->vdir, progress));
-    v3 normal = normalize3(add3(sh->n, mul3(sh->ndir, progress)));
-    v3 camvec = normalize3(sub3(sh->campos, center));
     v3 sun = mk3(d->sun_direction[0], d->sun_direction[1], d->sun_direction[2]);
     float face_sun = -dot3(normal, sun);
     if (face_sun < 0.0f)
@@ -429,14 +438,40 @@ static int sh_phong(const shader *sh, float progress)
         v3 reflection = add3(ld, mul3(normal, alignment * 2));
         float specular = dot3(reflection, camvec);
         if (specular > 0) {
-            specular = (float)pow((double)specular, (double)sh->shininess);
-            specular = specular * (float)sh->shininess / 2;
+            specular = (float)pow((double)specular, (double)shininess);
+            specular = specular * (float)shininess / 2;
             dyn += diffuse + specular / d2;
         } else {
             dyn += diffuse;
         }
     }
-    return f2i(65536 * (d->ambient + face_sun + dyn));
+    return d->ambient + face_sun + dyn;
+}
+
+/* pixel_shader_lights_phong::shade (src/render/pixel_shaders.cpp:159-205) */
+static int sh_phong(const shader *sh, float progress)
+{
+    v3 center = add3(sh->v, mul3(sh->vdir, progress));
+    v3 normal = normalize3(add3(sh->n, mul3(sh->ndir, progress)));
+    v3 camvec = normalize3(sub3(sh->campos, center));
+    return f2i(65536 * light_sum(sh->d, center, normal, camvec, sh->shininess));
+}
+
+/* pixel_shader_lights_flat::prepare_for_triangle (pixel_shaders.cpp:33-84):
+ * the face normal (cross() normalises; the unary minus of a normal_t builds a
+ * normal_t, normalised again), the centroid (v0 + v1 + v2) / 3 and the same
+ * light sum; shade() returns light * 65536 converted to int. */
+static int sh_flat_light(const shader *sh, const tvert *a, const tvert *b, const tvert *c, int inverted)
+{
+    v3 normal = cross_n(sub3(b->world, a->world), sub3(c->world, a->world));
+    if (inverted)
+        normal = normalize3(neg3(normal));
+    v3 sum = add3(add3(a->world, b->world), c->world);
+    v3 center = mk3(sum.x / 3, sum.y / 3, sum.z / 3);
+    v3 camvec = normalize3(sub3(sh->campos, center));
+    float light = light_sum(sh->d, center, normal, camvec, sh->shininess);
+    light *= 65536;
+    return f2i(light);
 }
 
 static inline uint8_t u8_of(float f) { return (uint8_t)f2i(f); }
@@ -484,7 +519,20 @@ static uint32_t sh_bilinear(const shader *sh, float progress)
     return out;
 }
 
-/* pixel_shader_light_and_texture::shade (swegl/render/pixel_shaders.hpp:159-178) */
+/* pixel_shader_texture::shade (src/render/pixel_shaders.cpp:276-281): the
+ * texel at (int)t % size, the int converted to unsigned by the unsigned
+ * texture width and height. */
+static uint32_t sh_nearest(const shader *sh, float progress)
+{
+    v2 t = add2(sh->t_left, mul2(sh->t_dir, progress));
+    const uint32_t tw = (uint32_t)sh->tw, th = (uint32_t)sh->th;
+    const uint32_t u = (uint32_t)f2i(t.x) % tw;
+    const uint32_t v = (uint32_t)f2i(t.y) % th;
+    return sh->tex[v * tw + u];
+}
+
+/* The view's pixel shader; the combinations are
+ * pixel_shader_light_and_texture::shade (swegl/render/pixel_shaders.hpp:159-178). */
 static uint32_t sh_shade(shader *sh, float progress, int ordinal)
 {
     switch (sh->kind) {
@@ -494,8 +542,18 @@ static uint32_t sh_shade(shader *sh, float progress, int ordinal)
     case 4: return sh_bilinear(sh, progress);
     default: break;
     }
-    uint32_t color = sh_bilinear(sh, progress);
-    float light = (float)((double)sh_phong(sh, progress) / 65536.0);
+    switch (sh->mode) {
+    case SGL_SHADER_COLOR: return sh->color;
+    case SGL_SHADER_BILINEAR: return sh_bilinear(sh, progress);
+    case SGL_SHADER_NEAREST: return sh_nearest(sh, progress);
+    case SGL_SHADER_PHONG: return (uint32_t)sh_phong(sh, progress);
+    case SGL_SHADER_FLAT: return (uint32_t)sh->flat_light;
+    default: break;
+    }
+    const int nearest = sh->mode == SGL_SHADER_PHONG_NEAREST || sh->mode == SGL_SHADER_FLAT_NEAREST;
+    uint32_t color = nearest ? sh_nearest(sh, progress) : sh_bilinear(sh, progress);
+    const int li = mode_flat(sh->mode) ? sh->flat_light : sh_phong(sh, progress);
+    float light = (float)((double)li / 65536.0);
     uint8_t ch[4];
     memcpy(ch, &color, 4);
     if (light < 1) {
@@ -789,6 +847,7 @@ static int render_view(const oscene *s, const sgl_view *view, const sgl_target *
     r.sh.d = d;
     r.sh.campos = mk3(view->camera_pos[0], view->camera_pos[1], view->camera_pos[2]);
     r.sh.kind = kind;
+    r.sh.mode = view->shader;
 
     int q0 = 0;
     for (int n = 0; n < d->n_nodes; n++) {

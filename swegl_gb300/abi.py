@@ -60,9 +60,13 @@ class DofDesc(C.Structure):
                 ("max_radius", C.c_float), ("px_scale", C.c_float)]
 
 
+SHADERS = ("phong_bilinear", "phong_nearest", "flat_bilinear", "flat_nearest", "color", "bilinear", "nearest",
+           "phong", "flat")  # SGL_SHADER_* in order
+
+
 class ViewDesc(C.Structure):
     _fields_ = [("x", C.c_int), ("y", C.c_int), ("w", C.c_int), ("h", C.c_int),
-                ("view", F16), ("proj", F16), ("camera_pos", F3), ("dof", DofDesc)]
+                ("view", F16), ("proj", F16), ("camera_pos", F3), ("dof", DofDesc), ("shader", C.c_int)]
 
 
 class Target(C.Structure):
@@ -170,6 +174,7 @@ def view_desc(v) -> ViewDesc:
     d.camera_pos[:] = [float(x) for x in np.asarray(v.camera_pos, np.float32)]
     d.dof = DofDesc(1 if v.dof else 0, float(v.dof_focus), float(v.dof_aperture), float(v.dof_max_radius),
                     float(v.dof_px_scale))
+    d.shader = int(getattr(v, "shader", 0))
     return d
 
 

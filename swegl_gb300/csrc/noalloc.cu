@@ -213,7 +213,8 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     CUDA_TRY(cudaMemsetAsync(base + o_item_counters, 0, 2 * sizeof(unsigned long long), st));
     CUDA_TRY(cudaMemsetAsync(base + o_key, 0xFF, 8 * px, st)); // kEmptyKey
 
-    CUDA_TRY(launch_batch((const BatchDev *)(base + o_batch), tile, dof, st, nullptr, nullptr));
+    const int seq = (dof ? kSeqDof : 0) | (v.shader != SGL_SHADER_PHONG_BILINEAR ? kSeqShaders : 0);
+    CUDA_TRY(launch_batch((const BatchDev *)(base + o_batch), tile, seq, st, nullptr, nullptr));
     return SGL_OK;
 }
 

@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) k_vertex(const BatchDev *b)
             p.y = p.y / fabsf(p.z);
         }
         ndc[l] = make_float4(p.x, p.y, p.z, 0.0f);
-        yes[l] = 0;
+        yes[l] = below_near(p.z) ? kYesBehind : 0; // kYesDrawn is set by k_flags
     }
 }
 
@@ -197,9 +197,9 @@ __global__ void __launch_bounds__(256) k_flags(const BatchDev *b)
         const int m = prims[tri.w].material;
         const int ds = (m >= 0 && m < n_mats) ? mats[m].double_sided : 0;
         if (ds || cross_n_z(sub3(c1, a), sub3(c2, a)) > 0.0f) {
-            yes[tri.x] = 1;
-            yes[tri.y] = 1;
-            yes[tri.z] = 1;
+            yes[tri.x] = kYesDrawn | (below_near(a.z) ? kYesBehind : 0);
+            yes[tri.y] = kYesDrawn | (below_near(c1.z) ? kYesBehind : 0);
+            yes[tri.z] = kYesDrawn | (below_near(c2.z) ? kYesBehind : 0);
         }
     }
 }
@@ -222,7 +222,6 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
     int item = -1;
     uint32_t lo = 0, hi = 0;
     const uint4 *tris = nullptr;
-    const float4 *ndc = nullptr;
     const uint8_t *yes = nullptr;
     const uint32_t total = b->total_tri;
     // every thread of the block runs the same number of iterations (barriers inside)
@@ -241,15 +240,14 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
                 hi = __ldg(b->tri_base + item + 1);
                 const ItemDev &it = b->items[item];
                 tris = it.s.tris;
-                ndc = it.ndc;
                 yes = it.yes;
             }
             t = g - lo;
             const uint4 tri = tris[t];
-            if (yes[tri.x] && yes[tri.y] && yes[tri.z]) {
+            const uint32_t ya = yes[tri.x], yb = yes[tri.y], yc = yes[tri.z];
+            if (ya & yb & yc & kYesDrawn) {
                 // fill_triangle's cases (renderer.cpp:281-318): the smallest z' decides
-                const float za = ndc[tri.x].z, zb = ndc[tri.y].z, zc = ndc[tri.z].z;
-                list = (below_near(za) || below_near(zb) || below_near(zc)) ? 1 : 0;
+                list = ((ya | yb | yc) & kYesBehind) ? 1 : 0;
             }
         }
         uint32_t pos = 0;
@@ -1337,6 +1335,7 @@ __device__ __forceinline__ void bind_material(const SceneDev &s, uint32_t prim, 
 
 // prepare_for_upper/lower_triangle, prepare_for_scanline and shade for the
 // winner's progress values (renderer.cpp:433-493)
+template <bool ALL_MODES = true>
 __device__ __forceinline__ uint32_t shade_winner(Shader &sh, const LightsDev &L, const ViewDev &v, float4 rec)
 {
     const uint32_t bits = __float_as_uint(rec.w);
@@ -1346,7 +1345,7 @@ __device__ __forceinline__ uint32_t shade_winner(Shader &sh, const LightsDev &L,
     else
         sh_prepare_upper(sh, llr);
     sh_prepare_scanline(sh, rec.y, rec.z);
-    return sh_shade(sh, L, v, rec.x);
+    return sh_shade<ALL_MODES>(sh, L, v, rec.x);
 }
 
 // A winner of a near-clipped triangle: the clip vertices are rebuilt exactly
@@ -1369,6 +1368,9 @@ __device__ __noinline__ uint32_t shade_clip_px(const ItemDev &it, uint32_t i, ui
         const V2 su[3] = {p0->uv, p1->uv, p2->uv};
         bind_material(it.s, it.s.tris[slot >> 1].w, sh);
         sh_prepare_triangle(sh, sw, sn, su, !ffv);
+        if (it.v.shader == SGL_SHADER_FLAT_BILINEAR || it.v.shader == SGL_SHADER_FLAT_NEAREST ||
+            it.v.shader == SGL_SHADER_FLAT)
+            sh.flat_light = flat_light(sw, !ffv, *it.s.lights, it.v, sh.shininess);
         done = true;
     };
     clip_triangle(it, slot >> 1, emit);
@@ -1413,8 +1415,9 @@ __device__ __forceinline__ bool rec_replay(const TriRec *rp, const ViewDev &v, i
 }
 
 // The colour of one winning fragment: pixel i of item `item`, won by `slot`.
-__device__ __forceinline__ uint32_t shade_winner_px(const BatchDev *b, uint32_t item, uint32_t i, uint32_t slot,
-                                                   bool overflow)
+template <bool ALL_MODES>
+__device__ __forceinline__ uint32_t shade_winner_impl(const BatchDev *b, uint32_t item, uint32_t i, uint32_t slot,
+                                                     bool overflow)
 {
     const ItemDev &it = b->items[item];
     const ViewDev &v = it.v;
@@ -1438,8 +1441,13 @@ __device__ __forceinline__ uint32_t shade_winner_px(const BatchDev *b, uint32_t 
     const V3 sn[3] = {mk3(n0.x, n0.y, n0.z), mk3(n1.x, n1.y, n1.z), mk3(n2.x, n2.y, n2.z)};
     const V2 su[3] = {mk2(u0.x, u0.y), mk2(u1.x, u1.y), mk2(u2.x, u2.y)};
     sh_prepare_triangle(sh, sw, sn, su, (flags & kRecFFV) == 0u);
-    return shade_winner(sh, *it.s.lights, v, rec);
+    if (ALL_MODES &&
+        (v.shader == SGL_SHADER_FLAT_BILINEAR || v.shader == SGL_SHADER_FLAT_NEAREST || v.shader == SGL_SHADER_FLAT))
+        sh.flat_light = flat_light(sw, (flags & kRecFFV) == 0u, *it.s.lights, v, sh.shininess);
+    return shade_winner<ALL_MODES>(sh, *it.s.lights, v, rec);
 }
+
+
 
 // Per pixel: the background of viewport_t::clear (viewport.cpp:88-113) or the
 // colour of the winning fragment, and its depth.  A block takes TILE x TILE
@@ -1450,7 +1458,7 @@ constexpr int kShadeThreads = 256;
 #ifndef SGL_SHADE_MIN_BLOCKS
 #define SGL_SHADE_MIN_BLOCKS 4 // resident blocks per SM the shade is compiled for
 #endif
-template <int TILE>
+template <int TILE, bool ALL_MODES>
 __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(const BatchDev *b)
 {
     __shared__ uint4 queue[2 * kShadeThreads];
@@ -1521,7 +1529,7 @@ __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(c
                 const uint4 e = queue[threadIdx.x];
                 const ItemDev &ie = b->items[e.y];
                 const ViewDev &ve = ie.v;
-                const uint32_t c = shade_winner_px(b, e.y, e.x, e.z, overflow);
+                const uint32_t c = shade_winner_impl<ALL_MODES>(b, e.y, e.x, e.z, overflow);
                 const int yy = (int)(e.x / (uint32_t)ve.w), xx = (int)(e.x - (uint32_t)yy * (uint32_t)ve.w);
                 ie.pixels[(long long)yy * ie.pitch_px + xx] = c;
                 __syncthreads();
@@ -1537,7 +1545,7 @@ __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(c
     if ((int)threadIdx.x < qn) {
         const uint4 e = queue[threadIdx.x];
         const ItemDev &ie = b->items[e.y];
-        const uint32_t c = shade_winner_px(b, e.y, e.x, e.z, overflow);
+        const uint32_t c = shade_winner_impl<ALL_MODES>(b, e.y, e.x, e.z, overflow);
         const int yy = (int)(e.x / (uint32_t)ie.v.w), xx = (int)(e.x - (uint32_t)yy * (uint32_t)ie.v.w);
         ie.pixels[(long long)yy * ie.pitch_px + xx] = c;
     }
@@ -1729,7 +1737,7 @@ cudaError_t launch_dof(const BatchDev *b, cudaStream_t st)
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t st, int *launches, Profiler *prof)
+cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st, int *launches, Profiler *prof)
 {
     const bool timed = prof && prof->enabled;
     if (timed) {
@@ -1766,15 +1774,27 @@ cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t
     k_winners<<<sms * 4, 256, 0, st>>>(b);
     n++;
     mark(PK_SHADE);
-    if (tile == 8)
-        k_shade<8><<<sms * SGL_SHADE_MIN_BLOCKS, kShadeThreads, 0, st>>>(b);
-    else if (tile == 32)
-        k_shade<32><<<sms * SGL_SHADE_MIN_BLOCKS, kShadeThreads, 0, st>>>(b);
-    else
-        k_shade<16><<<sms * SGL_SHADE_MIN_BLOCKS, kShadeThreads, 0, st>>>(b);
+    // the kernel with every pixel shader only when a view asks for another
+    // than the default, which then keeps all the registers
+    const unsigned sg = sms * SGL_SHADE_MIN_BLOCKS;
+    if (flags & kSeqShaders) {
+        if (tile == 8)
+            k_shade<8, true><<<sg, kShadeThreads, 0, st>>>(b);
+        else if (tile == 32)
+            k_shade<32, true><<<sg, kShadeThreads, 0, st>>>(b);
+        else
+            k_shade<16, true><<<sg, kShadeThreads, 0, st>>>(b);
+    } else {
+        if (tile == 8)
+            k_shade<8, false><<<sg, kShadeThreads, 0, st>>>(b);
+        else if (tile == 32)
+            k_shade<32, false><<<sg, kShadeThreads, 0, st>>>(b);
+        else
+            k_shade<16, false><<<sg, kShadeThreads, 0, st>>>(b);
+    }
     n++;
     mark(PK_DOF);
-    if (any_dof) {
+    if (flags & kSeqDof) {
         k_dof<<<sms * 8, 256, 0, st>>>(b);
         n++;
     }

@@ -28,6 +28,7 @@ ViewDev make_view(const sgl_view &v)
     d.campos[0] = v.camera_pos[0];
     d.campos[1] = v.camera_pos[1];
     d.campos[2] = v.camera_pos[2];
+    d.shader = v.shader;
     // viewport_t constructor (src/render/viewport.cpp:94-97): x+w/2.0f, w/2.0f, -h/2.0f
     d.vm00 = (float)v.w / 2.0f;
     d.vm03 = (float)v.x + (float)v.w / 2.0f;
@@ -38,6 +39,10 @@ ViewDev make_view(const sgl_view &v)
 
 sgl_status check_view(Ctx *ctx, const sgl_view &v, const sgl_target &t)
 {
+    if (v.shader < 0 || v.shader >= SGL_SHADER_COUNT) {
+        ctx->fail("unknown pixel shader %d", v.shader);
+        return SGL_ERR_INVALID;
+    }
     if (v.w <= 0 || v.h <= 0 || v.x < 0 || v.y < 0 || (int64_t)v.w * v.h > (1ll << 28)) {
         ctx->fail("bad viewport %d,%d %dx%d", v.x, v.y, v.w, v.h);
         return SGL_ERR_INVALID;

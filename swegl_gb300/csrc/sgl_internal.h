@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "sgl.h"
+
 namespace sgl {
 
 constexpr int kMaxPointLights = 16;
@@ -63,6 +65,7 @@ struct ViewDev {
     float proj[12];               // rows 0-2 of camera_t::m_projectionmatrix
     float campos[3];
     float vm00, vm03, vm11, vm13; // viewport_t::m_viewportmatrix (viewport.cpp:94-99)
+    int shader;                   // SGL_SHADER_* (include/sgl.h)
 };
 
 // One view of a batch: its scene, camera and buffers.
@@ -70,7 +73,7 @@ struct ItemDev {
     SceneDev s;
     ViewDev v;
     float4 *ndc;             // per vertex: v_viewport before the viewport transform
-    uint8_t *yes;            // per vertex visibility flag (mesh_vertex_t::yes)
+    uint8_t *yes;            // per vertex: kYesDrawn (mesh_vertex_t::yes) | kYesBehind (z' below the near plane)
     unsigned long long *key; // per view pixel: (depth bits << 32) | draw slot
     float4 *prec;            // per view pixel: recorded winner (progress, progL, progR, bits)
     uint32_t *pixels;        // surface (device), BGRA8, at the viewport's top-left pixel
@@ -87,6 +90,9 @@ struct ItemDev {
     int dof_halo;    // tap reach in pixels (ceil of max_radius, <= kDofMaxHalo), -1: gather from memory
     int dof_tiles_x; // kDofTile tiles across the view
 };
+
+constexpr uint8_t kYesDrawn = 1;  // a visible triangle flagged the vertex (renderer.cpp:86-185)
+constexpr uint8_t kYesBehind = 2; // its z' is below the near plane (fill_triangle's clip test)
 
 // Depth-of-field tiles: kDofTile x kDofTile pixels with a halo of up to
 // kDofMaxHalo pixels staged in shared memory.
@@ -203,9 +209,12 @@ void prof_flush(Profiler *p);
 // kernel launchers (raster.cu)
 cudaError_t launch_world(const SceneDev &s, cudaStream_t st);
 // The launch sequence of a batch whose BatchDev lives at `b` (device memory).
-// `any_dof` adds the depth-of-field gather.  The depth keys must hold
+// `flags`: kSeqDof adds the depth-of-field gather, kSeqShaders shades with
+// every pixel shader (a view asks for another than the default).  The depth
+// keys must hold
 // kEmptyKey on entry; the shade kernel leaves them so (unless keep_keys).
-cudaError_t launch_batch(const BatchDev *b, int tile, bool any_dof, cudaStream_t st, int *launches, Profiler *prof);
+constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqVariants = 4;
+cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st, int *launches, Profiler *prof);
 // The depth-of-field gather alone (items prepared by the caller).
 cudaError_t launch_dof(const BatchDev *b, cudaStream_t st);
 // Upload the constant tables (depth-of-field taps) to the current device.

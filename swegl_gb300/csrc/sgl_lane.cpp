@@ -166,7 +166,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         if (dofz_px)
             CUDA_TRY(dofz.ensure(4 * dofz_px));
     }
-    bool any_dof = false;
+    int seq_flags = 0;
     ItemDev *hi = (ItemDev *)sl.h_items.ptr;
     for (int i = 0; i < n; i++) {
         const BatchEntry &en = e[i];
@@ -185,7 +185,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         if (en.view.dof.enabled) {
             // the shade kernel fills a scratch colour buffer; the gather writes the target
             const sgl_dof_desc &d = en.view.dof;
-            any_dof = true;
+            seq_flags |= kSeqDof;
             it.dof = 1;
             it.dof_out = en.rect_pixels;
             it.dof_pitch = en.pitch_px;
@@ -202,6 +202,8 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
             it.dof_halo = dof_halo_of(d.max_radius);
             it.dof_tiles_x = (en.view.w + kDofTile - 1) / kDofTile;
         }
+        if (en.view.shader != SGL_SHADER_PHONG_BILINEAR)
+            seq_flags |= kSeqShaders;
         hi[i] = it;
     }
     BatchDev *hbd = (BatchDev *)sl.h_batch.ptr;
@@ -243,7 +245,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     CUDA_TRY(cudaEventRecord(sl.staged, stream));
     sl.used = true;
     sl.n_items = n;
-    sl.any_dof = any_dof;
+    sl.seq_flags = seq_flags;
     *slot_out = si;
     return SGL_OK;
 }
@@ -256,7 +258,7 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
     const BatchDev *db = (const BatchDev *)sl.d_batch.ptr;
     keys_dirty = true; // until the sequence is enqueued: its shade kernel empties the keys
     if (use_graph) {
-        cudaGraphExec_t &g = sl.graph[tile_index(tile)][sl.any_dof ? 1 : 0];
+        cudaGraphExec_t &g = sl.graph[tile_index(tile)][sl.seq_flags];
         if (!g) {
             // captured on a private stream (the caller's may be the legacy
             // default stream, which cannot be captured), launched on the caller's
@@ -265,8 +267,8 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
             cudaGraph_t graph = nullptr;
             CUDA_TRY(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal));
             int kernels = 0;
-            cudaError_t le = launch_batch(db, tile, sl.any_dof, capture_stream, &kernels, nullptr);
-            sl.graph_kernels[tile_index(tile)][sl.any_dof ? 1 : 0] = kernels;
+            cudaError_t le = launch_batch(db, tile, sl.seq_flags, capture_stream, &kernels, nullptr);
+            sl.graph_kernels[tile_index(tile)][sl.seq_flags] = kernels;
             cudaError_t ce = cudaStreamEndCapture(capture_stream, &graph);
             CUDA_TRY(le);
             CUDA_TRY(ce);
@@ -276,9 +278,9 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
         }
         CUDA_TRY(cudaGraphLaunch(g, stream));
         if (launches)
-            *launches += sl.graph_kernels[tile_index(tile)][sl.any_dof ? 1 : 0];
+            *launches += sl.graph_kernels[tile_index(tile)][sl.seq_flags];
     } else {
-        CUDA_TRY(launch_batch(db, tile, sl.any_dof, stream, launches, prof));
+        CUDA_TRY(launch_batch(db, tile, sl.seq_flags, stream, launches, prof));
     }
     keys_dirty = sl.keep_keys;
     unsigned long long *hc = (unsigned long long *)sl.h_counters.ptr; // per-item counters only

@@ -96,10 +96,10 @@ struct Lane {
         cudaEvent_t staged = nullptr; // staging copies of this slot done
         cudaEvent_t done = nullptr;   // launch sequence of this slot done
         bool used = false;
-        cudaGraphExec_t graph[3][2] = {}; // per tile 8/16/32, without / with depth of field
-        int graph_kernels[3][2] = {};     // kernels in each graph
+        cudaGraphExec_t graph[3][kSeqVariants] = {}; // per tile 8/16/32 and sequence flags (kSeq*)
+        int graph_kernels[3][kSeqVariants] = {};     // kernels in each graph
         int n_items = 0;
-        bool any_dof = false;
+        int seq_flags = 0;
         bool keep_keys = false;
     } slots[kSlots];
     int next = 0;

@@ -1,8 +1,10 @@
-// sgl_shade.cuh — the pixel shader of the swegl render path on the device:
-// pixel_shader_light_and_texture<pixel_shader_lights_phong,
-// pixel_shader_texture_bilinear> (swegl/render/pixel_shaders.hpp:121-179,
-// src/render/pixel_shaders.cpp:88-205,284-384), with the reference's
-// single-precision operation order.
+// sgl_shade.cuh — the pixel shaders of the swegl render path on the device:
+// pixel_shader_lights_phong, pixel_shader_lights_flat, pixel_shader_texture
+// (nearest), pixel_shader_texture_bilinear, the material colour of
+// pixel_shader_t, and their pixel_shader_light_and_texture<L, T>
+// combinations (swegl/render/pixel_shaders.hpp:15-179,
+// src/render/pixel_shaders.cpp:14-384), with the reference's single-precision
+// operation order.
 #pragma once
 
 #include "sgl_device.cuh"
@@ -21,6 +23,7 @@ struct Shader {
     const uint32_t *tex;
     uint32_t color;
     int tw, th, shininess;
+    int flat_light; // pixel_shader_lights_flat::light as shade() returns it
 };
 
 // pixel_shader_*::prepare_for_triangle (src/render/pixel_shaders.cpp:88-105,304-318)
@@ -105,12 +108,11 @@ __device__ __forceinline__ void sh_prepare_scanline(Shader &sh, float pl, float 
     }
 }
 
-// pixel_shader_lights_phong::shade (src/render/pixel_shaders.cpp:159-205)
-__device__ __forceinline__ int sh_phong(const Shader &sh, const LightsDev &L, const ViewDev &v, float progress)
+// The sun and point-light sum of the Phong and the flat light shaders
+// (src/render/pixel_shaders.cpp:159-205 per pixel, :33-84 per triangle): the
+// same expressions at a point with a normal.
+__device__ __forceinline__ float light_sum(const LightsDev &L, V3 center, V3 normal, V3 camvec, int shininess)
 {
-    const V3 center = add3(sh.v, mul3(sh.vdir, progress));
-    const V3 normal = normalize3(add3(sh.n, mul3(sh.ndir, progress)));
-    const V3 camvec = normalize3(sub3(mk3(v.campos[0], v.campos[1], v.campos[2]), center));
     float face_sun = -dot3(normal, mk3(L.sun[0], L.sun[1], L.sun[2]));
     if (face_sun < 0.0f)
         face_sun = 0.0f;
@@ -132,14 +134,54 @@ __device__ __forceinline__ int sh_phong(const Shader &sh, const LightsDev &L, co
         const V3 reflection = add3(ld, mul3(normal, alignment * 2.0f));
         float specular = dot3(reflection, camvec);
         if (specular > 0.0f) {
-            specular = spec_pow(specular, sh.shininess);
-            specular = specular * (float)sh.shininess / 2.0f;
+            specular = spec_pow(specular, shininess);
+            specular = specular * (float)shininess / 2.0f;
             dyn = dyn + (diffuse + specular / d2);
         } else {
             dyn = dyn + diffuse;
         }
     }
-    return f2i(65536.0f * (L.ambient + face_sun + dyn));
+    return L.ambient + face_sun + dyn;
+}
+
+// pixel_shader_lights_phong::shade (src/render/pixel_shaders.cpp:159-205)
+__device__ __forceinline__ int sh_phong(const Shader &sh, const LightsDev &L, const ViewDev &v, float progress)
+{
+    const V3 center = add3(sh.v, mul3(sh.vdir, progress));
+    const V3 normal = normalize3(add3(sh.n, mul3(sh.ndir, progress)));
+    const V3 camvec = normalize3(sub3(mk3(v.campos[0], v.campos[1], v.campos[2]), center));
+    return f2i(65536.0f * light_sum(L, center, normal, camvec, sh.shininess));
+}
+
+// pixel_shader_lights_flat::prepare_for_triangle (src/render/pixel_shaders.cpp:
+// 33-84) on fill_triangle_2's vertex order: the face normal (cross()
+// normalises; the unary minus of a normal_t builds a normal_t, normalised
+// again), the centroid (v0 + v1 + v2) / 3 and the same light sum; shade()
+// returns light * 65536 converted to int.
+__device__ __forceinline__ int flat_light(const V3 w[3], bool inverted, const LightsDev &L, const ViewDev &v,
+                                          int shininess)
+{
+    V3 normal = cross_n(sub3(w[1], w[0]), sub3(w[2], w[0]));
+    if (inverted)
+        normal = normalize3(neg3(normal));
+    const V3 sum = add3(add3(w[0], w[1]), w[2]);
+    const V3 center = mk3(sum.x / 3.0f, sum.y / 3.0f, sum.z / 3.0f);
+    const V3 camvec = normalize3(sub3(mk3(v.campos[0], v.campos[1], v.campos[2]), center));
+    float light = light_sum(L, center, normal, camvec, shininess);
+    light = light * 65536.0f;
+    return f2i(light);
+}
+
+// pixel_shader_texture::shade (src/render/pixel_shaders.cpp:276-281): the
+// texel at (int)t % size, the int converted to unsigned by the unsigned width
+// and height.
+__device__ __forceinline__ uint32_t sh_nearest(const Shader &sh, float progress)
+{
+    const V2 t = add2(sh.t_left, mul2(sh.t_dir, progress));
+    const uint32_t tw = (uint32_t)sh.tw, th = (uint32_t)sh.th;
+    const uint32_t u = (uint32_t)f2i(t.x) % tw;
+    const uint32_t vv = (uint32_t)f2i(t.y) % th;
+    return sh.tex ? __ldg(sh.tex + vv * tw + u) : sh.color; // untextured: 1x1 of the colour
 }
 
 // pixel_shader_texture_bilinear::shade (src/render/pixel_shaders.cpp:348-384)
@@ -193,12 +235,27 @@ __device__ __forceinline__ uint32_t sh_bilinear(const Shader &sh, float progress
     return out;
 }
 
-// pixel_shader_light_and_texture::shade (swegl/render/pixel_shaders.hpp:159-178)
+// The view's pixel shader (SGL_SHADER_*, include/sgl.h); the combinations are
+// pixel_shader_light_and_texture::shade (swegl/render/pixel_shaders.hpp:159-178).
+// ALL_MODES = false compiles the default Phong + bilinear shader alone.
+template <bool ALL_MODES = true>
 __device__ __forceinline__ uint32_t sh_shade(const Shader &sh, const LightsDev &L, const ViewDev &v, float progress)
 {
-    uint32_t color = sh_bilinear(sh, progress);
+    const int mode = ALL_MODES ? v.shader : SGL_SHADER_PHONG_BILINEAR;
+    if (mode >= SGL_SHADER_COLOR) {
+        switch (mode) {
+        case SGL_SHADER_COLOR: return sh.color;
+        case SGL_SHADER_BILINEAR: return sh_bilinear(sh, progress);
+        case SGL_SHADER_NEAREST: return sh_nearest(sh, progress);
+        case SGL_SHADER_PHONG: return (uint32_t)sh_phong(sh, L, v, progress);
+        default: return (uint32_t)sh.flat_light; // SGL_SHADER_FLAT
+        }
+    }
+    const bool nearest = mode == SGL_SHADER_PHONG_NEAREST || mode == SGL_SHADER_FLAT_NEAREST;
+    const bool flat = mode == SGL_SHADER_FLAT_BILINEAR || mode == SGL_SHADER_FLAT_NEAREST;
+    uint32_t color = nearest ? sh_nearest(sh, progress) : sh_bilinear(sh, progress);
     // (float)(i / 65536.0): the int rounded to float, then an exact power-of-two scale
-    float light = __int2float_rn(sh_phong(sh, L, v, progress)) * (1.0f / 65536.0f);
+    float light = __int2float_rn(flat ? sh.flat_light : sh_phong(sh, L, v, progress)) * (1.0f / 65536.0f);
     uint32_t out = color & 0xFF000000u;
     if (light < 1.0f) {
 #pragma unroll

@@ -215,6 +215,7 @@ class View:
     dof_aperture: float = 0.05
     dof_max_radius: float = 16.0
     dof_px_scale: float = 0.0
+    shader: int = 0  # SGL_SHADER_* (include/sgl.h)
 
 
 @dataclass

@@ -32,6 +32,26 @@ struct Reader {
         }
     }
 };
+// The swegl pixel shader of an SGL_SHADER_* mode, as an application builds it.
+std::shared_ptr<swegl::pixel_shader_t> make_shader(int mode)
+{
+    using namespace swegl;
+    switch (mode) {
+    case SGL_SHADER_PHONG_NEAREST:
+        return std::make_shared<pixel_shader_light_and_texture<pixel_shader_lights_phong, pixel_shader_texture>>();
+    case SGL_SHADER_FLAT_BILINEAR:
+        return std::make_shared<pixel_shader_light_and_texture<pixel_shader_lights_flat, pixel_shader_texture_bilinear>>();
+    case SGL_SHADER_FLAT_NEAREST:
+        return std::make_shared<pixel_shader_light_and_texture<pixel_shader_lights_flat, pixel_shader_texture>>();
+    case SGL_SHADER_COLOR: return std::make_shared<pixel_shader_t>();
+    case SGL_SHADER_BILINEAR: return std::make_shared<pixel_shader_texture_bilinear>();
+    case SGL_SHADER_NEAREST: return std::make_shared<pixel_shader_texture>();
+    case SGL_SHADER_PHONG: return std::make_shared<pixel_shader_lights_phong>();
+    case SGL_SHADER_FLAT: return std::make_shared<pixel_shader_lights_flat>();
+    default:
+        return std::make_shared<pixel_shader_light_and_texture<pixel_shader_lights_phong, pixel_shader_texture_bilinear>>();
+    }
+}
 } // namespace
 
 int main(int argc, char **argv)
@@ -117,8 +137,7 @@ int main(int argc, char **argv)
     std::vector<uint32_t> pixels((size_t)sw * sh, 0);
     SDL_PixelFormat fmt{4};
     SDL_Surface surface{sw, sh, 4 * sw, pixels.data(), &fmt};
-    std::shared_ptr<swegl::pixel_shader_t> shader = std::make_shared<
-        swegl::pixel_shader_light_and_texture<swegl::pixel_shader_lights_phong, swegl::pixel_shader_texture_bilinear>>();
+    std::vector<std::shared_ptr<swegl::pixel_shader_t>> shaders;
     std::vector<std::unique_ptr<swegl::viewport_t>> vps;
     swegl::post_shader_t post_null;
     for (int i = 0; i < n_views; i++) {
@@ -127,7 +146,8 @@ int main(int argc, char **argv)
         r.get(view, sizeof view);
         r.get(proj, sizeof proj);
         r.get(cam, sizeof cam);
-        auto vp = std::make_unique<swegl::viewport_t>(x, y, w, h, &surface, shader, 0);
+        shaders.push_back(make_shader(r.get<int>()));
+        auto vp = std::make_unique<swegl::viewport_t>(x, y, w, h, &surface, shaders.back(), 0);
         for (int k = 0; k < 16; k++) {
             vp->m_camera.m_viewmatrix[k / 4][k % 4] = view[k];
             vp->m_camera.m_projectionmatrix[k / 4][k % 4] = proj[k];

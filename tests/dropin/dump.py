@@ -45,5 +45,6 @@ def write_dump(path, scene, views, surface_wh):
         f32(np.asarray(v.view, np.float32).reshape(-1))
         f32(np.asarray(v.proj, np.float32).reshape(-1))
         f32(v.camera_pos)
+        i32(int(getattr(v, "shader", 0)))
     with open(path, "wb") as fh:
         fh.write(out)

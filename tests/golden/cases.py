@@ -12,6 +12,7 @@ import math
 
 import numpy as np
 
+from swegl_gb300 import abi
 from swegl_gb300 import scenes as S
 
 FULL = "full"      # per-pixel arrays stored
@@ -74,6 +75,24 @@ def cases() -> dict:
         for i, v in enumerate(vs):
             v.x, v.y = (i % 2) * 320, (i // 2) * 240
         return vs
+
+    # the other pixel shaders of the reference (SGL_SHADER_* 1..8), on the
+    # mixed scene (textures, untextured, fans / strips / lists, double sided)
+    # and on the cube
+    def shaded(view_fn, mode):
+        def views():
+            vs = view_fn()
+            for v in vs:
+                v.shader = mode
+            return vs
+        return views
+
+    for mode in range(1, 9):
+        name = abi.SHADERS[mode]
+        out[f"mixed_{name}_320x240"] = dict(scene="mixed", views=shaded(lambda: [_look((0.5, 0.8, 4.5), (0, 0, 0), 320, 240)], mode),
+                                           kinds=(0,), store=FULL)
+        out[f"cube_{name}_320x240"] = dict(scene="cube", views=shaded(lambda: [_look((0.3, 0.2, 1.2), (0, 0, 0), 320, 240)], mode),
+                                          kinds=(0,), store=FULL)
 
     out["shared_4x320x240"] = dict(scene="spheres200", views=shared_views, shared=(640, 480), kinds=(0, 1), store=FULL)
     out["spheres_1920x1080"] = dict(scene="spheres200", views=lambda: [S.spheres_view(1920, 1080)], kinds=(0, 1, 2),

@@ -49,6 +49,7 @@ def test_dropin_render_matches_oracle(tmp_path):
         m, c = S.look_at(pos, (0, 0, 0))
         v = S.view_for(320, 240, m, c)
         v.x = 320 * i
+        v.shader = (0, 3)[i]  # Phong + bilinear; flat light + nearest texture
         views.append(v)
     dump = os.path.join(str(tmp_path), "scene.bin")
     out = os.path.join(str(tmp_path), "out.bin")

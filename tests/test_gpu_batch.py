@@ -99,3 +99,33 @@ def test_graph_replay_and_autotune(rig):
     ref = oracle.render(sc, views2)
     for i in range(len(views2)):
         assert np.array_equal(got[i][1].view(np.uint32), ref.frames[i].zbuffer.view(np.uint32))
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_of_every_pixel_shader(rig, use_graph):
+    """One batch with a view per pixel shader (SGL_SHADER_*): the frames of the
+    default shader and of the other shaders come from different kernel
+    instantiations of the same sequence; each matches the oracle."""
+    r, torch = rig
+    sc = G.scene("mixed")
+    sid = r.upload(sc)
+    views = []
+    for mode in range(len(abi.SHADERS)):
+        m, c = S.look_at((0.5 + 0.2 * mode, 0.8, 4.5), (0, 0, 0))
+        v = S.view_for(160 + 8 * mode, 120, m, c)
+        v.shader = mode
+        views.append(v)
+    bufs, tgts = device_targets(torch, views)
+    r.render_batch([(sid, v, t) for v, t in zip(views, tgts)], use_graph=use_graph)
+    torch.cuda.synchronize()
+    for mode, ((pix, z), v) in enumerate(zip(frames_of(bufs), views)):
+        ref = oracle.render(sc, [v])
+        assert np.array_equal(z.view(np.uint32), ref.zbuffer.view(np.uint32)), abi.SHADERS[mode]
+        if mode in (7, 8):
+            # the light shaders write the int light value: compare it as an int
+            dl = np.abs(pix.astype(np.int64) - ref.pixels.astype(np.int64))
+            assert int(dl.max()) <= 2, (abi.SHADERS[mode], int(dl.max()))
+        else:
+            d = np.abs(pix.view(np.uint8).astype(np.int16) - ref.pixels.view(np.uint8).astype(np.int16))
+            assert int(d.max()) <= 2, (abi.SHADERS[mode], int(d.max()))
+    r.release(sid)
