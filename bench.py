@@ -27,6 +27,8 @@ torchrun (N > 1) every rank serves its own stream (replicas, no collective);
 value sums the frames of all ranks over the max-over-ranks time.
 
 --workload frame times the plain renderer alone on the 1080p frame.
+--workload layers times a 1080p frame with 4 transparency layers of the
+200-sphere scene whose textures carry block alpha (translucent spheres).
 --impl reference times the reference's CPU algorithm (the oracle's C
 restatement, oracle/sgl_oracle.c) on all host threads on the same requests.
 """
@@ -324,6 +326,111 @@ def cpu_frame_baseline(scene, view, args, gpu_frame=None) -> dict:
     if gpu_frame is not None:
         out["parity"] = parity_of([gpu_frame], first[:1])
     return out
+
+
+# ------------------------------------------------------ transparency layers --
+def layers_scene_view():
+    """The 200-sphere scene (819,200 triangles) with 8 block-alpha textures
+    (1024^2, 64-texel squares: 3/8 opaque, 1/8 clear, 1/2 translucent) and its
+    1080p camera with 4 transparency layers."""
+    from swegl_gb300 import scenes as S
+
+    texs = [S.texture_block_alpha(900 + t, 1024, 1024, 64) for t in range(8)]
+    scene = S.spheres_scene(textures=texs)
+    v = S.spheres_view(1920, 1080)
+    v.layers = 4
+    return scene, v
+
+
+def run_layers(args, rank, world, local_rank):
+    import torch
+
+    from swegl_gb300 import abi
+    from swegl_gb300.runtime import Renderer
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    r = Renderer(local_rank)
+    scene, v = layers_scene_view()
+    copies = [r.upload(scene) for _ in range(2)]  # ~270 MB in rotation, above L2
+    stream = torch.cuda.Stream()
+    bufs, tgt = device_target(torch, v.w, v.h)
+
+    def step(k):
+        r.render_device(copies[k % len(copies)], [v], [tgt], stream=stream.cuda_stream)
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    stats = r.render_device(copies[0], [v], [tgt], stream=stream.cuda_stream, stats=True)
+    gpu_frame = (bufs[0].cpu().numpy().view(np.uint32).copy(), bufs[1].cpu().numpy().copy())
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        for k in range(args.steps):
+            starts[k].record(stream)
+            step(k)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    frame_ms = max_over_ranks(torch, dist, sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps)
+    r.profile(True)
+    for k in range(args.steps):
+        step(k)
+    torch.cuda.synchronize()
+    prof = r.profile_read()
+    r.profile(False)
+    # end to end: host surface and depth buffer through sgl_render
+    host_pix = torch.zeros((v.h, v.w), dtype=torch.int32).pin_memory()
+    host_z = torch.zeros((v.h, v.w), dtype=torch.float32).pin_memory()
+    htgt = abi.Target()
+    htgt.pixels = host_pix.data_ptr()
+    htgt.pitch = 4 * v.w
+    htgt.width, htgt.height = v.w, v.h
+    htgt.zbuffer = C.cast(C.c_void_p(host_z.data_ptr()), C.POINTER(C.c_float))
+    vd = (abi.ViewDesc * 1)(abi.view_desc(v))
+    td = (abi.Target * 1)(htgt)
+    for k in range(args.warmup):
+        r.lib.sgl_render(r.ctx, copies[k % 2], vd, td, 1, 0, None, None)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        st = r.lib.sgl_render(r.ctx, copies[k % 2], vd, td, 1, 0, None, None)
+        if st != 0:
+            raise RuntimeError(f"sgl_render failed: {st}")
+    e2e_fps = args.steps / (time.perf_counter() - t0)
+    e2e = sum_over_ranks(torch, dist, e2e_fps) if dist else e2e_fps
+    fps = world * 1e3 / frame_ms
+    fm = {"frame_ms": frame_ms, "prof": prof, "alg_bytes": frame_alg_bytes(scene, v.w, v.h)}
+    out = {
+        "metric": "frames/s (1080p frame with 4 transparency layers)",
+        "value": round(fps, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(frame_ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic (seeded scene, swegl_gb300/scenes.py)",
+        "config": {"workload": "translucent_spheres200_1080p_4layers", "triangles": scene.n_triangles,
+                   "viewport": "1920x1080", "layers": v.layers,
+                   "l2": "inputs larger than L2: 2 resident scene copies in rotation"},
+        "fragments": int(stats["fragments"]),
+        "kernels": kernels_of(fm),
+        "dominant_kernel": max(prof.items(), key=lambda kv: kv[1]["total_ms"])[0] if prof else None,
+        "e2e": {"value": round(e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": 4 * v.w * v.h + C.sizeof(abi.ViewDesc),
+                "d2h_bytes_per_step": 8 * v.w * v.h},
+        "gpu_launches": int(stats["kernel_launches"]) * args.steps,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_frame_baseline(scene, v, args, gpu_frame)
+    for c in copies:
+        r.release(c)
+    r.close()
+    if dist:
+        dist.destroy_process_group()
+    return out if rank == 0 else None
 
 
 def serve_config(args) -> dict:
@@ -639,7 +746,7 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["serve", "frame"], default="serve")
+    ap.add_argument("--workload", choices=["serve", "frame", "layers"], default="serve")
     ap.add_argument("--requests-per-step", type=int, default=256)
     ap.add_argument("--seq-requests", type=int, default=512)
     ap.add_argument("--duration", type=float, default=10.0, help="open-loop latency run, seconds")
@@ -658,6 +765,8 @@ def main():
         out = run_reference(args, rank, world)
     elif args.workload == "frame":
         out = run_frame(args, rank, world, local_rank)
+    elif args.workload == "layers":
+        out = run_layers(args, rank, world, local_rank)
     else:
         out = run_serve(args, rank, world, local_rank)
     if out is not None:

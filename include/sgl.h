@@ -166,7 +166,11 @@ typedef struct sgl_view {
     float        camera_pos[3];     /* camera_t::m_center */
     sgl_dof_desc dof;
     int          shader;            /* SGL_SHADER_*; 0 = Phong + bilinear */
+    int          layers;            /* transparency layers (viewport_t's transparency_layer_count),
+                                       0 = opaque; 1..SGL_MAX_LAYERS, plain sgl_render only */
 } sgl_view;
+
+#define SGL_MAX_LAYERS 8
 
 /* The SDL_Surface fields the reference writes (pixels, pitch, w, h with
  * BytesPerPixel = 4) plus viewport_t::m_zbuffer (w*h floats of the view). */

@@ -17,9 +17,10 @@
 // reference does.  Differences, all explicit:
 //   * the reference's pixel shaders (pixel_shader_t, the flat and Phong light
 //     shaders, the nearest and bilinear texture shaders and their
-//     pixel_shader_light_and_texture<L, T> combinations) and opaque viewports
-//     (0 transparency layers) run on the GPU; layered viewports throw
-//     swegl::render_error (there is no CPU fallback);
+//     pixel_shader_light_and_texture<L, T> combinations) and viewports with
+//     0 to SGL_MAX_LAYERS transparency layers run on the GPU; more layers, or
+//     layers with the depth-of-field post shader, throw swegl::render_error
+//     (there is no CPU fallback);
 //   * the scene is not mutated (v_world, v_viewport, normal_world, yes and
 //     the temporary clip vertices of the reference are not written back);
 //   * errors throw swegl::render_error instead of undefined behaviour;
@@ -668,8 +669,6 @@ inline void render_one(int scene_id, viewport_t &vp)
 {
     if (!vp.m_pixel_shader)
         throw render_error(SGL_ERR_INVALID, "viewport without a pixel shader");
-    if (vp.m_got_transparency)
-        throw render_error(SGL_ERR_UNSUPPORTED, "the GPU path renders opaque viewports (0 transparency layers)");
     if (!vp.m_screen || !vp.m_screen->format || vp.m_screen->format->BytesPerPixel != 4)
         throw render_error(SGL_ERR_INVALID, "viewport surface must be 32-bit");
     sgl_view v{};
@@ -684,6 +683,7 @@ inline void render_one(int scene_id, viewport_t &vp)
     v.camera_pos[2] = vp.m_camera.m_center.z();
     v.dof = vp.m_post_shader ? vp.m_post_shader->dof() : sgl_dof_desc{0, 0, 0, 0, 0};
     v.shader = vp.m_pixel_shader->gpu_shader();
+    v.layers = vp.m_got_transparency ? vp.m_transparency_layer_count : 0;
     sgl_target t{vp.m_screen->pixels, vp.m_screen->pitch, vp.m_screen->w, vp.m_screen->h, vp.m_zbuffer.get()};
     check(sgl_render(context(), scene_id, &v, &t, 1, 0, nullptr, nullptr), "sgl_render");
 }

@@ -80,14 +80,17 @@ class Result:
 
 
 def render(scene, views, kind: int = KIND_FULL, which: str = "restatement", winner: bool = False,
-           shared_surface: tuple[int, int] | None = None) -> Result:
+           shared_surface: tuple[int, int] | None = None, background: np.ndarray | None = None) -> Result:
     """Render `views` in order (swegl::render(scene, vp0, vp1, ...)).
 
     Each view gets its own surface of the view's size unless `shared_surface`
-    = (width, height) asks for one surface shared by all views."""
+    = (width, height) asks for one surface shared by all views; `background`
+    (shared surfaces only) is the surface's content before the render."""
     holder = abi.SceneDescHolder(scene)
     if shared_surface:
         surf = abi.HostFrame(*shared_surface)
+        if background is not None:
+            surf.pixels[...] = background
         frames = []
         for v in views:
             f = abi.HostFrame(*shared_surface, zw=v.w, zh=v.h)

@@ -218,7 +218,8 @@ __attribute__((visibility("default"))) int ref_render(const sgl_scene_desc *desc
         default: return -1;
         }
         const sgl_view &v = views[i];
-        auto vp = std::make_unique<swegl::viewport_t>(v.x, v.y, v.w, v.h, &surfaces[i], shaders[i], 0);
+        auto vp = std::make_unique<swegl::viewport_t>(v.x, v.y, v.w, v.h, &surfaces[i], shaders[i],
+                                                      shader_kind == 0 ? v.layers : 0);
         vp->m_camera.m_viewmatrix = to_matrix(v.view);
         vp->m_camera.m_projectionmatrix = to_matrix(v.proj);
         vp->m_camera.m_center = swegl::vertex_t(v.camera_pos[0], v.camera_pos[1], v.camera_pos[2]);

@@ -582,7 +582,106 @@ typedef struct {
     uint64_t fragments;
     uint64_t drawn;
     uint64_t clip_one, clip_two; /* triangles through the near-clip branches */
+    /* transparency layers (viewport_t::m_transparency_layers): layer k of
+     * view pixel p at [k * w * h + p]; 0 = opaque view */
+    int n_layers;
+    float *lz;
+    uint32_t *lc;
 } raster;
+
+static const union { int32_t i; float f; } MAX_Z = {0x7F7F7F7F}; /* max_z, renderer.cpp:15-19 */
+
+/* blend (src/render/colors.cpp:39-57) on 0xAARRGGBB pixels */
+static uint32_t blend_px(uint32_t back, uint32_t front)
+{
+    const int alpha = (int)(front >> 24), balpha = (int)(back >> 24);
+    const int new_alpha = 255 - ((255 - alpha) * (255 - balpha) / 255);
+    if (alpha == 255)
+        return (front & 0x00FFFFFFu) | ((uint32_t)(uint8_t)new_alpha << 24);
+    if (alpha == 0)
+        return (back & 0x00FFFFFFu) | ((uint32_t)(uint8_t)new_alpha << 24);
+    uint32_t out = (uint32_t)(uint8_t)new_alpha << 24;
+    for (int c = 0; c < 3; c++) {
+        const int b = (int)((back >> (8 * c)) & 0xFF), f = (int)((front >> (8 * c)) & 0xFF);
+        out |= (uint32_t)(uint8_t)(b * ((256 - alpha) / 256.0) + f * (alpha / 256.0)) << (8 * c);
+    }
+    return out;
+}
+
+/* A fragment that passed the depth test of a view with transparency layers
+ * (renderer.cpp:500-550): an opaque colour is drawn and drops the layers
+ * behind it; a transparent one is inserted among the layers, in front of
+ * those farther away, pushing the others up (or, when every layer is used,
+ * down, losing the farthest). */
+static void layer_insert(raster *r, long off, uint32_t *video, float z, uint32_t color)
+{
+    const int n = r->n_layers;
+    const long px = (long)r->view->w * r->view->h;
+    float *lz = r->lz + off;
+    uint32_t *lc = r->lc + off;
+    int li;
+    for (li = 0; li < n; li++)
+        if (lz[li * px] == MAX_Z.f || lz[li * px] < z)
+            break;
+    if ((color >> 24) == 255) {
+        *video = color;
+        r->zb[off] = z;
+        int i, k;
+        for (i = 0, k = li; k < n; i++, k++) {
+            lz[i * px] = lz[k * px];
+            lc[i * px] = lc[k * px];
+        }
+        for (; i < n; i++) {
+            lz[i * px] = MAX_Z.f;
+            lc[i * px] = 0;
+        }
+    } else if (lz[(n - 1) * px] != MAX_Z.f) {
+        while (li-- > 0) {
+            const float tz = lz[li * px];
+            const uint32_t tc = lc[li * px];
+            lz[li * px] = z;
+            lc[li * px] = color;
+            z = tz;
+            color = tc;
+        }
+    } else {
+        for (; li < n; li++) {
+            const float tz = lz[li * px];
+            const uint32_t tc = lc[li * px];
+            lz[li * px] = z;
+            lc[li * px] = color;
+            z = tz;
+            color = tc;
+            if (z == MAX_Z.f)
+                break;
+        }
+    }
+}
+
+/* viewport_t::flatten (viewport.cpp:43-86), then post_shader_t::shade's copy
+ * of the first layer to the screen (post_shaders.hpp:22-47).  As in the
+ * reference, the screen pixels read and written are those of surface row j
+ * (flatten) and row j + y (copy), column i, for view pixel (i, j). */
+static void layers_resolve(raster *r)
+{
+    const sgl_view *v = r->view;
+    const long px = (long)v->w * v->h;
+    uint32_t *screen = (uint32_t *)r->target->pixels;
+    const int pitch_px = r->target->pitch / 4;
+    for (int k = 1; k < r->n_layers; k++)
+        for (long p = 0; p < px; p++)
+            if (r->lc[k * px + p] >> 24)
+                r->lc[p] = blend_px(r->lc[p], r->lc[k * px + p]);
+    for (int j = 0; j < v->h; j++)
+        for (int i = 0; i < v->w; i++) {
+            const uint32_t back = screen[(long)j * pitch_px + i];
+            uint32_t *f = &r->lc[(long)j * v->w + i];
+            *f = (*f >> 24) ? blend_px(back, *f) : back;
+        }
+    for (int j = 0; j < v->h; j++)
+        for (int i = 0; i < v->w; i++)
+            screen[(long)(j + v->y) * pitch_px + i] = r->lc[(long)j * v->w + i];
+}
 
 /* fill_half_triangle (src/render/renderer.cpp:462-558), opaque branch */
 static void fill_half(raster *r, int y, int y_end, line_side *L, line_side *R)
@@ -610,7 +709,12 @@ static void fill_half(raster *r, int y, int y_end, line_side *L, line_side *R)
                     continue;
                 if (z >= r->zb[zoff])
                     continue;
-                pixels[(long)y * pitch_px + x1] = sh_shade(&r->sh, q.alpha, r->sh.calls - 1);
+                const uint32_t color = sh_shade(&r->sh, q.alpha, r->sh.calls - 1);
+                if (r->n_layers) {
+                    layer_insert(r, zoff, &pixels[(long)y * pitch_px + x1], z, color);
+                    continue;
+                }
+                pixels[(long)y * pitch_px + x1] = color;
                 r->zb[zoff] = z;
                 if (r->winner_slot)
                     r->winner_slot[zoff] = r->slot;
@@ -848,6 +952,21 @@ static int render_view(const oscene *s, const sgl_view *view, const sgl_target *
     r.sh.campos = mk3(view->camera_pos[0], view->camera_pos[1], view->camera_pos[2]);
     r.sh.kind = kind;
     r.sh.mode = view->shader;
+    if (view->layers > 0 && kind == 0) {
+        const size_t lpx = (size_t)view->layers * view->w * view->h;
+        r.n_layers = view->layers;
+        r.lz = (float *)malloc(sizeof(float) * lpx);
+        r.lc = (uint32_t *)calloc(lpx, sizeof(uint32_t));
+        if (!r.lz || !r.lc) {
+            free(r.lz);
+            free(r.lc);
+            free(vpos);
+            free(yes);
+            free(zb);
+            return -1;
+        }
+        memset(r.lz, 0x7F, sizeof(float) * lpx); /* viewport_t::clear (viewport.cpp:107-112) */
+    }
 
     int q0 = 0;
     for (int n = 0; n < d->n_nodes; n++) {
@@ -908,6 +1027,11 @@ static int render_view(const oscene *s, const sgl_view *view, const sgl_target *
             }
         }
         q0 = q1;
+    }
+    if (r.n_layers) {
+        layers_resolve(&r);
+        free(r.lz);
+        free(r.lc);
     }
     if (target->zbuffer)
         memcpy(target->zbuffer, zb, sizeof(float) * (size_t)view->w * view->h);

@@ -66,7 +66,8 @@ SHADERS = ("phong_bilinear", "phong_nearest", "flat_bilinear", "flat_nearest", "
 
 class ViewDesc(C.Structure):
     _fields_ = [("x", C.c_int), ("y", C.c_int), ("w", C.c_int), ("h", C.c_int),
-                ("view", F16), ("proj", F16), ("camera_pos", F3), ("dof", DofDesc), ("shader", C.c_int)]
+                ("view", F16), ("proj", F16), ("camera_pos", F3), ("dof", DofDesc), ("shader", C.c_int),
+                ("layers", C.c_int)]
 
 
 class Target(C.Structure):
@@ -175,6 +176,7 @@ def view_desc(v) -> ViewDesc:
     d.dof = DofDesc(1 if v.dof else 0, float(v.dof_focus), float(v.dof_aperture), float(v.dof_max_radius),
                     float(v.dof_px_scale))
     d.shader = int(getattr(v, "shader", 0))
+    d.layers = int(getattr(v, "layers", 0))
     return d
 
 

@@ -85,6 +85,8 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
         return SGL_ERR_NOT_FOUND;
     }
     sgl_status r = check_view(ctx, *view, *target);
+    if (r == SGL_OK)
+        r = reject_layers(ctx, *view);
     if (r != SGL_OK)
         return r;
     if (cudaSetDevice(ctx->device) != cudaSuccess) {

@@ -1351,9 +1351,8 @@ __device__ __forceinline__ uint32_t shade_winner(Shader &sh, const LightsDev &L,
 // A winner of a near-clipped triangle: the clip vertices are rebuilt exactly
 // as fill_triangle makes them; the progress values were recorded by the
 // near-clip winner walk.  Rare, so kept out of line.
-__device__ __noinline__ uint32_t shade_clip_px(const ItemDev &it, uint32_t i, uint32_t slot)
+__device__ __noinline__ uint32_t shade_clip_rec(const ItemDev &it, uint32_t slot, float4 rec)
 {
-    const float4 rec = it.prec[i];
     Shader sh;
     bool done = false;
     auto emit = [&](uint32_t sl, const TV &a, const TV &c1, const TV &c2, bool ffv) {
@@ -1375,6 +1374,11 @@ __device__ __noinline__ uint32_t shade_clip_px(const ItemDev &it, uint32_t i, ui
     };
     clip_triangle(it, slot >> 1, emit);
     return done ? shade_winner(sh, *it.s.lights, it.v, rec) : 0u;
+}
+
+__device__ __forceinline__ uint32_t shade_clip_px(const ItemDev &it, uint32_t i, uint32_t slot)
+{
+    return shade_clip_rec(it, slot, it.prec[i]);
 }
 
 // The progress values of pixel (X, Y) (surface coordinates) from its winning
@@ -1414,6 +1418,9 @@ __device__ __forceinline__ bool rec_replay(const TriRec *rp, const ViewDev &v, i
     return true;
 }
 
+template <bool ALL_MODES>
+__device__ __forceinline__ uint32_t shade_rec(const ItemDev &it, uint4 q7, uint32_t flags, float4 rec);
+
 // The colour of one winning fragment: pixel i of item `item`, won by `slot`.
 template <bool ALL_MODES>
 __device__ __forceinline__ uint32_t shade_winner_impl(const BatchDev *b, uint32_t item, uint32_t i, uint32_t slot,
@@ -1432,6 +1439,15 @@ __device__ __forceinline__ uint32_t shade_winner_impl(const BatchDev *b, uint32_
     float4 rec;
     if (overflow || (flags & kRecTall) || !rec_replay(rp, v, b->inline_span, x + v.x, y + v.y, rec))
         rec = it.prec[i]; // recorded by the span kernels (or the overflow winner walk)
+    return shade_rec<ALL_MODES>(it, q7, flags, rec);
+}
+
+// The colour of a fragment of a set-up triangle (vertices and primitive
+// `q7`, TriRec flags `flags`) at the progress values `rec`.
+template <bool ALL_MODES>
+__device__ __forceinline__ uint32_t shade_rec(const ItemDev &it, uint4 q7, uint32_t flags, float4 rec)
+{
+    const ViewDev &v = it.v;
     Shader sh;
     bind_material(it.s, q7.w, sh);
     const float4 w0 = it.s.wpos[q7.x], w1 = it.s.wpos[q7.y], w2 = it.s.wpos[q7.z];
@@ -1668,6 +1684,245 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
     }
 }
 
+// ------------------------------------------------------ transparency layers --
+//
+// A view with transparency layers (renderer.cpp:494-550) keeps per pixel the
+// opaque depth and colour and up to `layers` transparent fragments sorted by
+// depth, layer 0 the farthest.  The outcome depends on the draw order only
+// through depth ties, so it can be computed from the pixel's fragments taken
+// in any order:
+//  - the screen gets the first drawn of the nearest opaque (alpha 255)
+//    fragments, as without layers, and the depth buffer its depth;
+//  - the layers hold the `layers` nearest transparent fragments strictly in
+//    front of it, nearer meaning a smaller depth or, at equal depth, drawn
+//    later (an insertion goes in front of the equal depths already there,
+//    and when every layer is used the farthest is dropped).
+// The capture walk chains every fragment of a pixel; the resolve takes a
+// pixel's chain in (depth, draw order), shading fragments up to the first
+// opaque one.  The flatten and copy passes follow viewport_t::flatten
+// (viewport.cpp:43-86) and post_shader_t's copy of the first layer to the
+// screen (post_shaders.hpp:22-47).  A layered batch holds one view.
+
+__device__ __forceinline__ unsigned long long *frag_counter(const BatchDev *b)
+{
+    return b->counters + C_FRAGS / 2;
+}
+
+// The fragment pool was too small: nothing is written, the host renders again.
+__device__ __forceinline__ bool frags_overflowed(const BatchDev *b)
+{
+    return *frag_counter(b) > (unsigned long long)b->frag_cap;
+}
+
+// blend (src/render/colors.cpp:39-57): back * (256 - a) / 256 + front * a / 256
+// truncated, which is exact in integers (both terms are multiples of 1/256).
+__device__ __forceinline__ uint32_t blend_px(uint32_t back, uint32_t front)
+{
+    const uint32_t a = front >> 24, ba = back >> 24;
+    const uint32_t na = 255u - ((255u - a) * (255u - ba) / 255u);
+    if (a == 255u)
+        return (front & 0x00FFFFFFu) | (na << 24);
+    if (a == 0u)
+        return (back & 0x00FFFFFFu) | (na << 24);
+    uint32_t out = na << 24;
+#pragma unroll
+    for (int c = 0; c < 24; c += 8) {
+        const uint32_t bc = (back >> c) & 0xFFu, fc = (front >> c) & 0xFFu;
+        out |= ((bc * (256u - a) + fc * a) >> 8) << c;
+    }
+    return out;
+}
+
+// Chains every fragment of its spans to the pixels; a span reserves its
+// fragments with one atomic (pixels skipped at the near plane leave holes).
+struct FragVisitor {
+    const BatchDev *b;
+    const ItemDev *it;
+    uint32_t slot;
+    unsigned long long drawn_n, fragments;
+
+    __device__ __forceinline__ bool active() const { return true; }
+    __device__ __forceinline__ void drawn() { drawn_n++; }
+    __device__ __forceinline__ void span(int y, int x1, int x2, const Side &Ls, const Side &Rs, uint32_t bits)
+    {
+        const unsigned long long n = (unsigned long long)(x2 - x1);
+        fragments += n;
+        unsigned long long k = atomicAdd(frag_counter(b), n);
+        if (k + n > (unsigned long long)b->frag_cap)
+            return; // counted, not stored: the pool is grown and the view rendered again
+        const ViewDev &v = it->v;
+        uint32_t *head = it->frag_head + ((long long)(y - v.y) * v.w - v.x);
+        Frag *pool = b->frags;
+        const uint32_t sl = slot;
+        const float pl = Ls.it.alpha, pr = Rs.it.alpha, fb = __uint_as_float(bits);
+        auto op = [&](int x, float z, float progress) {
+            const uint32_t at = (uint32_t)k + (uint32_t)(x - x1);
+            const uint32_t next = atomicExch(head + x, at);
+            reinterpret_cast<float4 *>(pool + at)[0] = make_float4(progress, pl, pr, fb);
+            reinterpret_cast<uint4 *>(pool + at)[1] = make_uint4(__float_as_uint(z), sl, next, 0u);
+        };
+        span_pixels(x1, x2, Ls, Rs, op);
+    }
+};
+
+// Fragment capture: one thread per triangle of the walk list (the walk of
+// fill_triangle_2 from its vertices) and per near-clipped triangle.
+__global__ void __launch_bounds__(256) k_frags(const BatchDev *b)
+{
+    const uint32_t n_raw = *counter32(b, C_LIST), c_raw = *counter32(b, C_CLIP);
+    const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
+    const uint32_t nc = c_raw < b->clip_cap ? c_raw : b->clip_cap;
+    ItemAcc acc;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; i0 < n + nc; i0 += stride) {
+        const uint32_t i = i0 + (threadIdx.x & 31);
+        FragVisitor vis{b, nullptr, 0u, 0ull, 0ull};
+        uint32_t item = 0;
+        if (i < n) {
+            const uint2 e = b->list[i];
+            const ItemDev &it = b->items[e.y];
+            item = e.y;
+            vis.it = &it;
+            vis.slot = 2 * e.x;
+            const uint4 tri = it.s.tris[e.x];
+            V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
+            int pa = 0, pb = 1, pc = 2;
+            sort_z_desc(a, c1, c2, pa, pb, pc);
+            walk_sub(it.v, a, c1, c2, vis);
+            vis.drawn_n = 0; // the set-up counted it
+        } else if (i < n + nc) {
+            const uint2 e = b->clip[b->clip_cap - 1 - (i - n)];
+            const ItemDev &it = b->items[e.y];
+            item = e.y;
+            vis.it = &it;
+            auto emit = [&](uint32_t slot, const TV &a, const TV &c1, const TV &c2, bool) {
+                vis.slot = slot;
+                walk_sub(it.v, a.vp, c1.vp, c2.vp, vis);
+            };
+            clip_triangle(it, e.x, emit);
+        }
+        acc.add(b, item, vis.drawn_n, vis.fragments, i < n + nc);
+    }
+    acc.flush(b);
+}
+
+// The colour of a captured fragment.
+__device__ __forceinline__ uint32_t shade_frag(const BatchDev *b, const ItemDev &it, uint32_t item, uint32_t slot,
+                                               float4 rec)
+{
+    const uint32_t ri = b->recmap[__ldg(b->tri_base + item) + (slot >> 1)];
+    if (ri == kRecClip)
+        return shade_clip_rec(it, slot, rec);
+    const uint4 *q = reinterpret_cast<const uint4 *>(b->recs + ri);
+    return shade_rec<true>(it, q[7], q[6].y, rec);
+}
+
+// Per pixel: the opaque winner to the screen and the depth buffer, the
+// transparent layers in front of it merged into the first one
+// (viewport_t::flatten(front, back), viewport.cpp:43-51).
+__global__ void __launch_bounds__(128) k_layers(const BatchDev *b)
+{
+    if (frags_overflowed(b))
+        return;
+    const ItemDev &it = b->items[0];
+    const int w = it.v.w, n_layers = it.layers;
+    const uint32_t total = (uint32_t)w * (uint32_t)it.v.h;
+    const Frag *pool = b->frags;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const uint32_t head = it.frag_head[i];
+        uint32_t lz[SGL_MAX_LAYERS], ls[SGL_MAX_LAYERS], lc[SGL_MAX_LAYERS]; // kept, nearest first
+        int nt = 0;
+        uint32_t wz = kMaxZBits, wc = 0u;
+        unsigned long long prev = 0ull;
+        bool first = true;
+        for (;;) {
+            // the next fragment in (depth, draw order)
+            unsigned long long best = ~0ull;
+            uint32_t bi = kFragEnd;
+            for (uint32_t f = head; f != kFragEnd;) {
+                const uint4 m = reinterpret_cast<const uint4 *>(pool + f)[1];
+                const unsigned long long key = ((unsigned long long)m.x << 32) | m.y;
+                if ((first || key > prev) && key < best) {
+                    best = key;
+                    bi = f;
+                }
+                f = m.z;
+            }
+            if (bi == kFragEnd)
+                break;
+            first = false;
+            prev = best;
+            const uint32_t z = (uint32_t)(best >> 32), slot = (uint32_t)best;
+            const uint32_t c = shade_frag(b, it, 0u, slot, reinterpret_cast<const float4 *>(pool + bi)[0]);
+            if ((c >> 24) == 255u) {
+                wz = z;
+                wc = c;
+                while (nt > 0 && lz[nt - 1] == z)
+                    nt--; // not strictly in front
+                break;
+            }
+            if (nt == n_layers && (z > lz[nt - 1] || (z == lz[nt - 1] && slot < ls[nt - 1])))
+                continue; // farther than every kept layer
+            int k = nt < n_layers ? nt : n_layers - 1;
+            while (k > 0 && (lz[k - 1] > z || (lz[k - 1] == z && ls[k - 1] < slot))) {
+                lz[k] = lz[k - 1];
+                ls[k] = ls[k - 1];
+                lc[k] = lc[k - 1];
+                k--;
+            }
+            lz[k] = z;
+            ls[k] = slot;
+            lc[k] = c;
+            if (nt < n_layers)
+                nt++;
+        }
+        const int y = (int)(i / (uint32_t)w), x = (int)(i - (uint32_t)y * (uint32_t)w);
+        it.pixels[(long long)y * it.pitch_px + x] = wc; // 0 = viewport_t::clear's background
+        if (it.zbuf)
+            it.zbuf[i] = __uint_as_float(wz);
+        uint32_t l0 = nt > 0 ? lc[nt - 1] : 0u;
+        for (int k = 1; k < nt; k++) {
+            const uint32_t f = lc[nt - 1 - k];
+            if (f >> 24)
+                l0 = blend_px(l0, f);
+        }
+        it.layer0[i] = l0;
+    }
+}
+
+// viewport_t::flatten(front) (viewport.cpp:53-79): view pixel (x, y) reads
+// the surface at row y, column x.
+__global__ void __launch_bounds__(256) k_flatten(const BatchDev *b)
+{
+    if (frags_overflowed(b))
+        return;
+    const ItemDev &it = b->items[0];
+    const int w = it.v.w;
+    const uint32_t total = (uint32_t)w * (uint32_t)it.v.h;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int y = (int)(i / (uint32_t)w), x = (int)(i - (uint32_t)y * (uint32_t)w);
+        const uint32_t back = it.surface[(long long)y * it.pitch_px + x];
+        const uint32_t f = it.layer0[i];
+        it.layer0[i] = (f >> 24) ? blend_px(back, f) : back;
+    }
+}
+
+// post_shader_t::copy_first_transparency_layer_to_screen
+// (post_shaders.hpp:22-31): view pixel (x, y) to surface row y + view y,
+// column x.
+__global__ void __launch_bounds__(256) k_copy_layer(const BatchDev *b)
+{
+    if (frags_overflowed(b))
+        return;
+    const ItemDev &it = b->items[0];
+    const int w = it.v.w;
+    const uint32_t total = (uint32_t)w * (uint32_t)it.v.h;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int y = (int)(i / (uint32_t)w), x = (int)(i - (uint32_t)y * (uint32_t)w);
+        it.surface[(long long)(y + it.v.y) * it.pitch_px + x] = it.layer0[i];
+    }
+}
+
 // ---------------------------------------------------------------- launches --
 
 static inline unsigned grid_for(uint64_t n, int block) { return (unsigned)((n + block - 1) / block); }
@@ -1694,8 +1949,9 @@ cudaError_t launch_world(const SceneDev &s, cudaStream_t st)
 
 const char *prof_kernel_name(int k)
 {
-    static const char *names[kProfKernels] = {"k_vertex", "k_flags",   "k_compact", "k_setup", "k_walk",
-                                              "k_spans",  "k_winners", "k_shade",   "k_dof"};
+    static const char *names[kProfKernels] = {"k_vertex", "k_flags",   "k_compact", "k_setup",  "k_walk",
+                                              "k_spans",  "k_winners", "k_shade",   "k_dof",    "k_frags",
+                                              "k_layers", "k_flatten", "k_copy_layer"};
     return (k >= 0 && k < kProfKernels) ? names[k] : "?";
 }
 
@@ -1707,6 +1963,8 @@ static void prof_collect(Profiler *p)
     if (cudaEventSynchronize(p->ev[kProfKernels]) == cudaSuccess) {
         for (int k = 0; k < kProfKernels; k++) {
             float ms = 0.0f;
+            if (!(p->ran & (1u << k)))
+                continue; // a stage this sequence skipped
             if (cudaEventElapsedTime(&ms, p->ev[k], p->ev[k + 1]) == cudaSuccess) {
                 p->ms[k] += ms;
                 p->launches[k]++;
@@ -1746,32 +2004,69 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
             if (!prof->ev[k] && cudaEventCreate(&prof->ev[k]) != cudaSuccess)
                 return cudaGetLastError();
     }
+    if (timed)
+        prof->ran = 0;
     auto mark = [&](int k) {
         if (timed)
             cudaEventRecord(prof->ev[k], st);
+    };
+    auto ran = [&](int k) {
+        if (timed)
+            prof->ran |= 1u << k;
     };
     const int sms = sm_count();
     int n = 0;
     mark(PK_VERTEX);
     k_vertex<<<sms * 8, 256, 0, st>>>(b);
+    ran(PK_VERTEX);
     n++;
     mark(PK_FLAGS);
     k_flags<<<sms * 8, 256, 0, st>>>(b);
+    ran(PK_FLAGS);
     n++;
     mark(PK_COMPACT);
     k_compact<<<sms * 4, kCompactBlock, 0, st>>>(b);
+    ran(PK_COMPACT);
     n++;
     mark(PK_SETUP);
     k_setup<<<sms * 8, 256, 0, st>>>(b);
+    ran(PK_SETUP);
     n++;
+    if (flags & kSeqLayers) {
+        for (int k = PK_WALK; k <= PK_DOF; k++)
+            mark(k);
+        mark(PK_FRAGS);
+        k_frags<<<sms * 8, 256, 0, st>>>(b);
+        ran(PK_FRAGS);
+        mark(PK_LAYERS);
+        k_layers<<<sms * 16, 128, 0, st>>>(b);
+        ran(PK_LAYERS);
+        mark(PK_FLATTEN);
+        k_flatten<<<sms * 8, 256, 0, st>>>(b);
+        ran(PK_FLATTEN);
+        mark(PK_COPY);
+        k_copy_layer<<<sms * 8, 256, 0, st>>>(b);
+        ran(PK_COPY);
+        n += 4;
+        if (timed) {
+            cudaEventRecord(prof->ev[kProfKernels], st);
+            prof->pending = true;
+        }
+        if (launches)
+            *launches += n;
+        return cudaGetLastError();
+    }
     mark(PK_WALK);
     k_walk<<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
+    ran(PK_WALK);
     n++;
     mark(PK_SPANS);
     k_spans<<<sms * 4, 256, 0, st>>>(b);
+    ran(PK_SPANS);
     n++;
     mark(PK_WINNER);
     k_winners<<<sms * 4, 256, 0, st>>>(b);
+    ran(PK_WINNER);
     n++;
     mark(PK_SHADE);
     // the kernel with every pixel shader only when a view asks for another
@@ -1792,12 +2087,16 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
         else
             k_shade<16, false><<<sg, kShadeThreads, 0, st>>>(b);
     }
+    ran(PK_SHADE);
     n++;
     mark(PK_DOF);
     if (flags & kSeqDof) {
         k_dof<<<sms * 8, 256, 0, st>>>(b);
+        ran(PK_DOF);
         n++;
     }
+    for (int k = PK_FRAGS; k <= PK_COPY; k++)
+        mark(k);
     if (timed) {
         cudaEventRecord(prof->ev[kProfKernels], st);
         prof->pending = true;

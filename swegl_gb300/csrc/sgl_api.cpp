@@ -43,6 +43,14 @@ sgl_status check_view(Ctx *ctx, const sgl_view &v, const sgl_target &t)
         ctx->fail("unknown pixel shader %d", v.shader);
         return SGL_ERR_INVALID;
     }
+    if (v.layers < 0 || v.layers > SGL_MAX_LAYERS) {
+        ctx->fail("transparency layers %d outside 0..%d", v.layers, SGL_MAX_LAYERS);
+        return SGL_ERR_INVALID;
+    }
+    if (v.layers > 0 && v.dof.enabled) {
+        ctx->fail("depth of field on a view with transparency layers is not implemented");
+        return SGL_ERR_UNSUPPORTED;
+    }
     if (v.w <= 0 || v.h <= 0 || v.x < 0 || v.y < 0 || (int64_t)v.w * v.h > (1ll << 28)) {
         ctx->fail("bad viewport %d,%d %dx%d", v.x, v.y, v.w, v.h);
         return SGL_ERR_INVALID;
@@ -69,6 +77,72 @@ static sgl_status ext_lane(Ctx *ctx, cudaStream_t st, Lane **out)
     }
     ctx->ext_lane->stream = st;
     *out = ctx->ext_lane.get();
+    return SGL_OK;
+}
+
+// Entry points other than sgl_render take opaque views only.
+sgl_status reject_layers(Ctx *ctx, const sgl_view &v)
+{
+    if (v.layers == 0)
+        return SGL_OK;
+    ctx->fail("views with transparency layers render through sgl_render only");
+    return SGL_ERR_UNSUPPORTED;
+}
+
+// One view with transparency layers.  Its flatten and copy passes read and
+// write the surface outside the viewport's rectangle (viewport.cpp:53-79,
+// post_shaders.hpp:22-31), so a host surface is staged whole.  The call
+// waits for the frame: the fragment pool is checked and, when it was too
+// small (nothing was written then), grown and the view rendered again.
+static sgl_status render_layered(Ctx *ctx, Lane *lane, BatchEntry &e, const sgl_target &t, bool device_buffers,
+                                 int *launches, sgl_frame_stats *acc, bool want_stats)
+{
+    const sgl_view &v = e.view;
+    const size_t surf_bytes = (size_t)t.pitch * t.height, px = (size_t)v.w * v.h;
+    if (device_buffers) {
+        e.surface = (uint32_t *)t.pixels;
+    } else {
+        CUDA_TRY(ctx->stage_pixels.ensure(surf_bytes));
+        CUDA_TRY(ctx->stage_z.ensure(4 * px));
+        CUDA_TRY(cudaMemcpyAsync(ctx->stage_pixels.ptr, t.pixels, surf_bytes, cudaMemcpyHostToDevice, lane->stream));
+        e.surface = (uint32_t *)ctx->stage_pixels.ptr;
+        e.zbuf = t.zbuffer ? (float *)ctx->stage_z.ptr : nullptr;
+    }
+    e.pitch_px = t.pitch / 4;
+    e.rect_pixels = e.surface + (size_t)v.y * e.pitch_px + v.x;
+    int slot = 0;
+    bool fit = false;
+    for (int attempt = 0; attempt < 3 && !fit; attempt++) {
+        sgl_status r = lane->prepare(ctx, &e, 1, ctx->tile, ctx->inline_span, nullptr, &slot);
+        if (r == SGL_OK)
+            r = lane->launch(ctx, slot, ctx->tile, false, launches, &ctx->prof);
+        if (r == SGL_OK)
+            r = lane->layered_fit(ctx, slot, &fit);
+        if (r != SGL_OK)
+            return r;
+    }
+    if (!fit) {
+        ctx->fail("the fragment pool did not fit after growing");
+        return SGL_ERR_OOM;
+    }
+    if (!device_buffers) {
+        // rows y .. y+h-1 hold every pixel the view wrote
+        const size_t row0 = (size_t)v.y * t.pitch;
+        CUDA_TRY(cudaMemcpyAsync((uint8_t *)t.pixels + row0, (uint8_t *)ctx->stage_pixels.ptr + row0,
+                                 (size_t)v.h * t.pitch, cudaMemcpyDeviceToHost, lane->stream));
+        if (t.zbuffer)
+            CUDA_TRY(cudaMemcpyAsync(t.zbuffer, ctx->stage_z.ptr, 4 * px, cudaMemcpyDeviceToHost, lane->stream));
+        CUDA_TRY(cudaStreamSynchronize(lane->stream));
+    }
+    if (want_stats) {
+        unsigned long long d = 0, f = 0;
+        sgl_status r = lane->read_counters(ctx, slot, &d, &f, nullptr);
+        if (r != SGL_OK)
+            return r;
+        acc->drawn_triangles += d;
+        acc->fragments += f;
+    }
+    acc->pixels += px;
     return SGL_OK;
 }
 
@@ -267,6 +341,12 @@ SGL_API sgl_status sgl_render(sgl_ctx *c, int scene_id, const sgl_view *views, c
         const sgl_target &t = targets[i];
         BatchEntry e{s, v, nullptr, t.pitch / 4, t.zbuffer};
         const size_t px = (size_t)v.w * v.h;
+        if (v.layers > 0) {
+            sgl_status r = render_layered(ctx, lane, e, t, device_buffers != 0, &launches, &acc, stats != nullptr);
+            if (r != SGL_OK)
+                return r;
+            continue;
+        }
         if (device_buffers) {
             e.rect_pixels = (uint32_t *)t.pixels + (size_t)v.y * (t.pitch / 4) + v.x;
         } else {
@@ -319,6 +399,8 @@ SGL_API sgl_status sgl_render_debug(sgl_ctx *c, int scene_id, const sgl_view *vi
         return SGL_ERR_NOT_FOUND;
     cudaSetDevice(ctx->device);
     sgl_status r = check_view(ctx, *view, *target);
+    if (r == SGL_OK)
+        r = reject_layers(ctx, *view);
     if (r != SGL_OK)
         return r;
     Lane *lane = ctx->lane.get();
@@ -380,6 +462,8 @@ static sgl_status batch_entries(Ctx *ctx, const sgl_batch_item *items, int n, st
             return SGL_ERR_NOT_FOUND;
         }
         sgl_status st = check_view(ctx, items[i].view, items[i].target);
+        if (st == SGL_OK)
+            st = reject_layers(ctx, items[i].view);
         if (st != SGL_OK)
             return st;
         const sgl_target &t = items[i].target;

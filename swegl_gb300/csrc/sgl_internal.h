@@ -89,7 +89,25 @@ struct ItemDev {
     int dof_pitch;
     int dof_halo;    // tap reach in pixels (ceil of max_radius, <= kDofMaxHalo), -1: gather from memory
     int dof_tiles_x; // kDofTile tiles across the view
+    // transparency layers (viewport_t::m_transparency_layers); when layers
+    // > 0, `pixels` points into a whole surface whose row 0, column 0 is
+    // `surface`, and each view pixel has a fragment list and a layer colour
+    int layers;
+    uint32_t *surface;
+    uint32_t *frag_head; // per view pixel: first fragment (kFragEnd: none)
+    uint32_t *layer0;    // per view pixel: the layers merged into the first one
 };
+
+// One fragment of a view with transparency layers: its depth, draw slot and
+// the progress values that shade it, chained per pixel.
+struct __align__(16) Frag {
+    float4 rec;   // progress, progL, progR, span bits (as in ItemDev::prec)
+    uint32_t z;   // depth bits
+    uint32_t slot;
+    uint32_t next;
+    uint32_t pad;
+};
+constexpr uint32_t kFragEnd = 0xFFFFFFFFu;
 
 constexpr uint8_t kYesDrawn = 1;  // a visible triangle flagged the vertex (renderer.cpp:86-185)
 constexpr uint8_t kYesBehind = 2; // its z' is below the near plane (fill_triangle's clip test)
@@ -159,7 +177,7 @@ constexpr uint32_t kRecClip = 0xFFFFFFFFu; // recmap entry of a near-clipped tri
 
 // Batch counters (32-bit words); the drawn-triangle and fragment counts are
 // kept per item (item_counters) and summed by the host.
-enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_TALL = 10 };
+enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_FRAGS = 8, C_TALL = 10 };
 // Work queues of the shade kernel's tiles: kQueues counters, one per 128-byte
 // line so that blocks of different queues do not contend.
 constexpr int kQueues = 16;
@@ -190,17 +208,23 @@ struct BatchDev {
     unsigned long long *counters;      // kCounterWords words
     unsigned long long *item_counters; // per item: drawn, fragments
     uint8_t *slot_flags;       // debug, single-item batches: slot reached scanline setup
+    Frag *frags;               // fragment pool of the views with transparency layers
+    uint32_t frag_cap;
 };
 
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each stage of a launch sequence (enabled with sgl_profile).
-constexpr int kProfKernels = 9;
-enum ProfKernel { PK_VERTEX = 0, PK_FLAGS, PK_COMPACT, PK_SETUP, PK_WALK, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF };
+constexpr int kProfKernels = 13;
+enum ProfKernel {
+    PK_VERTEX = 0, PK_FLAGS, PK_COMPACT, PK_SETUP, PK_WALK, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF,
+    PK_FRAGS, PK_LAYERS, PK_FLATTEN, PK_COPY
+};
 struct Profiler {
     bool enabled = false;
     cudaEvent_t ev[kProfKernels + 1] = {};
     double ms[kProfKernels] = {};
     uint64_t launches[kProfKernels] = {};
+    uint32_t ran = 0; // stages the pending sequence launched (bit per ProfKernel)
     bool pending = false;
 };
 const char *prof_kernel_name(int k);
@@ -213,7 +237,12 @@ cudaError_t launch_world(const SceneDev &s, cudaStream_t st);
 // every pixel shader (a view asks for another than the default).  The depth
 // keys must hold
 // kEmptyKey on entry; the shade kernel leaves them so (unless keep_keys).
-constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqVariants = 4;
+// kSeqLayers (a single view with transparency layers) replaces the depth walk
+// and shade by the fragment capture, the per-pixel layer resolve and the
+// flatten and copy passes; its fragment pool must have been big enough
+// (C_FRAGS <= frag_cap) for the outputs to be written, else they are left
+// untouched and the host renders again with a bigger pool.
+constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqLayers = 4, kSeqVariants = 8;
 cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st, int *launches, Profiler *prof);
 // The depth-of-field gather alone (items prepared by the caller).
 cudaError_t launch_dof(const BatchDev *b, cudaStream_t st);

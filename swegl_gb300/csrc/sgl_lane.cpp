@@ -167,6 +167,25 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
             CUDA_TRY(dofz.ensure(4 * dofz_px));
     }
     int seq_flags = 0;
+    int layers = 0;
+    for (int i = 0; i < n; i++)
+        layers = std::max(layers, e[i].view.layers);
+    size_t frag_cap = 0;
+    if (layers > 0) {
+        // one view per layered batch: its flatten and copy passes read and
+        // write the whole surface, in view order
+        if (n != 1 || e[0].view.dof.enabled || !e[0].surface) {
+            ctx->fail("transparency layers take one view per launch sequence, without depth of field");
+            return SGL_ERR_UNSUPPORTED;
+        }
+        frag_want = std::max<size_t>(frag_want, std::max<size_t>(4 * tp, 65536));
+        CUDA_TRY(frags.ensure(sizeof(Frag) * frag_want));
+        CUDA_TRY(frag_head.ensure(4 * tp));
+        CUDA_TRY(layer0.ensure(4 * tp));
+        CUDA_TRY(cudaMemsetAsync(frag_head.ptr, 0xFF, 4 * tp, stream)); // kFragEnd
+        frag_cap = std::min<size_t>(frags.bytes / sizeof(Frag), 0xFFFFFFFFu);
+        seq_flags |= kSeqLayers;
+    }
     ItemDev *hi = (ItemDev *)sl.h_items.ptr;
     for (int i = 0; i < n; i++) {
         const BatchEntry &en = e[i];
@@ -204,6 +223,12 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         }
         if (en.view.shader != SGL_SHADER_PHONG_BILINEAR)
             seq_flags |= kSeqShaders;
+        if (layers > 0) {
+            it.layers = en.view.layers;
+            it.surface = en.surface;
+            it.frag_head = (uint32_t *)frag_head.ptr;
+            it.layer0 = (uint32_t *)layer0.ptr;
+        }
         hi[i] = it;
     }
     BatchDev *hbd = (BatchDev *)sl.h_batch.ptr;
@@ -236,6 +261,8 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.counters = (unsigned long long *)sl.d_counters.ptr;
     bd.item_counters = (unsigned long long *)sl.d_item_counters.ptr;
     bd.slot_flags = slot_flags;
+    bd.frags = (Frag *)frags.ptr;
+    bd.frag_cap = (uint32_t)frag_cap;
     *hbd = bd;
     CUDA_TRY(cudaMemcpyAsync(sl.d_items.ptr, hi, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(sl.d_bases.ptr, hb, sizeof(uint32_t) * 5 * (n + 1), cudaMemcpyHostToDevice, stream));
@@ -286,6 +313,9 @@ sgl_status Lane::launch(Ctx *ctx, int si, int tile, bool use_graph, int *launche
     unsigned long long *hc = (unsigned long long *)sl.h_counters.ptr; // per-item counters only
     CUDA_TRY(cudaMemcpyAsync(hc + kCounterWords, sl.d_item_counters.ptr,
                              2 * sizeof(unsigned long long) * sl.n_items, cudaMemcpyDeviceToHost, stream));
+    if (sl.seq_flags & kSeqLayers) // and the fragment count of a layered view
+        CUDA_TRY(cudaMemcpyAsync(hc + C_FRAGS / 2, (unsigned long long *)sl.d_counters.ptr + C_FRAGS / 2,
+                                 sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaEventRecord(sl.done, stream));
     return SGL_OK;
 }
@@ -308,6 +338,23 @@ sgl_status Lane::read_counters(Ctx *ctx, int si, unsigned long long *drawn, unsi
         *fragments = f;
     if (per_item)
         per_item->assign(hc + kCounterWords, hc + kCounterWords + 2 * sl.n_items);
+    return SGL_OK;
+}
+
+sgl_status Lane::layered_fit(Ctx *ctx, int si, bool *fit)
+{
+    Slot &sl = slots[si];
+    CUDA_TRY(cudaEventSynchronize(sl.done));
+    const unsigned long long need = ((const unsigned long long *)sl.h_counters.ptr)[C_FRAGS / 2];
+    const size_t cap = std::min<size_t>(frags.bytes / sizeof(Frag), 0xFFFFFFFFu);
+    *fit = need <= cap;
+    if (!*fit) {
+        if (need + need / 4 >= 0xFFFFFFFFull) {
+            ctx->fail("%llu fragments exceed the fragment pool's 32-bit index", need);
+            return SGL_ERR_UNSUPPORTED;
+        }
+        frag_want = (size_t)(need + need / 4);
+    }
     return SGL_OK;
 }
 

@@ -73,6 +73,7 @@ struct BatchEntry {
     uint32_t *rect_pixels; // device, at the viewport's top-left pixel
     int pitch_px;
     float *zbuf;           // device, w*h, may be null
+    uint32_t *surface = nullptr; // device, the whole surface (row 0, column 0): views with transparency layers
 };
 
 // Scratch bytes a view needs beyond its output buffers: vertex NDC and flags,
@@ -104,6 +105,8 @@ struct Lane {
     } slots[kSlots];
     int next = 0;
     DevBuf list, recs, recmap, tall, spans, ndc, yes, key, prec, doftmp, dofz;
+    DevBuf frags, frag_head, layer0; // views with transparency layers
+    size_t frag_want = 0;            // fragments the pool must hold (grown after an overflow)
     bool keys_dirty = false; // the key pool may hold other than kEmptyKey (debug, failed launch)
     ~Lane();
 
@@ -117,6 +120,9 @@ struct Lane {
     // Per-batch and per-item counters of a finished slot (synchronises the slot).
     sgl_status read_counters(Ctx *ctx, int slot, unsigned long long *drawn, unsigned long long *fragments,
                              std::vector<unsigned long long> *per_item);
+    // A finished layered slot: true when its fragment pool was big enough,
+    // else grows frag_want for the next attempt (synchronises the slot).
+    sgl_status layered_fit(Ctx *ctx, int slot, bool *fit);
 };
 
 struct Ctx {
@@ -142,5 +148,6 @@ struct Ctx {
 
 ViewDev make_view(const sgl_view &v);
 sgl_status check_view(Ctx *ctx, const sgl_view &v, const sgl_target &t);
+sgl_status reject_layers(Ctx *ctx, const sgl_view &v);
 
 } // namespace sgl

@@ -271,6 +271,8 @@ SGL_API sgl_status sgl_server_submit(sgl_server *s, const sgl_request *req, uint
     const sgl_view &v = req->view;
     if (v.w <= 0 || v.h <= 0 || (int64_t)v.w * v.h > (1ll << 28))
         return SGL_ERR_INVALID;
+    if (v.layers != 0)
+        return SGL_ERR_UNSUPPORTED; // transparency layers render through sgl_render only
     Job j{};
     j.req = *req;
     j.scene = scene;

@@ -119,11 +119,14 @@ class Renderer:
         return {"triangles": t.value, "vertices": v.value, "device_bytes": b.value}
 
     # rendering ------------------------------------------------------------
-    def render(self, scene_id: int, views, shared_surface=None, stats: bool = False):
+    def render(self, scene_id: int, views, shared_surface=None, stats: bool = False, background=None):
         """Render `views` in order into host surfaces (one per view, or one
-        shared surface of size `shared_surface`).  Returns (frames, stats)."""
+        shared surface of size `shared_surface`, holding `background` before
+        the render).  Returns (frames, stats)."""
         if shared_surface:
             surf = abi.HostFrame(*shared_surface)
+            if background is not None:
+                surf.pixels[...] = background
             frames = []
             for v in views:
                 f = abi.HostFrame(*shared_surface, zw=v.w, zh=v.h)

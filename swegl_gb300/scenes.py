@@ -216,6 +216,7 @@ class View:
     dof_max_radius: float = 16.0
     dof_px_scale: float = 0.0
     shader: int = 0  # SGL_SHADER_* (include/sgl.h)
+    layers: int = 0  # transparency layers (0 = opaque)
 
 
 @dataclass
@@ -390,6 +391,21 @@ def texture_value_noise(seed: int, size: int, octaves: int = 4, base_cells: int 
     return (np.uint32(0xFF000000) | (r << np.uint32(16)) | (g << np.uint32(8)) | b).astype(np.uint32)
 
 
+def texture_block_alpha(seed: int, w: int, h: int, block: int = 8) -> np.ndarray:
+    """Uniform random RGB texels whose alpha is constant over block x block
+    texel squares: per square 255 (3/8 of them), 0 (1/8) or uniform in
+    1..254, so that bilinear filtering inside a square keeps its alpha."""
+    i = np.arange(w * h, dtype=np.uint64)
+    rgb = (hash64(seed, 0xA1F, i) & np.uint64(0xFFFFFF)).astype(np.uint32).reshape(h, w)
+    by, bx = np.meshgrid(np.arange(h, dtype=np.uint64) // np.uint64(block),
+                         np.arange(w, dtype=np.uint64) // np.uint64(block), indexing="ij")
+    hv = hash64(seed, 0xB10C, by, bx)
+    sel = (hv & np.uint64(7)).astype(np.uint32)
+    rnd = (np.uint64(1) + (hv >> np.uint64(8)) % np.uint64(254)).astype(np.uint32)
+    a = np.where(sel == 0, np.uint32(0), np.where(sel <= 3, np.uint32(255), rnd))
+    return (rgb | (a << np.uint32(24))).astype(np.uint32)
+
+
 # --------------------------------------------------------------------------
 # the benchmark scenes
 # --------------------------------------------------------------------------
@@ -530,6 +546,50 @@ def mixed_scene(seed: int = 4) -> Scene:
         s.add_primitive(n3, TRIANGLE_STRIP, 3, p, n, t, idx)
     s.point_lights = [(0.5, 2.0, 1.5, 3.0), (-2.0, -0.5, 1.0, 1.5)]
     s.ambient = 0.15
+    s.sun_intensity = 0.6
+    return s.finalize()
+
+
+def glass_scene(seed: int = 8) -> Scene:
+    """Scene for transparency layers: an opaque textured cube behind stacked
+    double-sided sheets and random triangles whose textures have block alpha
+    (opaque, clear and translucent squares), a sphere with such a texture,
+    and untextured materials whose colours carry alpha (seen by the
+    material-colour shader)."""
+    rng = Rng(seed)
+    s = Scene()
+    s.textures.append(texture_uniform(seed, 128, 128))
+    s.textures.append(texture_block_alpha(seed + 1, 64, 64, 8))
+    s.textures.append(texture_block_alpha(seed + 2, 128, 64, 16))
+    s.materials.append((0xFFFFFFFF, 0, 0, 32))   # opaque texture
+    s.materials.append((0x80FF4020, 1, 1, 32))   # block alpha, double-sided; colour alpha 128
+    s.materials.append((0xC02060FF, 2, 1, 32))   # block alpha (coarser), double-sided; colour alpha 192
+    s.materials.append((0x4040FF40, -1, 1, 32))  # untextured, colour alpha 64
+    s.materials.append((0xFFFFFF00, -1, 0, 32))  # untextured, opaque colour
+    n0 = s.add_node(translation=(0.0, 0.0, -1.5), rotation=matmul4(rot_y(0.5), rot_x(0.4)).astype(np.float32))
+    for (p, n, t, i) in cube_mesh(1.6):
+        s.add_primitive(n0, TRIANGLE_FAN, 0, p, n, t, i)
+    # four stacked sheets (quads as fans), each a little nearer, alternating materials
+    for k in range(4):
+        z = -0.6 + 0.45 * k
+        nk = s.add_node(translation=(0.15 * k - 0.2, 0.1 * k - 0.15, z), rotation=rot_z(0.2 * k).astype(np.float32))
+        q = np.array([[-1.1, -0.8, 0.0], [1.1, -0.8, 0.0], [1.1, 0.8, 0.0], [-1.1, 0.8, 0.0]], np.float32)
+        nq = np.tile(np.array([0.0, 0.0, 1.0], np.float32), (4, 1))
+        uq = np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.0, 1.0]], np.float32)
+        s.add_primitive(nk, TRIANGLE_FAN, 1 + (k % 3), q, nq, uq, np.arange(4, dtype=np.uint32))
+    # 30 random triangles through the stack
+    n5 = s.add_node(translation=(0.2, 0.0, -0.4))
+    pos = rng.uniform(-1.0, 1.0, 30 * 9).reshape(90, 3).astype(np.float32)
+    nrm = normalize_f32(rng.uniform(-1.0, 1.0, 90 * 3).reshape(90, 3))
+    uv = rng.uniform(0.0, 1.0, 180).reshape(90, 2).astype(np.float32)
+    s.add_primitive(n5, TRIANGLES, 2, pos[:45], nrm[:45], uv[:45], np.arange(45, dtype=np.uint32))
+    s.add_primitive(n5, TRIANGLES, 4, pos[45:60], nrm[45:60], uv[45:60], np.arange(15, dtype=np.uint32))
+    s.add_primitive(n5, TRIANGLES, 1, pos[60:], nrm[60:], uv[60:], np.arange(30, dtype=np.uint32))
+    n6 = s.add_node(translation=(-0.9, 0.6, 0.3))
+    for (p, n, t, idx) in uv_sphere_mesh(12, 6, 0.5):
+        s.add_primitive(n6, TRIANGLE_STRIP, 1, p, n, t, idx)
+    s.point_lights = [(0.5, 1.5, 2.0, 2.5)]
+    s.ambient = 0.2
     s.sun_intensity = 0.6
     return s.finalize()
 

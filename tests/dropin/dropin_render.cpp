@@ -147,7 +147,8 @@ int main(int argc, char **argv)
         r.get(proj, sizeof proj);
         r.get(cam, sizeof cam);
         shaders.push_back(make_shader(r.get<int>()));
-        auto vp = std::make_unique<swegl::viewport_t>(x, y, w, h, &surface, shaders.back(), 0);
+        const int layers = r.get<int>();
+        auto vp = std::make_unique<swegl::viewport_t>(x, y, w, h, &surface, shaders.back(), layers);
         for (int k = 0; k < 16; k++) {
             vp->m_camera.m_viewmatrix[k / 4][k % 4] = view[k];
             vp->m_camera.m_projectionmatrix[k / 4][k % 4] = proj[k];

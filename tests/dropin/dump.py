@@ -46,5 +46,6 @@ def write_dump(path, scene, views, surface_wh):
         f32(np.asarray(v.proj, np.float32).reshape(-1))
         f32(v.camera_pos)
         i32(int(getattr(v, "shader", 0)))
+        i32(int(getattr(v, "layers", 0)))
     with open(path, "wb") as fh:
         fh.write(out)

@@ -31,6 +31,8 @@ def scene(key: str) -> S.Scene:
         return S.spheres_scene(shininess=32)
     if key == "grid":
         return S.grid_scene()
+    if key == "glass":
+        return S.glass_scene()
     raise KeyError(key)
 
 
@@ -94,6 +96,33 @@ def cases() -> dict:
         out[f"cube_{name}_320x240"] = dict(scene="cube", views=shaded(lambda: [_look((0.3, 0.2, 1.2), (0, 0, 0), 320, 240)], mode),
                                           kinds=(0,), store=FULL)
 
+    # transparency layers (viewport_t's transparency_layer_count) on the glass scene
+    def glass(w=320, h=240, pos=(0.3, 0.4, 3.2), target=(0.0, 0.0, -0.5), **kw):
+        def views():
+            v = _look(pos, target, w, h)
+            for k, x in kw.items():
+                setattr(v, k, x)
+            return [v]
+        return views
+
+    out["glass_320x240"] = dict(scene="glass", views=glass(), kinds=(0,), store=FULL)
+    for layers, mode in ((1, 0), (2, 0), (3, 0), (8, 0), (2, 4), (3, 6), (1, 8)):
+        out[f"glass_l{layers}_{abi.SHADERS[mode]}_320x240"] = dict(
+            scene="glass", views=glass(layers=layers, shader=mode), kinds=(0,), store=FULL)
+    out["glass_close_l4_320x240"] = dict(scene="glass", views=glass(pos=(0.1, 0.0, 0.3), target=(0.2, 0.1, -2.0),
+                                                                   layers=4), kinds=(0,), store=FULL)
+    # a view off the surface's corner: the layer resolve reads surface rows
+    # 0..h-1 and writes rows y..y+h-1, columns 0..w-1 (viewport.cpp:53-79,
+    # post_shaders.hpp:22-31)
+    out["glass_offset_l3_320x240"] = dict(scene="glass", views=glass(layers=3, x=40, y=30), shared=(400, 300),
+                                          kinds=(0,), store=FULL)
+
+    def glass_pair():
+        a = glass(200, 150, layers=2)()[0]
+        b = glass(200, 150, pos=(-0.5, 0.2, 2.5), layers=4, x=200, y=150)()[0]
+        return [a, b]
+
+    out["glass_pair_2x200x150"] = dict(scene="glass", views=glass_pair, shared=(400, 300), kinds=(0,), store=FULL)
     out["shared_4x320x240"] = dict(scene="spheres200", views=shared_views, shared=(640, 480), kinds=(0, 1), store=FULL)
     out["spheres_1920x1080"] = dict(scene="spheres200", views=lambda: [S.spheres_view(1920, 1080)], kinds=(0, 1, 2),
                                     store=DIGEST)

@@ -35,7 +35,8 @@ def test_header_compiles(tmp_path):
 
 
 @pytest.mark.gpu
-def test_dropin_render_matches_oracle(tmp_path):
+@pytest.mark.parametrize("scene,layers", [("mixed", (0, 0)), ("glass", (3, 0))])
+def test_dropin_render_matches_oracle(tmp_path, scene, layers):
     import cases as G
     import oracle
     from dump import write_dump
@@ -43,13 +44,14 @@ def test_dropin_render_matches_oracle(tmp_path):
     from swegl_gb300 import scenes as S
 
     exe = compile_dropin(str(tmp_path))
-    sc = G.scene("mixed")
+    sc = G.scene(scene)
     views = []
     for i, pos in enumerate([(0.5, 0.8, 4.5), (-2.0, 1.0, 3.5)]):
         m, c = S.look_at(pos, (0, 0, 0))
         v = S.view_for(320, 240, m, c)
         v.x = 320 * i
         v.shader = (0, 3)[i]  # Phong + bilinear; flat light + nearest texture
+        v.layers = layers[i]  # viewport_t's transparency_layer_count
         views.append(v)
     dump = os.path.join(str(tmp_path), "scene.bin")
     out = os.path.join(str(tmp_path), "out.bin")
