@@ -1733,13 +1733,30 @@ __device__ __forceinline__ uint32_t blend_px(uint32_t back, uint32_t front)
     return out;
 }
 
-// Chains every fragment of its spans to the pixels; a span reserves its
-// fragments with one atomic (pixels skipped at the near plane leave holes).
+// The fragments a triangle reserves (one per span pixel): the walk of its
+// edges without the pixel loops.
+struct FragCount {
+    uint32_t slot; // unused (the walk's emit sets it)
+    unsigned long long n;
+
+    __device__ __forceinline__ bool active() const { return true; }
+    __device__ __forceinline__ void drawn() {}
+    __device__ __forceinline__ void span(int, int x1, int x2, const Side &, const Side &, uint32_t)
+    {
+        n += (unsigned long long)(x2 - x1);
+    }
+};
+
+// Chains every fragment of its spans to the pixels, from the triangle's
+// reserved range at `at` (pixels skipped at the near plane leave holes).
+// Spans longer than kFragInline are binned for k_frag_spans.
+constexpr int kFragInline = 32;
 struct FragVisitor {
     const BatchDev *b;
     const ItemDev *it;
     uint32_t slot;
     unsigned long long drawn_n, fragments;
+    unsigned long long at;
 
     __device__ __forceinline__ bool active() const { return true; }
     __device__ __forceinline__ void drawn() { drawn_n++; }
@@ -1747,9 +1764,35 @@ struct FragVisitor {
     {
         const unsigned long long n = (unsigned long long)(x2 - x1);
         fragments += n;
-        unsigned long long k = atomicAdd(frag_counter(b), n);
+        const unsigned long long k = at;
+        at += n;
         if (k + n > (unsigned long long)b->frag_cap)
             return; // counted, not stored: the pool is grown and the view rendered again
+        if (n > (unsigned long long)kFragInline) {
+            // a long span goes to the bins: its pixels are stored a warp at a time
+            const uint32_t si = atomicAdd(counter32(b, C_SPANS), 1u);
+            if (si < b->span_cap) {
+                Interp q;
+                q.init_self(Rs.x - Ls.x, Ls.it.value(), Rs.it.value());
+                q.displace((float)x1 - Ls.x);
+                SpanRec r;
+                r.slot = slot;
+                r.y_bits = (uint32_t)y | bits;
+                r.x1 = x1;
+                r.x2 = x2;
+                r.top = q.top;
+                r.tstep = q.tstep;
+                r.bottom = q.bottom;
+                r.bstep = q.bstep;
+                r.v0 = q.v0;
+                r.dv = q.dv;
+                r.progL = Ls.it.alpha;
+                r.progR = Rs.it.alpha;
+                r.item = (uint32_t)k; // the span's first fragment (a layered batch has one item)
+                b->spans[si] = r;
+                return;
+            }
+        }
         const ViewDev &v = it->v;
         uint32_t *head = it->frag_head + ((long long)(y - v.y) * v.w - v.x);
         Frag *pool = b->frags;
@@ -1766,47 +1809,120 @@ struct FragVisitor {
 };
 
 // Fragment capture: one thread per triangle of the walk list (the walk of
-// fill_triangle_2 from its vertices) and per near-clipped triangle.
+// fill_triangle_2 from its vertices) and per near-clipped triangle.  Each
+// lane first counts its triangle's fragments; the warp then reserves its
+// lanes' ranges with one atomic and walks again to store them.
 __global__ void __launch_bounds__(256) k_frags(const BatchDev *b)
 {
     const uint32_t n_raw = *counter32(b, C_LIST), c_raw = *counter32(b, C_CLIP);
     const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
     const uint32_t nc = c_raw < b->clip_cap ? c_raw : b->clip_cap;
+    const int lane = threadIdx.x & 31;
     ItemAcc acc;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; i0 < n + nc; i0 += stride) {
-        const uint32_t i = i0 + (threadIdx.x & 31);
-        FragVisitor vis{b, nullptr, 0u, 0ull, 0ull};
-        uint32_t item = 0;
+        const uint32_t i = i0 + (uint32_t)lane;
+        uint32_t item = 0, t = 0;
+        bool clip = false;
         if (i < n) {
             const uint2 e = b->list[i];
-            const ItemDev &it = b->items[e.y];
             item = e.y;
-            vis.it = &it;
-            vis.slot = 2 * e.x;
-            const uint4 tri = it.s.tris[e.x];
-            V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
-            int pa = 0, pb = 1, pc = 2;
-            sort_z_desc(a, c1, c2, pa, pb, pc);
-            walk_sub(it.v, a, c1, c2, vis);
-            vis.drawn_n = 0; // the set-up counted it
+            t = e.x;
         } else if (i < n + nc) {
             const uint2 e = b->clip[b->clip_cap - 1 - (i - n)];
-            const ItemDev &it = b->items[e.y];
             item = e.y;
-            vis.it = &it;
-            auto emit = [&](uint32_t slot, const TV &a, const TV &c1, const TV &c2, bool) {
-                vis.slot = slot;
-                walk_sub(it.v, a.vp, c1.vp, c2.vp, vis);
-            };
-            clip_triangle(it, e.x, emit);
+            t = e.x;
+            clip = true;
         }
+        const ItemDev &it = b->items[item];
+        auto walk = [&](auto &vis) {
+            if (i >= n + nc)
+                return;
+            if (!clip) {
+                vis.slot = 2 * t;
+                const uint4 tri = it.s.tris[t];
+                V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
+                int pa = 0, pb = 1, pc = 2;
+                sort_z_desc(a, c1, c2, pa, pb, pc);
+                walk_sub(it.v, a, c1, c2, vis);
+            } else {
+                auto emit = [&](uint32_t slot, const TV &a, const TV &c1, const TV &c2, bool) {
+                    vis.slot = slot;
+                    walk_sub(it.v, a.vp, c1.vp, c2.vp, vis);
+                };
+                clip_triangle(it, t, emit);
+            }
+        };
+        FragCount cnt{0u, 0ull};
+        walk(cnt);
+        unsigned long long incl = cnt.n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long up = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o)
+                incl += up;
+        }
+        unsigned long long base = 0;
+        if (lane == 31 && incl)
+            base = atomicAdd(frag_counter(b), incl);
+        base = __shfl_sync(0xFFFFFFFFu, base, 31);
+        FragVisitor vis{b, &it, 0u, 0ull, 0ull, base + incl - cnt.n};
+        walk(vis);
+        if (!clip)
+            vis.drawn_n = 0; // the set-up counted it
         acc.add(b, item, vis.drawn_n, vis.fragments, i < n + nc);
     }
     acc.flush(b);
 }
 
+// The binned long spans of the capture, one warp each: the qpixel chain as in
+// k_spans, then every lane stores its pixel's fragment.
+__global__ void __launch_bounds__(256) k_frag_spans(const BatchDev *b)
+{
+    if (frags_overflowed(b))
+        return;
+    const uint32_t n_raw = *counter32(b, C_SPANS);
+    const uint32_t n = n_raw < b->span_cap ? n_raw : b->span_cap;
+    const ItemDev &it = b->items[0];
+    const ViewDev &v = it.v;
+    Frag *pool = b->frags;
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = warp; i < n; i += n_warps) {
+        const SpanRec r = b->spans[i];
+        const int y = (int)(r.y_bits & kYMask);
+        uint32_t *head = it.frag_head + ((long long)(y - v.y) * v.w - v.x);
+        const float fb = __uint_as_float(r.y_bits & ~kYMask);
+        float top = r.top, bottom = r.bottom;
+        for (int x0 = r.x1; x0 < r.x2; x0 += 32) {
+            float mt = top, mb = bottom;
+#pragma unroll
+            for (int k = 0; k < 32; k++) {
+                if (k == lane) {
+                    mt = top;
+                    mb = bottom;
+                }
+                top = top + r.tstep;
+                bottom = bottom + r.bstep;
+            }
+            const int x = x0 + lane;
+            if (x >= r.x2)
+                continue;
+            const float alpha = mt / mb;
+            const float z = r.v0 + r.dv * alpha;
+            if (below_near(z) || __float_as_uint(z) >= kMaxZBits)
+                continue;
+            const uint32_t at = r.item + (uint32_t)(x - r.x1);
+            const uint32_t next = atomicExch(head + x, at);
+            reinterpret_cast<float4 *>(pool + at)[0] = make_float4(alpha, r.progL, r.progR, fb);
+            reinterpret_cast<uint4 *>(pool + at)[1] = make_uint4(__float_as_uint(z), r.slot, next, 0u);
+        }
+    }
+}
+
 // The colour of a captured fragment.
+template <bool ALL_MODES>
 __device__ __forceinline__ uint32_t shade_frag(const BatchDev *b, const ItemDev &it, uint32_t item, uint32_t slot,
                                                float4 rec)
 {
@@ -1814,80 +1930,129 @@ __device__ __forceinline__ uint32_t shade_frag(const BatchDev *b, const ItemDev 
     if (ri == kRecClip)
         return shade_clip_rec(it, slot, rec);
     const uint4 *q = reinterpret_cast<const uint4 *>(b->recs + ri);
-    return shade_rec<true>(it, q[7], q[6].y, rec);
+    return shade_rec<ALL_MODES>(it, q[7], q[6].y, rec);
 }
 
-// Per pixel: the opaque winner to the screen and the depth buffer, the
-// transparent layers in front of it merged into the first one
+// One pixel with fragments: the opaque winner to the screen and the depth
+// buffer, the transparent layers in front of it merged into the first one
 // (viewport_t::flatten(front, back), viewport.cpp:43-51).
-__global__ void __launch_bounds__(128) k_layers(const BatchDev *b)
+template <bool ALL_MODES>
+__device__ __forceinline__ void resolve_pixel(const BatchDev *b, const ItemDev &it, uint32_t i)
+{
+    const int w = it.v.w, n_layers = it.layers;
+    const Frag *pool = b->frags;
+    const uint32_t head = it.frag_head[i];
+    uint32_t lz[SGL_MAX_LAYERS], ls[SGL_MAX_LAYERS], lc[SGL_MAX_LAYERS]; // kept, nearest first
+    int nt = 0;
+    uint32_t wz = kMaxZBits, wc = 0u;
+    unsigned long long prev = 0ull;
+    bool first = true;
+    for (;;) {
+        // the next fragment in (depth, draw order)
+        unsigned long long best = ~0ull;
+        uint32_t bi = kFragEnd;
+        for (uint32_t f = head; f != kFragEnd;) {
+            const uint4 m = reinterpret_cast<const uint4 *>(pool + f)[1];
+            const unsigned long long key = ((unsigned long long)m.x << 32) | m.y;
+            if ((first || key > prev) && key < best) {
+                best = key;
+                bi = f;
+            }
+            f = m.z;
+        }
+        if (bi == kFragEnd)
+            break;
+        first = false;
+        prev = best;
+        const uint32_t z = (uint32_t)(best >> 32), slot = (uint32_t)best;
+        const uint32_t c = shade_frag<ALL_MODES>(b, it, 0u, slot, reinterpret_cast<const float4 *>(pool + bi)[0]);
+        if ((c >> 24) == 255u) {
+            wz = z;
+            wc = c;
+            while (nt > 0 && lz[nt - 1] == z)
+                nt--; // not strictly in front
+            break;
+        }
+        if (nt == n_layers && (z > lz[nt - 1] || (z == lz[nt - 1] && slot < ls[nt - 1])))
+            continue; // farther than every kept layer
+        int k = nt < n_layers ? nt : n_layers - 1;
+        while (k > 0 && (lz[k - 1] > z || (lz[k - 1] == z && ls[k - 1] < slot))) {
+            lz[k] = lz[k - 1];
+            ls[k] = ls[k - 1];
+            lc[k] = lc[k - 1];
+            k--;
+        }
+        lz[k] = z;
+        ls[k] = slot;
+        lc[k] = c;
+        if (nt < n_layers)
+            nt++;
+    }
+    const int y = (int)(i / (uint32_t)w), x = (int)(i - (uint32_t)y * (uint32_t)w);
+    it.pixels[(long long)y * it.pitch_px + x] = wc; // 0 = viewport_t::clear's background
+    if (it.zbuf)
+        it.zbuf[i] = __uint_as_float(wz);
+    uint32_t l0 = nt > 0 ? lc[nt - 1] : 0u;
+    for (int k = 1; k < nt; k++) {
+        const uint32_t f = lc[nt - 1 - k];
+        if (f >> 24)
+            l0 = blend_px(l0, f);
+    }
+    it.layer0[i] = l0;
+}
+
+// Per pixel of the layered view: pixels without fragments get the background
+// at once, the others are queued in shared memory and resolved by full warps.
+template <bool ALL_MODES>
+__global__ void __launch_bounds__(256, 3) k_layers(const BatchDev *b)
 {
     if (frags_overflowed(b))
         return;
+    __shared__ uint32_t queue[2 * 256];
+    __shared__ int qn;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0)
+        qn = 0;
+    __syncthreads();
     const ItemDev &it = b->items[0];
-    const int w = it.v.w, n_layers = it.layers;
+    const int w = it.v.w;
     const uint32_t total = (uint32_t)w * (uint32_t)it.v.h;
-    const Frag *pool = b->frags;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const uint32_t head = it.frag_head[i];
-        uint32_t lz[SGL_MAX_LAYERS], ls[SGL_MAX_LAYERS], lc[SGL_MAX_LAYERS]; // kept, nearest first
-        int nt = 0;
-        uint32_t wz = kMaxZBits, wc = 0u;
-        unsigned long long prev = 0ull;
-        bool first = true;
-        for (;;) {
-            // the next fragment in (depth, draw order)
-            unsigned long long best = ~0ull;
-            uint32_t bi = kFragEnd;
-            for (uint32_t f = head; f != kFragEnd;) {
-                const uint4 m = reinterpret_cast<const uint4 *>(pool + f)[1];
-                const unsigned long long key = ((unsigned long long)m.x << 32) | m.y;
-                if ((first || key > prev) && key < best) {
-                    best = key;
-                    bi = f;
-                }
-                f = m.z;
+    for (uint32_t c0 = blockIdx.x * 256u; c0 < total; c0 += gridDim.x * 256u) {
+        const uint32_t i = c0 + threadIdx.x;
+        bool busy = false;
+        if (i < total) {
+            if (it.frag_head[i] == kFragEnd) {
+                const int y = (int)(i / (uint32_t)w), x = (int)(i - (uint32_t)y * (uint32_t)w);
+                it.pixels[(long long)y * it.pitch_px + x] = 0u; // viewport_t::clear's background
+                if (it.zbuf)
+                    it.zbuf[i] = __uint_as_float(kMaxZBits);
+                it.layer0[i] = 0u;
+            } else {
+                busy = true;
             }
-            if (bi == kFragEnd)
-                break;
-            first = false;
-            prev = best;
-            const uint32_t z = (uint32_t)(best >> 32), slot = (uint32_t)best;
-            const uint32_t c = shade_frag(b, it, 0u, slot, reinterpret_cast<const float4 *>(pool + bi)[0]);
-            if ((c >> 24) == 255u) {
-                wz = z;
-                wc = c;
-                while (nt > 0 && lz[nt - 1] == z)
-                    nt--; // not strictly in front
-                break;
-            }
-            if (nt == n_layers && (z > lz[nt - 1] || (z == lz[nt - 1] && slot < ls[nt - 1])))
-                continue; // farther than every kept layer
-            int k = nt < n_layers ? nt : n_layers - 1;
-            while (k > 0 && (lz[k - 1] > z || (lz[k - 1] == z && ls[k - 1] < slot))) {
-                lz[k] = lz[k - 1];
-                ls[k] = ls[k - 1];
-                lc[k] = lc[k - 1];
-                k--;
-            }
-            lz[k] = z;
-            ls[k] = slot;
-            lc[k] = c;
-            if (nt < n_layers)
-                nt++;
         }
-        const int y = (int)(i / (uint32_t)w), x = (int)(i - (uint32_t)y * (uint32_t)w);
-        it.pixels[(long long)y * it.pitch_px + x] = wc; // 0 = viewport_t::clear's background
-        if (it.zbuf)
-            it.zbuf[i] = __uint_as_float(wz);
-        uint32_t l0 = nt > 0 ? lc[nt - 1] : 0u;
-        for (int k = 1; k < nt; k++) {
-            const uint32_t f = lc[nt - 1 - k];
-            if (f >> 24)
-                l0 = blend_px(l0, f);
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, busy);
+        int wb = 0;
+        if (lane == 0 && m)
+            wb = atomicAdd(&qn, __popc(m));
+        wb = __shfl_sync(0xFFFFFFFFu, wb, 0);
+        if (busy)
+            queue[wb + __popc(m & ((1u << lane) - 1u))] = i;
+        __syncthreads();
+        const int have = qn;
+        if (have >= 256) {
+            resolve_pixel<ALL_MODES>(b, it, queue[threadIdx.x]);
+            __syncthreads();
+            if ((int)threadIdx.x < have - 256)
+                queue[threadIdx.x] = queue[256 + threadIdx.x];
+            __syncthreads();
+            if (threadIdx.x == 0)
+                qn = have - 256;
         }
-        it.layer0[i] = l0;
+        __syncthreads();
     }
+    if ((int)threadIdx.x < qn)
+        resolve_pixel<ALL_MODES>(b, it, queue[threadIdx.x]);
 }
 
 // viewport_t::flatten(front) (viewport.cpp:53-79): view pixel (x, y) reads
@@ -2037,9 +2202,13 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
             mark(k);
         mark(PK_FRAGS);
         k_frags<<<sms * 8, 256, 0, st>>>(b);
+        k_frag_spans<<<sms * 4, 256, 0, st>>>(b);
         ran(PK_FRAGS);
         mark(PK_LAYERS);
-        k_layers<<<sms * 16, 128, 0, st>>>(b);
+        if (flags & kSeqShaders)
+            k_layers<true><<<sms * 3, 256, 0, st>>>(b);
+        else
+            k_layers<false><<<sms * 3, 256, 0, st>>>(b);
         ran(PK_LAYERS);
         mark(PK_FLATTEN);
         k_flatten<<<sms * 8, 256, 0, st>>>(b);
@@ -2047,7 +2216,7 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
         mark(PK_COPY);
         k_copy_layer<<<sms * 8, 256, 0, st>>>(b);
         ran(PK_COPY);
-        n += 4;
+        n += 5;
         if (timed) {
             cudaEventRecord(prof->ev[kProfKernels], st);
             prof->pending = true;
