@@ -341,6 +341,37 @@ SGL_API sgl_status sgl_profile(sgl_ctx *ctx, int enable);
 SGL_API sgl_status sgl_profile_read(sgl_ctx *ctx, int kernel, const char **name, double *total_ms,
                                     uint64_t *launches);
 
+/* ------------------------------------------------------------ glTF scenes -- */
+
+/* swegl::load_scene (src/data/gltf.cpp:388-464): a .gltf file (JSON whose
+ * buffers and images are files next to it, or base64 data URIs) or a .glb
+ * file read into host memory as a scene description, with the reference
+ * loader's rules (see the notes of swegl_gb300/csrc/sgl_gltf.cpp): images
+ * decoded (BMP, PNG; src/misc/image.cpp:20-172), animations kept for
+ * sgl_gltf_animate.  Host only: no context or device is needed.  On failure
+ * `error` (if given) receives a message. */
+typedef struct sgl_gltf sgl_gltf;
+SGL_API sgl_status sgl_gltf_load(const char *path, sgl_gltf **out, char *error, size_t error_size);
+/* The scene description, valid until sgl_gltf_free; its nodes follow the
+ * animations.  Like a loaded scene_t it has no lights (ambient, sun and
+ * point lights zero): set them on a copy before sgl_scene_upload. */
+SGL_API const sgl_scene_desc *sgl_gltf_scene(const sgl_gltf *g);
+SGL_API int                   sgl_gltf_animation_count(const sgl_gltf *g);
+/* scene_t::animate(seconds) (swegl/data/model.hpp:146-177): every animation
+ * at `seconds` modulo its length, keyframes interpolated linearly, rotations
+ * normalised; the nodes' scale, rotation and translation are updated and,
+ * if `nodes` is given, all sgl_gltf_scene()->n_nodes of them written there
+ * for sgl_scene_set_nodes. */
+SGL_API sgl_status sgl_gltf_animate(sgl_gltf *g, float seconds, sgl_node_desc *nodes);
+SGL_API void       sgl_gltf_free(sgl_gltf *g);
+
+/* read_image_file (src/misc/image.cpp:20-27): a BMP or PNG file (chosen by
+ * its extension) decoded to 0xAARRGGBB texels, row 0 first; free them with
+ * sgl_image_free. */
+SGL_API sgl_status sgl_image_load(const char *path, uint32_t **texels, int *width, int *height, char *error,
+                                  size_t error_size);
+SGL_API void       sgl_image_free(uint32_t *texels);
+
 #ifdef __cplusplus
 }
 #endif

@@ -303,6 +303,12 @@ struct scene_t {
     std::vector<point_source_light> point_source_lights;
     std::vector<material_t> materials;
     std::vector<texture_t> images;
+    // the animations of a scene from load_scene (scene_t::animations)
+    std::shared_ptr<sgl_gltf> animation_source;
+
+    // scene_t::animate (model.hpp:146-177): the nodes' scale, rotation and
+    // translation at `elapsed_seconds`, for scenes from load_scene.
+    inline void animate(float elapsed_seconds);
 };
 
 // -------------------------------------------------------- procedural meshes --
@@ -702,6 +708,90 @@ inline void invalidate(const scene_t &s)
 }
 
 } // namespace gpu
+
+// load_scene (src/data/gltf.cpp:455-464): a .gltf or .glb file through the
+// library's loader (sgl_gltf_load, which follows the reference loader's
+// rules); like the reference's, the scene has no lights.
+inline scene_t load_scene(const std::string &filename)
+{
+    sgl_gltf *g = nullptr;
+    char err[512] = {0};
+    const sgl_status st = sgl_gltf_load(filename.c_str(), &g, err, sizeof err);
+    if (st != SGL_OK)
+        throw render_error(st, err);
+    std::shared_ptr<sgl_gltf> hold(g, sgl_gltf_free);
+    const sgl_scene_desc &d = *sgl_gltf_scene(g);
+    scene_t s;
+    s.nodes.resize((size_t)d.n_nodes);
+    for (int i = 0; i < d.n_nodes; i++) {
+        const sgl_node_desc &nd = d.nodes[i];
+        node_t &n = s.nodes[(size_t)i];
+        n.scale = vertex_t(nd.scale[0], nd.scale[1], nd.scale[2]);
+        for (int k = 0; k < 16; k++)
+            n.rotation[k / 4][k % 4] = nd.rotation[k];
+        n.translation = vertex_t(nd.translation[0], nd.translation[1], nd.translation[2]);
+    }
+    for (int i = 0; i < d.n_nodes; i++) {
+        const int p = d.nodes[i].parent;
+        if (p >= 0) {
+            s.nodes[(size_t)p].children_idx.push_back(i);
+            s.nodes[(size_t)i].root = false;
+        }
+    }
+    for (int i = 0; i < d.n_nodes; i++)
+        if (s.nodes[(size_t)i].root)
+            s.root_nodes.push_back(i);
+    for (int k = 0; k < d.n_primitives; k++) {
+        const sgl_primitive_desc &pd = d.primitives[k];
+        primitive_t pr;
+        pr.mode = (primitive_t::index_mode_t)pd.mode;
+        pr.material_id = pd.material;
+        pr.vertices.resize(pd.vertex_count);
+        for (uint32_t v = 0; v < pd.vertex_count; v++) {
+            const size_t g3 = 3 * (size_t)(pd.vertex_offset + v), g2 = 2 * (size_t)(pd.vertex_offset + v);
+            mesh_vertex_t &mv = pr.vertices[v];
+            mv.v = vertex_t(d.positions[g3], d.positions[g3 + 1], d.positions[g3 + 2]);
+            mv.normal.x() = d.normals[g3]; // as loaded, not normalised (gltf.cpp:170-174)
+            mv.normal.y() = d.normals[g3 + 1];
+            mv.normal.z() = d.normals[g3 + 2];
+            mv.tex_coords = vec2f_t(d.uvs[g2], d.uvs[g2 + 1]);
+        }
+        pr.indices.assign(d.indices + pd.index_offset, d.indices + pd.index_offset + pd.index_count);
+        s.nodes[(size_t)pd.node].primitives.push_back(std::move(pr));
+    }
+    for (int m = 0; m < d.n_materials; m++) {
+        material_t mt;
+        mt.color = pixel_colors((unsigned int)d.materials[m].color);
+        mt.texture_idx = d.materials[m].texture;
+        mt.double_sided = d.materials[m].double_sided != 0;
+        mt.shininess = d.materials[m].shininess;
+        s.materials.push_back(mt);
+    }
+    for (int t = 0; t < d.n_textures; t++) {
+        const sgl_texture_desc &td = d.textures[t];
+        unsigned int *copy = new unsigned int[(size_t)td.width * td.height];
+        std::memcpy(copy, td.texels, sizeof(unsigned int) * (size_t)td.width * td.height);
+        s.images.emplace_back(copy, td.width, td.height);
+    }
+    s.animation_source = std::move(hold);
+    return s;
+}
+
+inline void scene_t::animate(float elapsed_seconds)
+{
+    if (!animation_source)
+        return;
+    std::vector<sgl_node_desc> nd(nodes.size());
+    const sgl_status st = sgl_gltf_animate(animation_source.get(), elapsed_seconds, nd.data());
+    if (st != SGL_OK)
+        throw render_error(st, "sgl_gltf_animate");
+    for (size_t i = 0; i < nodes.size() && i < nd.size(); i++) {
+        nodes[i].scale = vertex_t(nd[i].scale[0], nd[i].scale[1], nd[i].scale[2]);
+        for (int k = 0; k < 16; k++)
+            nodes[i].rotation[k / 4][k % 4] = nd[i].rotation[k];
+        nodes[i].translation = vertex_t(nd[i].translation[0], nd[i].translation[1], nd[i].translation[2]);
+    }
+}
 
 // render(scene, vp...) (swegl/render/renderer.hpp:27-34): the world transform
 // once, then every viewport in order.

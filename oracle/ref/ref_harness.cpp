@@ -20,6 +20,12 @@
  *   kind 4  the bilinear texel colour alone
  * Kind 0 renders with the reference shader the view's `shader` field names
  * (SGL_SHADER_*, include/sgl.h).
+ *
+ * Also exported: matrix44_t::from_quaternion
+ * (swegl/projection/matrix44.hpp:34-43) and scene_t::animate
+ * (swegl/data/model.hpp:146-177) on flat inputs, which pin the glTF node and
+ * animation arithmetic of the restatement (the reference's glTF parser
+ * itself needs the un-vendored nlohmann/json and is not built).
  */
 #include <cstring>
 #include <memory>
@@ -241,6 +247,64 @@ __attribute__((visibility("default"))) int ref_render(const sgl_scene_desc *desc
             else
                 triangle_calls[i] = 0;
         }
+    }
+    return 0;
+}
+
+
+/* matrix44_t::from_quaternion(q[0], q[1], q[2], q[3]), row-major into out[16]. */
+__attribute__((visibility("default"))) void ref_from_quaternion(const float *q, float *out)
+{
+    const swegl::matrix44_t m = swegl::matrix44_t::from_quaternion(q[0], q[1], q[2], q[3]);
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+            out[4 * i + j] = m[i][j];
+}
+
+/* scene_t::animate(seconds) on `nodes` (scale, rotation, translation are
+ * read and written back).  Animation a has channels
+ * [ch_first[a], ch_first[a + 1]); channel c targets node ch_node[c] on path
+ * ch_path[c] (0 scale, 1 rotation, 2 translation, 3 other) with keyframes
+ * [st_first[c], st_first[c + 1]) of times `times` and 4-float `values`, in
+ * the order given (the loader sorts them by time).  Each animation's end
+ * time is the largest last keyframe time of its channels (gltf.cpp:381). */
+__attribute__((visibility("default"))) int ref_animate(sgl_node_desc *nodes, int n_nodes, int n_anims,
+                                                       const int *ch_first, const int *ch_node,
+                                                       const int *ch_path, const int *st_first,
+                                                       const float *times, const float *values, float seconds)
+{
+    swegl::scene_t s;
+    s.nodes.resize(n_nodes);
+    for (int i = 0; i < n_nodes; i++) {
+        s.nodes[i].scale = swegl::vertex_t(nodes[i].scale[0], nodes[i].scale[1], nodes[i].scale[2]);
+        s.nodes[i].rotation = to_matrix(nodes[i].rotation);
+        s.nodes[i].translation =
+            swegl::vertex_t(nodes[i].translation[0], nodes[i].translation[1], nodes[i].translation[2]);
+    }
+    for (int a = 0; a < n_anims; a++) {
+        swegl::animation_t &an = s.animations.emplace_back();
+        for (int c = ch_first[a]; c < ch_first[a + 1]; c++) {
+            if (ch_node[c] < 0 || ch_node[c] >= n_nodes || st_first[c + 1] <= st_first[c])
+                return -1;
+            swegl::animation_channel_t ch{ch_node[c], (swegl::animation_channel_t::path_t)ch_path[c], {}};
+            for (int k = st_first[c]; k < st_first[c + 1]; k++)
+                ch.steps.push_back(swegl::animation_step_t{
+                    times[k], swegl::vec4f_t(values[4 * k], values[4 * k + 1], values[4 * k + 2], values[4 * k + 3])});
+            an.end_time = std::max(an.end_time, ch.steps.back().time);
+            an.channels.push_back(std::move(ch));
+        }
+    }
+    s.animate(seconds);
+    for (int i = 0; i < n_nodes; i++) {
+        nodes[i].scale[0] = s.nodes[i].scale.x();
+        nodes[i].scale[1] = s.nodes[i].scale.y();
+        nodes[i].scale[2] = s.nodes[i].scale.z();
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++)
+                nodes[i].rotation[4 * r + c] = s.nodes[i].rotation[r][c];
+        nodes[i].translation[0] = s.nodes[i].translation.x();
+        nodes[i].translation[1] = s.nodes[i].translation.y();
+        nodes[i].translation[2] = s.nodes[i].translation.z();
     }
     return 0;
 }

@@ -18,7 +18,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libsgl.so")
 
-SOURCES = ["raster.cu", "sgl_api.cpp", "sgl_scene.cpp", "sgl_lane.cpp", "sgl_serve.cpp", "noalloc.cu"]
+SOURCES = ["raster.cu", "sgl_api.cpp", "sgl_scene.cpp", "sgl_lane.cpp", "sgl_serve.cpp", "noalloc.cu", "sgl_gltf.cpp",
+           "sgl_image.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -67,6 +67,14 @@ def library() -> C.CDLL:
             "sgl_server_destroy": ([C.c_void_p], None),
             "sgl_server_stats": ([C.c_void_p, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)], C.c_int),
             "sgl_profile_read": ([C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_uint64)], C.c_int),
+            "sgl_gltf_load": ([C.c_char_p, P(C.c_void_p), C.c_char_p, C.c_size_t], C.c_int),
+            "sgl_gltf_scene": ([C.c_void_p], P(abi.SceneDesc)),
+            "sgl_gltf_animation_count": ([C.c_void_p], C.c_int),
+            "sgl_gltf_animate": ([C.c_void_p, C.c_float, P(abi.NodeDesc)], C.c_int),
+            "sgl_gltf_free": ([C.c_void_p], None),
+            "sgl_image_load": ([C.c_char_p, P(P(C.c_uint32)), P(C.c_int), P(C.c_int), C.c_char_p, C.c_size_t],
+                               C.c_int),
+            "sgl_image_free": ([P(C.c_uint32)], None),
         }
         for name, (args, res) in sigs.items():
             fn = getattr(lib, name)

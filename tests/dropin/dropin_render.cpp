@@ -2,8 +2,10 @@
 // exactly as swegl code would: scene_t, viewport_t on one SDL surface, and
 // swegl::render(scene, vp0, vp1, ...).  Used by tests/test_gpu_dropin.py.
 //
-// usage: dropin_render <scene dump> <output>
-// Output: the surface (h * w uint32), then each view's z-buffer.
+// usage: dropin_render <scene dump> <output> [<scene.gltf|.glb> <seconds>]
+// Output: the surface (h * w uint32), then each view's z-buffer.  With a glTF
+// file the scene is swegl::load_scene(file) animated to <seconds>
+// (scene_t::animate), with the dump's lights; the dump's geometry is unused.
 #include <cstdio>
 #include <cstdlib>
 #include <memory>
@@ -56,7 +58,7 @@ std::shared_ptr<swegl::pixel_shader_t> make_shader(int mode)
 
 int main(int argc, char **argv)
 {
-    if (argc != 3)
+    if (argc != 3 && argc != 5)
         return 2;
     FILE *in = fopen(argv[1], "rb");
     if (!in)
@@ -132,6 +134,20 @@ int main(int argc, char **argv)
     scene.sun_direction.y() = sun[1];
     scene.sun_direction.z() = sun[2];
     scene.sun_intensity = r.get<float>();
+    if (argc == 5) {
+        try {
+            swegl::scene_t loaded = swegl::load_scene(argv[3]);
+            loaded.point_source_lights = scene.point_source_lights;
+            loaded.ambient_light_intensity = scene.ambient_light_intensity;
+            loaded.sun_direction = scene.sun_direction;
+            loaded.sun_intensity = scene.sun_intensity;
+            loaded.animate((float)atof(argv[4]));
+            scene = std::move(loaded);
+        } catch (const swegl::render_error &e) {
+            fprintf(stderr, "load_scene %d: %s\n", e.status, e.what());
+            return 3;
+        }
+    }
     const int n_views = r.get<int>();
     const int sw = r.get<int>(), sh = r.get<int>();
     std::vector<uint32_t> pixels((size_t)sw * sh, 0);

@@ -1,0 +1,307 @@
+"""Writers of synthetic glTF / GLB scenes and PNG / BMP images for the
+loader tests (no third-party encoder is available: PNG uses the standard
+library's zlib, the rest is plain packing)."""
+from __future__ import annotations
+
+import base64
+import json
+import math
+import os
+import struct
+import zlib
+
+import numpy as np
+
+# --------------------------------------------------------------------- PNG --
+ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
+
+
+def _chunk(kind: bytes, body: bytes) -> bytes:
+    return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
+
+
+def _pack_row(samples: np.ndarray, depth: int) -> bytes:
+    """One row of samples (already interleaved by channel) at `depth` bits."""
+    if depth == 16:
+        return samples.astype(">u2").tobytes()
+    if depth == 8:
+        return samples.astype(np.uint8).tobytes()
+    per = 8 // depth
+    n = len(samples)
+    out = bytearray((n * depth + 7) // 8)
+    for i, v in enumerate(samples):
+        out[i // per] |= (int(v) & ((1 << depth) - 1)) << (8 - depth * (i % per + 1))
+    return bytes(out)
+
+
+def _paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    if pa <= pb and pa <= pc:
+        return a
+    return b if pb <= pc else c
+
+
+def _filter(rows, bpp, rng):
+    out = bytearray()
+    prev = bytes(len(rows[0])) if rows else b""
+    for row in rows:
+        f = int(rng.integers(0, 5))
+        fr = bytearray(len(row))
+        for i in range(len(row)):
+            a = row[i - bpp] if i >= bpp else 0
+            b = prev[i]
+            c = prev[i - bpp] if i >= bpp else 0
+            pred = [0, a, b, (a + b) >> 1, _paeth(a, b, c)][f]
+            fr[i] = (row[i] - pred) & 0xFF
+        out += bytes([f]) + fr
+        prev = row
+    return bytes(out)
+
+
+def encode_png(samples: np.ndarray, ctype: int, depth: int, interlace: bool = False, palette=None, trns=None,
+               seed: int = 0) -> bytes:
+    """samples: (h, w, channels) integers at `depth`; rows filtered with
+    random filter types."""
+    h, w, ch = samples.shape
+    rng = np.random.default_rng(seed)
+    bpp = max(1, ch * depth // 8)
+    raw = b""
+    passes = ADAM7 if interlace else [(0, 0, 1, 1)]
+    for (x0, y0, dx, dy) in passes:
+        sub = samples[y0::dy, x0::dx]
+        if sub.size == 0:
+            continue
+        rows = [_pack_row(sub[y].reshape(-1), depth) for y in range(sub.shape[0])]
+        raw += _filter(rows, bpp, rng)
+    out = b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, 1 if interlace else 0))
+    if palette is not None:
+        out += _chunk(b"PLTE", bytes(np.asarray(palette, np.uint8).reshape(-1)))
+    if trns is not None:
+        out += _chunk(b"tRNS", bytes(trns))
+    comp = zlib.compress(raw, 6)
+    # split the stream over two IDAT chunks
+    out += _chunk(b"IDAT", comp[:len(comp) // 2]) + _chunk(b"IDAT", comp[len(comp) // 2:])
+    return out + _chunk(b"IEND", b"")
+
+
+def png_expected(samples, ctype, depth, palette=None, trns=None) -> np.ndarray:
+    """The texels libpng's transforms in read_png_file give (image.cpp:119-166):
+    8-bit RGBA, 16-bit samples to their high byte, low-depth grey scaled up,
+    tRNS to alpha, grey replicated; then 0xAARRGGBB."""
+    s = samples.astype(np.uint32)
+    h, w, _ = s.shape
+
+    def to8(v):
+        return {1: v * 255, 2: v * 85, 4: v * 17, 8: v, 16: v >> 8}[depth]
+
+    a = np.full((h, w), 255, np.uint32)
+    if ctype == 3:
+        pal = np.asarray(palette, np.uint32)
+        rgb = pal[s[..., 0]]
+        if trns is not None:
+            ta = np.full(len(pal), 255, np.uint32)
+            ta[:len(trns)] = list(trns)
+            a = ta[s[..., 0]]
+        r, g, b = rgb[..., 0], rgb[..., 1], rgb[..., 2]
+    elif ctype in (0, 4):
+        r = g = b = to8(s[..., 0])
+        if ctype == 4:
+            a = to8(s[..., 1])
+        elif trns is not None:
+            key = (trns[0] << 8) | trns[1]
+            a = np.where(s[..., 0] == key, 0, 255).astype(np.uint32)
+    else:
+        r, g, b = to8(s[..., 0]), to8(s[..., 1]), to8(s[..., 2])
+        if ctype == 6:
+            a = to8(s[..., 3])
+        elif trns is not None:
+            kr, kg, kb = (trns[0] << 8) | trns[1], (trns[2] << 8) | trns[3], (trns[4] << 8) | trns[5]
+            a = np.where((s[..., 0] == kr) & (s[..., 1] == kg) & (s[..., 2] == kb), 0, 255).astype(np.uint32)
+    return ((a << 24) | (r << 16) | (g << 8) | b).astype(np.uint32)
+
+
+# --------------------------------------------------------------------- BMP --
+def encode_bmp(rgb: np.ndarray) -> bytes:
+    """A standard bottom-up 24-bit BMP (rows padded to 4 bytes)."""
+    h, w, _ = rgb.shape
+    pad = (4 - (w * 3) % 4) % 4
+    body = b""
+    for y in range(h - 1, -1, -1):
+        body += rgb[y, :, ::-1].astype(np.uint8).tobytes() + b"\0" * pad
+    hdr = struct.pack("<2sIHHI", b"BM", 54 + len(body), 0, 0, 54)
+    info = struct.pack("<IiiHHIIiiII", 40, w, h, 1, 24, 0, len(body), 2835, 2835, 0, 0)
+    return hdr + info + body
+
+
+# -------------------------------------------------------------------- glTF --
+class GltfBuilder:
+    """Accumulates buffer views and accessors in one binary buffer."""
+
+    def __init__(self):
+        self.bin = bytearray()
+        self.j = {"asset": {"version": "2.0"}, "bufferViews": [], "accessors": [], "meshes": [], "nodes": [],
+                  "materials": [], "textures": [], "images": [], "animations": []}
+
+    def view(self, data: bytes, stride: int = 0) -> int:
+        while len(self.bin) % 4:
+            self.bin += b"\0"
+        bv = {"buffer": 0, "byteOffset": len(self.bin), "byteLength": len(data)}
+        if stride:
+            bv["byteStride"] = stride
+        self.bin += data
+        self.j["bufferViews"].append(bv)
+        return len(self.j["bufferViews"]) - 1
+
+    def accessor(self, arr: np.ndarray, ctype: int, typ: str, stride: int = 0, offset: int = 0) -> int:
+        data = np.ascontiguousarray(arr).tobytes()
+        if stride:
+            # interleave: element i at i * stride
+            esz = arr.dtype.itemsize * (arr.shape[1] if arr.ndim > 1 else 1)
+            buf = bytearray(stride * len(arr))
+            for i in range(len(arr)):
+                buf[i * stride:i * stride + esz] = np.ascontiguousarray(arr[i]).tobytes()
+            data = bytes(buf)
+        bvi = self.view(b"\0" * offset + data, stride)
+        a = {"bufferView": bvi, "componentType": ctype, "count": len(arr), "type": typ}
+        if offset:
+            a["byteOffset"] = offset
+        self.j["accessors"].append(a)
+        return len(self.j["accessors"]) - 1
+
+    def write(self, path: str, glb: bool, external_bin: bool = False):
+        j = dict(self.j)
+        j = {k: v for k, v in j.items() if v != []}
+        if glb:
+            j["buffers"] = [{"byteLength": len(self.bin)}]
+            js = json.dumps(j).encode()
+            js += b" " * ((4 - len(js) % 4) % 4)
+            binb = bytes(self.bin) + b"\0" * ((4 - len(self.bin) % 4) % 4)
+            total = 12 + 8 + len(js) + 8 + len(binb)
+            out = struct.pack("<4sII", b"glTF", 2, total) + struct.pack("<I4s", len(js), b"JSON") + js
+            out += struct.pack("<I4s", len(binb), b"BIN\0") + binb
+            with open(path, "wb") as fh:
+                fh.write(out)
+        else:
+            if external_bin:
+                name = os.path.splitext(os.path.basename(path))[0] + ".bin"
+                with open(os.path.join(os.path.dirname(path), name), "wb") as fh:
+                    fh.write(bytes(self.bin))
+                j["buffers"] = [{"byteLength": len(self.bin), "uri": name}]
+            else:
+                j["buffers"] = [{"byteLength": len(self.bin),
+                                 "uri": "data:application/octet-stream;base64," + base64.b64encode(bytes(self.bin)).decode()}]
+            with open(path, "w") as fh:
+                json.dump(j, fh)
+
+
+def quat(axis, angle):
+    ax = np.asarray(axis, np.float64)
+    ax = ax / np.linalg.norm(ax)
+    s = math.sin(angle / 2)
+    return [float(ax[0] * s), float(ax[1] * s), float(ax[2] * s), float(math.cos(angle / 2))]
+
+
+def _cube(size):
+    from swegl_gb300 import scenes as S
+
+    return S.cube_mesh(size)
+
+
+def build_test_scene(dirpath: str, glb: bool, seed: int = 3) -> str:
+    """A scene exercising the loader: a node hierarchy with TRS, quaternion
+    and matrix nodes; fans, strips and lists with 16- and 32-bit indices and
+    an interleaved vertex buffer; a mesh without primitives and a mesh used
+    twice; materials with and without pbrMetallicRoughness, base colours,
+    double sides and textures (a PNG in a buffer view or as a data URI, an
+    external PNG and BMP); translation, rotation and scale animations."""
+    from swegl_gb300 import scenes as S
+
+    rng = np.random.default_rng(seed)
+    g = GltfBuilder()
+    # images
+    tex_a = rng.integers(0, 256, size=(32, 48, 4)).astype(np.uint8)
+    tex_a[..., 3] = 255
+    png_a = encode_png(tex_a, 6, 8, seed=1)
+    tex_b = rng.integers(0, 256, size=(16, 16, 3)).astype(np.uint8)
+    png_b = encode_png(tex_b, 2, 8, interlace=True, seed=2)
+    tex_c = rng.integers(0, 256, size=(8, 10, 3)).astype(np.uint8)
+    with open(os.path.join(dirpath, "tex_c.bmp"), "wb") as fh:
+        fh.write(encode_bmp(tex_c))
+    with open(os.path.join(dirpath, "tex_b.png"), "wb") as fh:
+        fh.write(png_b)
+    if glb:
+        g.j["images"].append({"bufferView": g.view(png_a), "mimeType": "image/png"})
+    else:
+        g.j["images"].append({"uri": "data:image/png;base64," + base64.b64encode(png_a).decode()})
+    g.j["images"].append({"uri": "tex_b.png"})
+    g.j["images"].append({"uri": "tex_c.bmp"})
+    g.j["textures"] = [{"source": 2}, {"source": 0}, {"source": 1}]
+    g.j["materials"] = [
+        {"pbrMetallicRoughness": {"baseColorTexture": {"index": 1}}},
+        {"pbrMetallicRoughness": {"baseColorFactor": [0.8, 0.3, 0.1, 1.0]}, "doubleSided": True},
+        {"doubleSided": True},  # no pbr: white, single-sided
+        {"pbrMetallicRoughness": {"baseColorTexture": {"index": 2}, "metallicFactor": 0.5}, "doubleSided": True},
+        {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}, "roughnessFactor": 0.2}},
+    ]
+    meshes = []
+    # mesh 0: the cube's six fans, 16-bit indices
+    prims = []
+    for k, (p, n, t, i) in enumerate(_cube(1.2)):
+        prims.append({"attributes": {"POSITION": g.accessor(p, 5126, "VEC3"), "NORMAL": g.accessor(n, 5126, "VEC3"),
+                                     "TEXCOORD_0": g.accessor(t, 5126, "VEC2")},
+                      "indices": g.accessor(i.astype(np.uint16), 5123, "SCALAR"), "mode": 6, "material": k % 2 * 4})
+    meshes.append({"primitives": prims})
+    meshes.append({"name": "empty"})  # no primitives: skipped when meshes are numbered
+    # mesh 2 (loader index 1): a UV sphere as strips, 32-bit indices, interleaved positions
+    prims = []
+    for (p, n, t, i) in S.uv_sphere_mesh(12, 6, 0.6):
+        prims.append({"attributes": {"POSITION": g.accessor(p, 5126, "VEC3", stride=24),
+                                     "NORMAL": g.accessor(n, 5126, "VEC3", offset=8),
+                                     "TEXCOORD_0": g.accessor(t, 5126, "VEC2")},
+                      "indices": g.accessor(i.astype(np.uint32), 5125, "SCALAR"), "mode": 5, "material": 3})
+    meshes.append({"primitives": prims})
+    # mesh 3 (loader index 2): random triangles, one list without normals, one without indices, one of lines
+    p = rng.uniform(-0.7, 0.7, size=(30, 3)).astype(np.float32)
+    t = rng.uniform(0, 1, size=(30, 2)).astype(np.float32)
+    meshes.append({"primitives": [
+        {"attributes": {"POSITION": g.accessor(p, 5126, "VEC3"), "TEXCOORD_0": g.accessor(t, 5126, "VEC2")},
+         "indices": g.accessor(np.arange(30, dtype=np.uint16)[::-1].copy(), 5123, "SCALAR"), "material": 1},
+        {"attributes": {"POSITION": g.accessor(p, 5126, "VEC3")}, "material": 0},
+        {"attributes": {"POSITION": g.accessor(p, 5126, "VEC3")}, "indices": g.accessor(np.arange(6, dtype=np.uint16), 5123, "SCALAR"),
+         "mode": 1},
+    ]})
+    # mesh 4 (loader index 3): a quad fan with the untextured no-pbr material
+    q = np.array([[-2, -2, -1.5], [2, -2, -1.5], [2, 2, -1.5], [-2, 2, -1.5]], np.float32)
+    meshes.append({"primitives": [{"attributes": {"POSITION": g.accessor(q, 5126, "VEC3"),
+                                                  "NORMAL": g.accessor(np.tile([[0, 0, 1]], (4, 1)).astype(np.float32), 5126, "VEC3")},
+                                   "indices": g.accessor(np.arange(4, dtype=np.uint16), 5123, "SCALAR"),
+                                   "mode": 6, "material": 2}]})
+    g.j["meshes"] = meshes
+    m = np.eye(4)
+    m[:3, :3] = np.diag([1.2, 0.8, 1.0]) @ np.array([[0.8, -0.6, 0], [0.6, 0.8, 0], [0, 0, 1]])
+    m[:3, 3] = [0.9, -0.4, 0.2]
+    g.j["nodes"] = [
+        {"children": [1, 2], "translation": [0.0, 0.1, -0.5], "rotation": quat([0, 1, 0], 0.4)},
+        {"mesh": 0, "translation": [-1.0, 0.0, 0.0], "scale": [1.0, 0.9, 1.1], "rotation": quat([1, 1, 0], 0.3)},
+        {"mesh": 1, "matrix": [float(v) for v in m.T.reshape(-1)], "children": [3]},
+        {"mesh": 2, "translation": [0.3, 0.6, 0.4]},
+        {"mesh": 0, "translation": [1.5, 1.5, 0.0]},  # mesh 0 again: no primitives
+        {"mesh": 3},
+    ]
+    times = np.array([0.0, 0.5, 1.25, 2.0], np.float32)
+    tr = np.array([[-1.0, 0, 0], [-1.2, 0.3, 0], [-0.8, -0.2, 0.1], [-1.0, 0, 0]], np.float32)
+    rot = np.array([quat([0, 1, 0], a) for a in (0.0, 1.0, 2.5, 0.2)], np.float32)
+    sc = np.array([[1, 1, 1], [1.3, 1.0, 0.7]], np.float32)
+    ti, tt, tr_, ts = (g.accessor(times, 5126, "SCALAR"), g.accessor(times[:2].copy(), 5126, "SCALAR"),
+                       g.accessor(rot, 5126, "VEC4"), g.accessor(sc, 5126, "VEC3"))
+    g.j["animations"] = [
+        {"samplers": [{"input": ti, "output": g.accessor(tr, 5126, "VEC3")}, {"input": ti, "output": tr_}],
+         "channels": [{"sampler": 0, "target": {"node": 1, "path": "translation"}},
+                      {"sampler": 1, "target": {"node": 3, "path": "rotation"}}]},
+        {"samplers": [{"input": tt, "output": ts}],
+         "channels": [{"sampler": 0, "target": {"node": 0, "path": "scale"}}]},
+    ]
+    path = os.path.join(dirpath, "scene.glb" if glb else "scene.gltf")
+    g.write(path, glb, external_bin=not glb and seed % 2 == 1)
+    return path
