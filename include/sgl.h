@@ -347,7 +347,7 @@ SGL_API sgl_status sgl_profile_read(sgl_ctx *ctx, int kernel, const char **name,
  * buffers and images are files next to it, or base64 data URIs) or a .glb
  * file read into host memory as a scene description, with the reference
  * loader's rules (see the notes of swegl_gb300/csrc/sgl_gltf.cpp): images
- * decoded (BMP, PNG; src/misc/image.cpp:20-172), animations kept for
+ * decoded (BMP, PNG, baseline JPEG; src/misc/image.cpp:20-265), animations kept for
  * sgl_gltf_animate.  Host only: no context or device is needed.  On failure
  * `error` (if given) receives a message. */
 typedef struct sgl_gltf sgl_gltf;
@@ -365,9 +365,9 @@ SGL_API int                   sgl_gltf_animation_count(const sgl_gltf *g);
 SGL_API sgl_status sgl_gltf_animate(sgl_gltf *g, float seconds, sgl_node_desc *nodes);
 SGL_API void       sgl_gltf_free(sgl_gltf *g);
 
-/* read_image_file (src/misc/image.cpp:20-27): a BMP or PNG file (chosen by
- * its extension) decoded to 0xAARRGGBB texels, row 0 first; free them with
- * sgl_image_free. */
+/* read_image_file (src/misc/image.cpp:20-27): a BMP, PNG or baseline JPEG
+ * file (chosen by its extension) decoded to 0xAARRGGBB texels, row 0 first;
+ * free them with sgl_image_free. */
 SGL_API sgl_status sgl_image_load(const char *path, uint32_t **texels, int *width, int *height, char *error,
                                   size_t error_size);
 SGL_API void       sgl_image_free(uint32_t *texels);

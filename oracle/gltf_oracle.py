@@ -12,12 +12,16 @@ Follows, in the reference (gbizzotto/swegl):
   vec4f_t::normalize                              swegl/projection/vec2f.hpp:67-77
   read_bmp_file                                   src/misc/image.cpp:29-83
   read_png_file (libpng's transforms)             src/misc/image.cpp:92-172
+  read_jpeg_file (libjpeg default decompression) src/misc/image.cpp:183-255
 Arithmetic is numpy float32 in the reference's order of operations.  The
 parser (nlohmann/json) is not vendored with the reference, so the loader
 cannot be compiled here: the loader restatement is pinned by the scenes it
 produces (rendered against the compiled reference's renderer) and its
 quaternion and animation arithmetic by the compiled reference's
-from_quaternion and scene_t::animate (oracle/ref/ref_harness.cpp).
+from_quaternion and scene_t::animate (oracle/ref/ref_harness.cpp).  PNG is
+lossless (any correct decoder gives libpng's texels); the JPEG pixel path
+restates libjpeg's published default decompression, and with libjpeg absent
+here its parity with libjpeg is unpinned.
 """
 from __future__ import annotations
 
@@ -392,3 +396,109 @@ def animate(result: GltfResult, seconds: float) -> None:
                 s.node_translation[node] = np.array(f[:3], np.float32)
             elif path == 0:
                 s.node_scale[node] = np.array(f[:3], np.float32)
+
+
+# ------------------------------------------------------------------ JPEG --
+def _idct_islow(coef: np.ndarray, q: np.ndarray) -> np.ndarray:
+    """libjpeg's accurate integer IDCT (jidctint.c, the LL&M flow graph in
+    13-bit fixed point; columns with 2 extra bits, then rows) of blocks
+    (..., 8, 8) of quantised coefficients; samples level-shifted and
+    clamped (values wrapped mod 1024 first, as its masked table lookup)."""
+    CB, P1 = 13, 2
+    F = dict(a=2446, b=3196, c=4433, d=6270, e=7373, f=9633, g=12299, h=15137, i=16069, j=16819, k=20995, l=25172)
+    x = coef.astype(np.int64) * q.astype(np.int64)
+
+    def flow(v, scale_shift, out_shift):
+        # v[..., n] for n = 0..7 along the transformed axis
+        z2, z3 = v[..., 2], v[..., 6]
+        z1 = (z2 + z3) * F["c"]
+        t2 = z1 + z3 * (-F["h"])
+        t3 = z1 + z2 * F["d"]
+        t0 = (v[..., 0] + v[..., 4]) << CB
+        t1 = (v[..., 0] - v[..., 4]) << CB
+        t10, t13, t11, t12 = t0 + t3, t0 - t3, t1 + t2, t1 - t2
+        t0, t1, t2, t3 = v[..., 7], v[..., 5], v[..., 3], v[..., 1]
+        z1, z2, z3, z4 = t0 + t3, t1 + t2, t0 + t2, t1 + t3
+        z5 = (z3 + z4) * F["f"]
+        t0, t1, t2, t3 = t0 * F["a"], t1 * F["j"], t2 * F["l"], t3 * F["g"]
+        z1, z2, z3, z4 = z1 * -F["e"], z2 * -F["k"], z3 * -F["i"] + z5, z4 * -F["b"] + z5
+        t0, t1, t2, t3 = t0 + z1 + z3, t1 + z2 + z4, t2 + z2 + z3, t3 + z1 + z4
+        ds = lambda a: (a + (1 << (out_shift - 1))) >> out_shift
+        return np.stack([ds(t10 + t3), ds(t11 + t2), ds(t12 + t1), ds(t13 + t0),
+                         ds(t13 - t0), ds(t12 - t1), ds(t11 - t2), ds(t10 - t3)], -1)
+
+    cols = np.swapaxes(x, -1, -2)  # [..., col, row]: transform along rows index
+    ws = flow(cols, 0, CB - P1)    # [..., col, row-out]
+    dc_only = np.all(cols[..., 1:] == 0, axis=-1)
+    ws = np.where(dc_only[..., None], (cols[..., :1] << P1), ws)
+    ws = np.swapaxes(ws, -1, -2)   # [..., row, col]
+    out = flow(ws, 0, CB + P1 + 3)
+    dc_only = np.all(ws[..., 1:] == 0, axis=-1)
+    out = np.where(dc_only[..., None], (ws[..., :1] + (1 << (P1 + 2))) >> (P1 + 3), out)
+    v = out & 1023
+    v = np.where(v >= 512, v - 1024, v) + 128
+    return np.clip(v, 0, 255)
+
+
+def _upsample(plane: np.ndarray, dw: int, dh: int, hx: int, vx: int) -> np.ndarray:
+    """libjpeg's fancy (triangle) upsampling for 2x1, 2x2 (and libjpeg-turbo's
+    1x2), edge samples repeated; replication otherwise or when the
+    component is 2 samples wide or less."""
+    p = plane[:dh, :dw].astype(np.int64)
+    if hx == 1 and vx == 1:
+        return p
+    up = np.vstack([p[:1], p[:-1]])
+    dn = np.vstack([p[1:], p[-1:]])
+    if hx == 2 and vx == 1 and dw > 2:
+        o = np.zeros((dh, 2 * dw), np.int64)
+        left = np.hstack([p[:, :1], p[:, :-1]])
+        right = np.hstack([p[:, 1:], p[:, -1:]])
+        o[:, 0::2] = (3 * p + left + 1) >> 2
+        o[:, 1::2] = (3 * p + right + 2) >> 2
+        o[:, 0], o[:, -1] = p[:, 0], p[:, -1]
+        return o
+    if hx == 2 and vx == 2 and dw > 2:
+        o = np.zeros((2 * dh, 2 * dw), np.int64)
+        for half, nb in ((0, up), (1, dn)):
+            cs = 3 * p + nb
+            last = np.hstack([cs[:, :1], cs[:, :-1]])
+            nxt = np.hstack([cs[:, 1:], cs[:, -1:]])
+            ev = (3 * cs + last + 8) >> 4
+            od = (3 * cs + nxt + 7) >> 4
+            ev[:, 0] = (4 * cs[:, 0] + 8) >> 4
+            od[:, -1] = (4 * cs[:, -1] + 7) >> 4
+            o[half::2, 0::2] = ev
+            o[half::2, 1::2] = od
+        return o
+    if hx == 1 and vx == 2:
+        o = np.zeros((2 * dh, dw), np.int64)
+        o[0::2] = (3 * p + up + 1) >> 2
+        o[1::2] = (3 * p + dn + 2) >> 2
+        return o
+    return np.repeat(np.repeat(p, vx, 0), hx, 1)
+
+
+def jpeg_pixels(info: dict) -> np.ndarray:
+    """The texels libjpeg's default decompression gives for the quantised
+    coefficients of a JPEG (read_jpeg_file, image.cpp:183-255): IDCT,
+    upsampling, then YCbCr -> RGB with 16 fraction bits (grey replicated)."""
+    w, h, hmax, vmax = info["width"], info["height"], info["hmax"], info["vmax"]
+    full = []
+    for c in info["comps"]:
+        s = _idct_islow(c["coef"], info["qts"][c["tq"]])  # (bh, bw, 8, 8)
+        plane = s.transpose(0, 2, 1, 3).reshape(c["bh"] * 8, c["bw"] * 8)
+        full.append(_upsample(plane, c["dw"], c["dh"], hmax // c["h"], vmax // c["v"])[:h, :w])
+    if len(full) == 1:
+        g = full[0].astype(np.uint32)
+        return (0xFF000000 | (g << 16) | (g << 8) | g).astype(np.uint32)
+    fix = lambda x: int(x * 65536.0 + 0.5)
+    xs = np.arange(256, dtype=np.int64) - 128
+    cr_r = (fix(1.40200) * xs + (1 << 15)) >> 16
+    cb_b = (fix(1.77200) * xs + (1 << 15)) >> 16
+    cr_g = -fix(0.71414) * xs
+    cb_g = -fix(0.34414) * xs + (1 << 15)
+    y, cb, cr = full
+    r = np.clip(y + cr_r[cr], 0, 255).astype(np.uint32)
+    g = np.clip(y + ((cb_g[cb] + cr_g[cr]) >> 16), 0, 255).astype(np.uint32)
+    b = np.clip(y + cb_b[cb], 0, 255).astype(np.uint32)
+    return (0xFF000000 | (r << 16) | (g << 8) | b).astype(np.uint32)

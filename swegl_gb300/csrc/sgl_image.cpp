@@ -470,10 +470,562 @@ bool decode_png(const uint8_t *d, size_t size, Image &out, std::string &err)
 }
 
 // ------------------------------------------------------------------ JPEG --
+//
+// Baseline and extended sequential Huffman JPEG (ITU T.81 / JFIF), decoded
+// the way libjpeg's default decompression (which read_jpeg_file uses) does
+// it: the accurate integer IDCT (the Loeffler-Ligtenberg-Moschytz flow graph
+// in 13-bit fixed point, two passes, columns then rows), "fancy" triangle
+// upsampling of subsampled chroma, and fixed-point YCbCr -> RGB with 16
+// fraction bits.  Progressive and arithmetic-coded files are errors.
 
-bool decode_jpeg(const uint8_t *, size_t, Image &, std::string &err)
+namespace {
+
+const uint8_t kZigzag[64] = {0,  1,  8,  16, 9,  2,  3,  10, 17, 24, 32, 25, 18, 11, 4,  5,
+                             12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6,  7,  14, 21, 28,
+                             35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51,
+                             58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
+
+struct JHuff {
+    bool present = false;
+    uint8_t val[256];
+    int mincode[17], maxcode[18], valptr[17];
+};
+
+void jhuff_build(JHuff &h, const uint8_t *counts, const uint8_t *vals, int nvals)
 {
-    return fail(err, "JPEG: decoding is not built (PNG and BMP textures are)");
+    std::memcpy(h.val, vals, (size_t)nvals);
+    int code = 0, k = 0;
+    for (int l = 1; l <= 16; l++) {
+        h.valptr[l] = k;
+        h.mincode[l] = code;
+        code += counts[l - 1];
+        k += counts[l - 1];
+        h.maxcode[l] = counts[l - 1] ? code - 1 : -1;
+        code <<= 1;
+    }
+    h.maxcode[17] = 0x7FFFFFFF;
+    h.present = true;
+}
+
+struct JBits {
+    const uint8_t *p, *end;
+    uint32_t buf = 0;
+    int cnt = 0;
+    bool marker = false; // a marker was reached: further bits are zeros
+
+    void fill()
+    {
+        while (cnt <= 24) {
+            uint32_t byte = 0;
+            if (!marker && p < end) {
+                byte = *p;
+                if (byte == 0xFF) {
+                    if (p + 1 < end && p[1] == 0x00) {
+                        p += 2;
+                    } else {
+                        marker = true;
+                        byte = 0;
+                    }
+                } else {
+                    p++;
+                }
+            }
+            buf |= byte << (24 - cnt);
+            cnt += 8;
+        }
+    }
+    int bit()
+    {
+        if (cnt < 1)
+            fill();
+        const int b = (int)(buf >> 31);
+        buf <<= 1;
+        cnt--;
+        return b;
+    }
+    int bits(int n)
+    {
+        if (n == 0)
+            return 0;
+        if (cnt < n)
+            fill();
+        const int v = (int)(buf >> (32 - n));
+        buf <<= n;
+        cnt -= n;
+        return v;
+    }
+    // a restart marker: byte-align and skip it
+    bool restart()
+    {
+        buf = 0;
+        cnt = 0;
+        marker = false;
+        while (p + 1 < end && !(p[0] == 0xFF && p[1] >= 0xD0 && p[1] <= 0xD7))
+            p++;
+        if (p + 1 >= end)
+            return false;
+        p += 2;
+        return true;
+    }
+};
+
+int jdecode(JBits &b, const JHuff &h)
+{
+    int code = b.bit();
+    int l = 1;
+    while (code > h.maxcode[l]) {
+        code = (code << 1) | b.bit();
+        if (++l > 16)
+            return -1;
+    }
+    return h.val[(h.valptr[l] + code - h.mincode[l]) & 0xFF];
+}
+
+int jextend(int v, int s) { return v < (1 << (s - 1)) ? v - (1 << s) + 1 : v; }
+
+struct JComp {
+    int id = 0, h = 1, v = 1, tq = 0;
+    int td = 0, ta = 0, pred = 0;
+    int bw = 0, bh = 0;          // blocks across and down in the coefficient store
+    int dw = 0, dh = 0;          // downsampled width and height
+    std::vector<int16_t> coef;   // bw * bh blocks of 64 (natural order)
+    std::vector<uint8_t> plane;  // (8 bw) x (8 bh) samples after the IDCT
+};
+
+// The accurate integer inverse DCT of one block: dequantised coefficients,
+// columns with 2 extra fraction bits, then rows; output level-shifted by 128
+// and clamped (out-of-range values wrap mod 1024 first, as a masked table
+// lookup does).  64-bit intermediates, like libjpeg's on LP64 hosts.
+void idct_islow(const int16_t *in, const uint16_t *q, uint8_t *out, int stride)
+{
+    constexpr int CB = 13, P1 = 2;
+    constexpr int64_t F0298 = 2446, F0390 = 3196, F0541 = 4433, F0765 = 6270, F0899 = 7373, F1175 = 9633,
+                      F1501 = 12299, F1847 = 15137, F1961 = 16069, F2053 = 16819, F2562 = 20995, F3072 = 25172;
+    auto descale = [](int64_t x, int n) { return (x + ((int64_t)1 << (n - 1))) >> n; };
+    auto clamp = [](int64_t x) {
+        x &= 1023; // the low bits of the descaled value, as the masked table lookup sees them
+        if (x >= 512)
+            x -= 1024;
+        x += 128;
+        return (uint8_t)(x < 0 ? 0 : (x > 255 ? 255 : x));
+    };
+    int64_t ws[64];
+    for (int c = 0; c < 8; c++) {
+        const int16_t *i = in + c;
+        const uint16_t *qq = q + c;
+        if (!i[8] && !i[16] && !i[24] && !i[32] && !i[40] && !i[48] && !i[56]) {
+            const int64_t dc = ((int64_t)i[0] * qq[0]) * (1 << P1);
+            for (int r = 0; r < 8; r++)
+                ws[c + 8 * r] = dc;
+            continue;
+        }
+        int64_t z2 = i[16] * qq[16], z3 = i[48] * qq[48];
+        int64_t z1 = (z2 + z3) * F0541;
+        int64_t t2 = z1 + z3 * (-F1847), t3 = z1 + z2 * F0765;
+        z2 = i[0] * qq[0];
+        z3 = i[32] * qq[32];
+        int64_t t0 = (z2 + z3) * (1 << CB), t1 = (z2 - z3) * (1 << CB);
+        const int64_t t10 = t0 + t3, t13 = t0 - t3, t11 = t1 + t2, t12 = t1 - t2;
+        t0 = i[56] * qq[56];
+        t1 = i[40] * qq[40];
+        t2 = i[24] * qq[24];
+        t3 = i[8] * qq[8];
+        z1 = t0 + t3;
+        z2 = t1 + t2;
+        z3 = t0 + t2;
+        int64_t z4 = t1 + t3;
+        const int64_t z5 = (z3 + z4) * F1175;
+        t0 *= F0298;
+        t1 *= F2053;
+        t2 *= F3072;
+        t3 *= F1501;
+        z1 *= -F0899;
+        z2 *= -F2562;
+        z3 *= -F1961;
+        z4 *= -F0390;
+        z3 += z5;
+        z4 += z5;
+        t0 += z1 + z3;
+        t1 += z2 + z4;
+        t2 += z2 + z3;
+        t3 += z1 + z4;
+        ws[c + 0] = descale(t10 + t3, CB - P1);
+        ws[c + 56] = descale(t10 - t3, CB - P1);
+        ws[c + 8] = descale(t11 + t2, CB - P1);
+        ws[c + 48] = descale(t11 - t2, CB - P1);
+        ws[c + 16] = descale(t12 + t1, CB - P1);
+        ws[c + 40] = descale(t12 - t1, CB - P1);
+        ws[c + 24] = descale(t13 + t0, CB - P1);
+        ws[c + 32] = descale(t13 - t0, CB - P1);
+    }
+    for (int r = 0; r < 8; r++) {
+        const int64_t *w = ws + 8 * r;
+        uint8_t *o = out + (size_t)r * stride;
+        if (!w[1] && !w[2] && !w[3] && !w[4] && !w[5] && !w[6] && !w[7]) {
+            const uint8_t v = clamp(descale(w[0], P1 + 3));
+            for (int k = 0; k < 8; k++)
+                o[k] = v;
+            continue;
+        }
+        int64_t z2 = w[2], z3 = w[6];
+        int64_t z1 = (z2 + z3) * F0541;
+        int64_t t2 = z1 + z3 * (-F1847), t3 = z1 + z2 * F0765;
+        int64_t t0 = (w[0] + w[4]) * (1 << CB), t1 = (w[0] - w[4]) * (1 << CB);
+        const int64_t t10 = t0 + t3, t13 = t0 - t3, t11 = t1 + t2, t12 = t1 - t2;
+        t0 = w[7];
+        t1 = w[5];
+        t2 = w[3];
+        t3 = w[1];
+        z1 = t0 + t3;
+        z2 = t1 + t2;
+        z3 = t0 + t2;
+        int64_t z4 = t1 + t3;
+        const int64_t z5 = (z3 + z4) * F1175;
+        t0 *= F0298;
+        t1 *= F2053;
+        t2 *= F3072;
+        t3 *= F1501;
+        z1 *= -F0899;
+        z2 *= -F2562;
+        z3 *= -F1961;
+        z4 *= -F0390;
+        z3 += z5;
+        z4 += z5;
+        t0 += z1 + z3;
+        t1 += z2 + z4;
+        t2 += z2 + z3;
+        t3 += z1 + z4;
+        constexpr int S = CB + P1 + 3;
+        o[0] = clamp(descale(t10 + t3, S));
+        o[7] = clamp(descale(t10 - t3, S));
+        o[1] = clamp(descale(t11 + t2, S));
+        o[6] = clamp(descale(t11 - t2, S));
+        o[2] = clamp(descale(t12 + t1, S));
+        o[5] = clamp(descale(t12 - t1, S));
+        o[3] = clamp(descale(t13 + t0, S));
+        o[4] = clamp(descale(t13 - t0, S));
+    }
+}
+
+// One component plane upsampled to hmax/h x vmax/v: triangle ("fancy")
+// filters for 2x1, 2x2 and 1x2 (edge samples repeated), replication
+// otherwise.  Output rows of width 2*dw (or dw*hx) for dh*vx rows.
+bool upsample(const JComp &c, int hx, int vx, std::vector<uint8_t> &out, int &ow, int &oh)
+{
+    const int w = c.dw, h = c.dh, st = 8 * c.bw;
+    ow = w * hx;
+    oh = h * vx;
+    out.assign((size_t)ow * oh, 0);
+    auto in = [&](int y, int x) -> int { return c.plane[(size_t)y * st + x]; };
+    if (hx == 1 && vx == 1) {
+        for (int y = 0; y < h; y++)
+            std::memcpy(&out[(size_t)y * ow], &c.plane[(size_t)y * st], (size_t)w);
+        return true;
+    }
+    const bool fancy = w > 2;
+    if (hx == 2 && vx == 1 && fancy) {
+        for (int y = 0; y < h; y++) {
+            uint8_t *o = &out[(size_t)y * ow];
+            int v = in(y, 0);
+            o[0] = (uint8_t)v;
+            o[1] = (uint8_t)((v * 3 + in(y, 1) + 2) >> 2);
+            for (int x = 1; x < w - 1; x++) {
+                v = in(y, x) * 3;
+                o[2 * x] = (uint8_t)((v + in(y, x - 1) + 1) >> 2);
+                o[2 * x + 1] = (uint8_t)((v + in(y, x + 1) + 2) >> 2);
+            }
+            v = in(y, w - 1);
+            o[2 * w - 2] = (uint8_t)((v * 3 + in(y, w - 2) + 1) >> 2);
+            o[2 * w - 1] = (uint8_t)v;
+        }
+        return true;
+    }
+    if (hx == 2 && vx == 2 && fancy) {
+        for (int y = 0; y < h; y++)
+            for (int half = 0; half < 2; half++) {
+                const int y1 = half == 0 ? (y > 0 ? y - 1 : 0) : (y < h - 1 ? y + 1 : h - 1);
+                uint8_t *o = &out[(size_t)(2 * y + half) * ow];
+                auto col = [&](int x) { return in(y, x) * 3 + in(y1, x); };
+                int this_s = col(0), next_s = col(1), last_s;
+                o[0] = (uint8_t)((this_s * 4 + 8) >> 4);
+                o[1] = (uint8_t)((this_s * 3 + next_s + 7) >> 4);
+                last_s = this_s;
+                this_s = next_s;
+                for (int x = 1; x < w - 1; x++) {
+                    next_s = col(x + 1);
+                    o[2 * x] = (uint8_t)((this_s * 3 + last_s + 8) >> 4);
+                    o[2 * x + 1] = (uint8_t)((this_s * 3 + next_s + 7) >> 4);
+                    last_s = this_s;
+                    this_s = next_s;
+                }
+                o[2 * w - 2] = (uint8_t)((this_s * 3 + last_s + 8) >> 4);
+                o[2 * w - 1] = (uint8_t)((this_s * 4 + 7) >> 4);
+            }
+        return true;
+    }
+    if (hx == 1 && vx == 2) {
+        for (int y = 0; y < h; y++)
+            for (int half = 0; half < 2; half++) {
+                const int y1 = half == 0 ? (y > 0 ? y - 1 : 0) : (y < h - 1 ? y + 1 : h - 1);
+                const int bias = half == 0 ? 1 : 2;
+                uint8_t *o = &out[(size_t)(2 * y + half) * ow];
+                for (int x = 0; x < w; x++)
+                    o[x] = (uint8_t)((in(y, x) * 3 + in(y1, x) + bias) >> 2);
+            }
+        return true;
+    }
+    for (int y = 0; y < oh; y++)
+        for (int x = 0; x < ow; x++)
+            out[(size_t)y * ow + x] = (uint8_t)in(y / vx, x / hx);
+    return true;
+}
+
+} // namespace
+
+bool decode_jpeg(const uint8_t *d, size_t size, Image &out, std::string &err)
+{
+    if (size < 4 || d[0] != 0xFF || d[1] != 0xD8)
+        return fail(err, "JPEG: missing SOI marker");
+    uint16_t qt[4][64] = {{0}};
+    bool have_qt[4] = {false, false, false, false};
+    JHuff dc[4], ac[4];
+    std::vector<JComp> comps;
+    int width = 0, height = 0, hmax = 1, vmax = 1, restart = 0;
+    bool frame = false, adobe = false, jfif = false, scanned = false;
+    int adobe_transform = -1;
+    size_t p = 2;
+    while (p + 4 <= size) {
+        if (d[p] != 0xFF) {
+            p++;
+            continue;
+        }
+        const int m = d[p + 1];
+        if (m == 0xFF || m == 0x01 || (m >= 0xD0 && m <= 0xD7)) {
+            p++;
+            continue;
+        }
+        if (m == 0xD9)
+            break; // EOI
+        const size_t len = (size_t)((d[p + 2] << 8) | d[p + 3]);
+        const uint8_t *b = d + p + 4;
+        if (len < 2 || p + 2 + len > size)
+            return fail(err, "JPEG: segment overruns the file");
+        const size_t n = len - 2;
+        if (m == 0xDB) { // DQT
+            for (size_t k = 0; k < n;) {
+                const int pq = b[k] >> 4, tq = b[k] & 15;
+                if (tq > 3 || k + 1 + 64 * (pq + 1) > n)
+                    return fail(err, "JPEG: bad DQT");
+                for (int i = 0; i < 64; i++)
+                    qt[tq][kZigzag[i]] = pq ? (uint16_t)((b[k + 1 + 2 * i] << 8) | b[k + 2 + 2 * i]) : b[k + 1 + i];
+                have_qt[tq] = true;
+                k += 1 + 64 * (pq + 1);
+            }
+        } else if (m == 0xC4) { // DHT
+            for (size_t k = 0; k < n;) {
+                if (k + 17 > n)
+                    return fail(err, "JPEG: bad DHT");
+                const int tc = b[k] >> 4, th = b[k] & 15;
+                int total = 0;
+                for (int i = 0; i < 16; i++)
+                    total += b[k + 1 + i];
+                if (tc > 1 || th > 3 || total > 256 || k + 17 + total > n)
+                    return fail(err, "JPEG: bad DHT");
+                jhuff_build(tc ? ac[th] : dc[th], b + k + 1, b + k + 17, total);
+                k += 17 + (size_t)total;
+            }
+        } else if (m == 0xC0 || m == 0xC1) { // SOF0 / SOF1: sequential, Huffman
+            if (n < 6 || b[0] != 8)
+                return fail(err, "JPEG: only 8-bit samples are decoded");
+            height = (b[1] << 8) | b[2];
+            width = (b[3] << 8) | b[4];
+            const int nc = b[5];
+            if (width <= 0 || height <= 0 || (nc != 1 && nc != 3) || n < 6 + 3 * (size_t)nc ||
+                (int64_t)width * height > (1ll << 28))
+                return fail(err, "JPEG: unsupported frame (1 or 3 components, known size expected)");
+            comps.resize((size_t)nc);
+            for (int c = 0; c < nc; c++) {
+                comps[c].id = b[6 + 3 * c];
+                comps[c].h = b[7 + 3 * c] >> 4;
+                comps[c].v = b[7 + 3 * c] & 15;
+                comps[c].tq = b[8 + 3 * c] & 3;
+                if (comps[c].h < 1 || comps[c].h > 4 || comps[c].v < 1 || comps[c].v > 4)
+                    return fail(err, "JPEG: bad sampling factors");
+                hmax = std::max(hmax, comps[c].h);
+                vmax = std::max(vmax, comps[c].v);
+            }
+            const int mcux = (width + 8 * hmax - 1) / (8 * hmax), mcuy = (height + 8 * vmax - 1) / (8 * vmax);
+            for (JComp &c : comps) {
+                if (hmax % c.h || vmax % c.v)
+                    return fail(err, "JPEG: non-integral sampling ratios");
+                c.bw = mcux * c.h;
+                c.bh = mcuy * c.v;
+                c.dw = (width * c.h + hmax - 1) / hmax;
+                c.dh = (height * c.v + vmax - 1) / vmax;
+                c.coef.assign((size_t)c.bw * c.bh * 64, 0);
+            }
+            frame = true;
+        } else if (m >= 0xC2 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) {
+            return fail(err, "JPEG: progressive, lossless or arithmetic-coded files are not decoded");
+        } else if (m == 0xDD) { // DRI
+            if (n < 2)
+                return fail(err, "JPEG: bad DRI");
+            restart = (b[0] << 8) | b[1];
+        } else if (m == 0xE0 && n >= 5 && !std::memcmp(b, "JFIF", 4)) {
+            jfif = true;
+        } else if (m == 0xEE && n >= 12 && !std::memcmp(b, "Adobe", 5)) {
+            adobe = true;
+            adobe_transform = b[11];
+        } else if (m == 0xDA) { // SOS
+            if (!frame)
+                return fail(err, "JPEG: scan before the frame header");
+            const int ns = b[0];
+            if (ns < 1 || ns > 4 || n < 1 + 2 * (size_t)ns + 3)
+                return fail(err, "JPEG: bad scan header");
+            std::vector<JComp *> sc;
+            for (int k = 0; k < ns; k++) {
+                const int cid = b[1 + 2 * k];
+                JComp *c = nullptr;
+                for (JComp &cc : comps)
+                    if (cc.id == cid)
+                        c = &cc;
+                if (!c)
+                    return fail(err, "JPEG: scan names an unknown component");
+                c->td = b[2 + 2 * k] >> 4;
+                c->ta = b[2 + 2 * k] & 15;
+                if (c->td > 3 || c->ta > 3 || !dc[c->td].present || !ac[c->ta].present || !have_qt[c->tq])
+                    return fail(err, "JPEG: scan uses a missing table");
+                c->pred = 0;
+                sc.push_back(c);
+            }
+            JBits bits{d + p + 2 + len, d + size};
+            auto block = [&](JComp &c, int bx, int by) {
+                int16_t *co = &c.coef[((size_t)by * c.bw + bx) * 64];
+                const int t = jdecode(bits, dc[c.td]);
+                if (t < 0 || t > 11)
+                    return false;
+                c.pred += t ? jextend(bits.bits(t), t) : 0;
+                co[0] = (int16_t)c.pred;
+                for (int k = 1; k < 64;) {
+                    const int rs = jdecode(bits, ac[c.ta]);
+                    if (rs < 0)
+                        return false;
+                    const int r = rs >> 4, s2 = rs & 15;
+                    if (s2) {
+                        k += r;
+                        if (k > 63)
+                            return false;
+                        co[kZigzag[k]] = (int16_t)jextend(bits.bits(s2), s2);
+                        k++;
+                    } else if (r == 15) {
+                        k += 16;
+                    } else {
+                        break;
+                    }
+                }
+                return true;
+            };
+            int units_x, units_y;
+            if (ns == 1) {
+                units_x = (sc[0]->dw + 7) / 8;
+                units_y = (sc[0]->dh + 7) / 8;
+            } else {
+                units_x = (width + 8 * hmax - 1) / (8 * hmax);
+                units_y = (height + 8 * vmax - 1) / (8 * vmax);
+            }
+            int todo = restart;
+            for (int my = 0; my < units_y; my++)
+                for (int mx = 0; mx < units_x; mx++) {
+                    if (restart && todo == 0) {
+                        if (!bits.restart())
+                            return fail(err, "JPEG: missing restart marker");
+                        for (JComp *c : sc)
+                            c->pred = 0;
+                        todo = restart;
+                    }
+                    if (ns == 1) {
+                        if (!block(*sc[0], mx, my))
+                            return fail(err, "JPEG: corrupt entropy-coded data");
+                    } else {
+                        for (JComp *c : sc)
+                            for (int v = 0; v < c->v; v++)
+                                for (int h = 0; h < c->h; h++)
+                                    if (!block(*c, mx * c->h + h, my * c->v + v))
+                                        return fail(err, "JPEG: corrupt entropy-coded data");
+                    }
+                    todo--;
+                }
+            scanned = true;
+            // continue after the entropy-coded data: the next marker
+            p = (size_t)(bits.p - d);
+            while (p + 1 < size && !(d[p] == 0xFF && d[p + 1] != 0 && !(d[p + 1] >= 0xD0 && d[p + 1] <= 0xD7)))
+                p++;
+            continue;
+        }
+        p += 2 + len;
+    }
+    if (!frame || !scanned)
+        return fail(err, "JPEG: no frame or no scan");
+    for (JComp &c : comps) {
+        c.plane.assign((size_t)c.bw * 8 * c.bh * 8, 0);
+        for (int by = 0; by < c.bh; by++)
+            for (int bx = 0; bx < c.bw; bx++)
+                idct_islow(&c.coef[((size_t)by * c.bw + bx) * 64], qt[c.tq],
+                           &c.plane[(size_t)by * 8 * (8 * c.bw) + (size_t)bx * 8], 8 * c.bw);
+    }
+    std::vector<std::vector<uint8_t>> full(comps.size());
+    std::vector<int> fw(comps.size());
+    for (size_t k = 0; k < comps.size(); k++) {
+        int ow, oh;
+        upsample(comps[k], hmax / comps[k].h, vmax / comps[k].v, full[k], ow, oh);
+        if (ow < width || oh < height)
+            return fail(err, "JPEG: component smaller than the image");
+        fw[k] = ow;
+    }
+    out.width = width;
+    out.height = height;
+    out.texels.assign((size_t)width * height, 0u);
+    if (comps.size() == 1) {
+        // grey to grey RGB (the reference would read a one-channel buffer as RGB)
+        for (int y = 0; y < height; y++)
+            for (int x = 0; x < width; x++) {
+                const uint32_t g = full[0][(size_t)y * fw[0] + x];
+                out.texels[(size_t)y * width + x] = 0xFF000000u | (g << 16) | (g << 8) | g;
+            }
+        return true;
+    }
+    // colour space as libjpeg guesses it: a JFIF marker means YCbCr, else an
+    // Adobe marker's transform flag, else component ids 'R', 'G', 'B'
+    const bool rgb = !jfif && (adobe ? adobe_transform == 0
+                                     : (comps[0].id == 'R' && comps[1].id == 'G' && comps[2].id == 'B'));
+    // YCbCr -> RGB with 16 fraction bits (JFIF coefficients 1.402, 0.34414, 0.71414, 1.772)
+    auto fix = [](double x) { return (int32_t)(x * 65536.0 + 0.5); };
+    int32_t cr_r[256], cb_b[256], cr_g[256], cb_g[256];
+    for (int i = 0; i < 256; i++) {
+        const int32_t x = i - 128;
+        cr_r[i] = (fix(1.40200) * x + (1 << 15)) >> 16;
+        cb_b[i] = (fix(1.77200) * x + (1 << 15)) >> 16;
+        cr_g[i] = -fix(0.71414) * x;
+        cb_g[i] = -fix(0.34414) * x + (1 << 15);
+    }
+    auto lim = [](int32_t v) { return (uint32_t)(v < 0 ? 0 : (v > 255 ? 255 : v)); };
+    for (int y = 0; y < height; y++)
+        for (int x = 0; x < width; x++) {
+            const int c0 = full[0][(size_t)y * fw[0] + x], c1 = full[1][(size_t)y * fw[1] + x],
+                      c2 = full[2][(size_t)y * fw[2] + x];
+            uint32_t r, g, b;
+            if (rgb) {
+                r = (uint32_t)c0;
+                g = (uint32_t)c1;
+                b = (uint32_t)c2;
+            } else {
+                r = lim(c0 + cr_r[c2]);
+                g = lim(c0 + ((cb_g[c1] + cr_g[c2]) >> 16));
+                b = lim(c0 + cb_b[c1]);
+            }
+            out.texels[(size_t)y * width + x] = 0xFF000000u | (r << 16) | (g << 8) | b;
+        }
+    return true;
 }
 
 // ---------------------------------------------------------- by file name --

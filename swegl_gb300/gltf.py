@@ -4,7 +4,7 @@
 is read by `sgl_gltf_load` (include/sgl.h) and exposed as a `scenes.Scene`
 (for `Renderer.upload`) whose nodes follow `animate(seconds)`
 (scene_t::animate, swegl/data/model.hpp:146-177).  `load_image(path)` is
-read_image_file (src/misc/image.cpp:20-27) for BMP and PNG files.
+read_image_file (src/misc/image.cpp:20-27) for BMP, PNG and JPEG files.
 """
 from __future__ import annotations
 
@@ -84,7 +84,7 @@ class GltfScene:
 
 
 def load_image(path: str) -> np.ndarray:
-    """0xAARRGGBB texels (height, width) of a BMP or PNG file."""
+    """0xAARRGGBB texels (height, width) of a BMP, PNG or JPEG file."""
     lib = library()
     t = C.POINTER(C.c_uint32)()
     w, h = C.c_int(), C.c_int()

@@ -305,3 +305,237 @@ def build_test_scene(dirpath: str, glb: bool, seed: int = 3) -> str:
     path = os.path.join(dirpath, "scene.glb" if glb else "scene.gltf")
     g.write(path, glb, external_bin=not glb and seed % 2 == 1)
     return path
+
+
+# -------------------------------------------------------------------- JPEG --
+ZIGZAG = np.array([0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 26, 33, 40, 48, 41, 34, 27, 20,
+                   13, 6, 7, 14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51, 58, 59, 52,
+                   45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63])
+
+
+def _dct_matrix():
+    c = np.zeros((8, 8))
+    for k in range(8):
+        for n in range(8):
+            c[k, n] = (math.sqrt(0.125) if k == 0 else 0.5) * math.cos((2 * n + 1) * k * math.pi / 16)
+    return c
+
+
+def _huff_lengths(freq: dict) -> dict:
+    """Code lengths <= 16 with no all-ones code (a reserved dummy symbol,
+    then the length adjustment of T.81 Annex K.2)."""
+    import heapq
+
+    syms = dict(freq)
+    syms[256] = 1  # reserved
+    heap = [(f, i, [s]) for i, (s, f) in enumerate(sorted(syms.items()))]
+    heapq.heapify(heap)
+    depth = {s: 0 for s in syms}
+    if len(heap) == 1:
+        depth[heap[0][2][0]] = 1
+    cnt = len(heap)
+    while len(heap) > 1:
+        f1, _, a = heapq.heappop(heap)
+        f2, _, b = heapq.heappop(heap)
+        for s in a + b:
+            depth[s] += 1
+        cnt += 1
+        heapq.heappush(heap, (f1 + f2, cnt, a + b))
+    bits = [0] * 40
+    for s, d in depth.items():
+        bits[d] += 1
+    for i in range(39, 16, -1):
+        while bits[i] > 0:
+            j = i - 2
+            while bits[j] == 0:
+                j -= 1
+            bits[i] -= 2
+            bits[i - 1] += 1
+            bits[j + 1] += 2
+            bits[j] -= 1
+    i = 16
+    while bits[i] == 0:
+        i -= 1
+    bits[i] -= 1  # drop the reserved symbol's code
+    order = sorted(freq, key=lambda s: (-freq[s], s))
+    lengths, k = {}, 0
+    for L in range(1, 17):
+        for _ in range(bits[L]):
+            lengths[order[k]] = L
+            k += 1
+    return lengths
+
+
+def _canonical(lengths: dict):
+    """DHT body (counts, values) and the code of each symbol."""
+    order = sorted(lengths, key=lambda s: (lengths[s], s))
+    counts = [0] * 16
+    for s in order:
+        counts[lengths[s] - 1] += 1
+    codes, code, prev = {}, 0, 0
+    for s in order:
+        code <<= lengths[s] - prev
+        prev = lengths[s]
+        codes[s] = (code, lengths[s])
+        code += 1
+    return counts, order, codes
+
+
+def _cat(v: int) -> int:
+    return 0 if v == 0 else int(abs(v)).bit_length()
+
+
+def encode_jpeg(rgb: np.ndarray, sampling=(2, 2), quality: int = 80, restart: int = 0, grey: bool = False,
+                interleaved: bool = True):
+    """A baseline JPEG of an (h, w, 3) uint8 image: JFIF YCbCr, luma sampled
+    `sampling` (h, v) times the chroma, float DCT, scaled standard-shaped
+    quantisers, per-file Huffman tables, optional restart interval and
+    separate scans per component.  Returns (bytes, info) with the quantised
+    coefficients of every block (natural order) for checking."""
+    h, w, _ = rgb.shape
+    f = rgb.astype(np.float64)
+    y = 0.299 * f[..., 0] + 0.587 * f[..., 1] + 0.114 * f[..., 2]
+    cb = -0.168736 * f[..., 0] - 0.331264 * f[..., 1] + 0.5 * f[..., 2] + 128
+    cr = 0.5 * f[..., 0] - 0.418688 * f[..., 1] - 0.081312 * f[..., 2] + 128
+    planes = [y] if grey else [y, cb, cr]
+    hs, vs = (1, 1) if grey else sampling
+    factors = [(hs, vs)] + [(1, 1)] * (len(planes) - 1)
+    hmax, vmax = hs, vs
+    mcux, mcuy = -(-w // (8 * hmax)), -(-h // (8 * vmax))
+    base_l = np.array([16, 11, 10, 16, 24, 40, 51, 61] * 8).reshape(8, 8) * 0 + np.add.outer(np.arange(8), np.arange(8)) * 6 + 8
+    scale = 5000 / quality if quality < 50 else 200 - 2 * quality
+    q_l = np.clip((base_l * scale + 50) // 100, 1, 255).astype(np.int64)
+    q_c = np.clip(((base_l + 10) * scale + 50) // 100, 1, 255).astype(np.int64)
+    qts = [q_l, q_c]
+    C = _dct_matrix()
+    comps = []
+    for k, (pl, (ch, cv)) in enumerate(zip(planes, factors)):
+        dw, dh = -(-w * ch // hmax), -(-h * cv // vmax)
+        sx, sy = hmax // ch, vmax // cv
+        pad = np.pad(pl, ((0, dh * sy - h), (0, dw * sx - w)), mode="edge")
+        ds = pad.reshape(dh, sy, dw, sx).mean(axis=(1, 3))
+        ds = np.clip(np.round(ds), 0, 255)
+        bw, bh = mcux * ch, mcuy * cv
+        full = np.pad(ds, ((0, bh * 8 - dh), (0, bw * 8 - dw)), mode="edge") - 128
+        blocks = full.reshape(bh, 8, bw, 8).transpose(0, 2, 1, 3)
+        coef = np.einsum("ij,abjk,lk->abil", C, blocks, C)
+        qt = qts[0 if k == 0 else 1]
+        qc = np.round(coef / qt).astype(np.int64)
+        comps.append(dict(id=k + 1, h=ch, v=cv, tq=0 if k == 0 else 1, coef=qc, bw=bw, bh=bh, dw=dw, dh=dh))
+    # symbols per scan
+    scans = [list(range(len(comps)))] if interleaved else [[k] for k in range(len(comps))]
+    seqs = []  # per scan: list of (component, (by, bx)) in coding order, with restart flags
+    for sc in scans:
+        seq = []
+        if len(sc) > 1:
+            for my in range(mcuy):
+                for mx in range(mcux):
+                    seq.append([(k, my * comps[k]["v"] + v, mx * comps[k]["h"] + hh) for k in sc
+                                for v in range(comps[k]["v"]) for hh in range(comps[k]["h"])])
+        else:
+            c = comps[sc[0]]
+            for by in range(-(-c["dh"] // 8)):
+                for bx in range(-(-c["dw"] // 8)):
+                    seq.append([(sc[0], by, bx)])
+        seqs.append(seq)
+    dc_freq = [dict(), dict()]
+    ac_freq = [dict(), dict()]
+    coded = []  # per scan, per MCU: list of (table, [(sym, bits, nbits)...])
+    for seq in seqs:
+        pred = {}
+        out_scan = []
+        for n, mcu in enumerate(seq):
+            if restart and n % restart == 0:
+                pred = {}
+            items = []
+            for (k, by, bx) in mcu:
+                c = comps[k]
+                t = 0 if k == 0 else 1
+                zz = c["coef"][by, bx].reshape(-1)[ZIGZAG]
+                diff = int(zz[0]) - pred.get(k, 0)
+                pred[k] = int(zz[0])
+                s = _cat(diff)
+                dc_freq[t][s] = dc_freq[t].get(s, 0) + 1
+                syms = [("dc", t, s, diff)]
+                run = 0
+                last = max([i for i in range(1, 64) if zz[i] != 0], default=0)
+                for i in range(1, last + 1):
+                    v = int(zz[i])
+                    if v == 0:
+                        run += 1
+                        continue
+                    while run > 15:
+                        syms.append(("ac", t, 0xF0, 0))
+                        ac_freq[t][0xF0] = ac_freq[t].get(0xF0, 0) + 1
+                        run -= 16
+                    rs = (run << 4) | _cat(v)
+                    syms.append(("ac", t, rs, v))
+                    ac_freq[t][rs] = ac_freq[t].get(rs, 0) + 1
+                    run = 0
+                if last < 63:
+                    syms.append(("ac", t, 0x00, 0))
+                    ac_freq[t][0] = ac_freq[t].get(0, 0) + 1
+                items.extend(syms)
+            out_scan.append(items)
+        coded.append(out_scan)
+    ntab = 1 if grey else 2
+    dc_codes, ac_codes, dht = [], [], b""
+    for t in range(ntab):
+        for cls, freq, store in ((0, dc_freq[t], dc_codes), (1, ac_freq[t], ac_codes)):
+            counts, order, codes = _canonical(_huff_lengths(freq))
+            store.append(codes)
+            body = bytes([(cls << 4) | t]) + bytes(counts) + bytes(order)
+            dht += b"\xff\xc4" + struct.pack(">H", 2 + len(body)) + body
+    out = bytearray(b"\xff\xd8")
+    out += b"\xff\xe0" + struct.pack(">H", 16) + b"JFIF\0" + bytes([1, 1, 0, 0, 1, 0, 1, 0, 0])
+    for t in range(ntab):
+        out += b"\xff\xdb" + struct.pack(">H", 67) + bytes([t]) + bytes(qts[t].reshape(-1)[ZIGZAG].astype(np.uint8))
+    sof = bytes([8]) + struct.pack(">HH", h, w) + bytes([len(comps)])
+    for c in comps:
+        sof += bytes([c["id"], (c["h"] << 4) | c["v"], c["tq"]])
+    out += b"\xff\xc0" + struct.pack(">H", 2 + len(sof)) + sof
+    out += dht
+    if restart:
+        out += b"\xff\xdd" + struct.pack(">HH", 4, restart)
+    for sc, scan in zip(scans, coded):
+        sos = bytes([len(sc)])
+        for k in sc:
+            t = 0 if k == 0 else 1
+            sos += bytes([comps[k]["id"], (t << 4) | t])
+        sos += bytes([0, 63, 0])
+        out += b"\xff\xda" + struct.pack(">H", 2 + len(sos)) + sos
+        acc, nacc = 0, 0
+        data = bytearray()
+
+        def put(code, n):
+            nonlocal acc, nacc
+            acc = (acc << n) | code
+            nacc += n
+            while nacc >= 8:
+                byte = (acc >> (nacc - 8)) & 0xFF
+                data.append(byte)
+                if byte == 0xFF:
+                    data.append(0)
+                nacc -= 8
+            acc &= (1 << nacc) - 1 if nacc else 0
+
+        def flush():
+            nonlocal acc, nacc
+            if nacc:
+                put((1 << (8 - nacc)) - 1, 8 - nacc)
+
+        for n, items in enumerate(scan):
+            if restart and n and n % restart == 0:
+                flush()
+                data += bytes([0xFF, 0xD0 + ((n // restart - 1) % 8)])
+            for (kind, t, sym, val) in items:
+                code, ln = (dc_codes if kind == "dc" else ac_codes)[t][sym]
+                put(code, ln)
+                s = sym if kind == "dc" else (sym & 15)
+                if s:
+                    put(val if val > 0 else val + (1 << s) - 1, s)
+        flush()
+        out += data
+    out += b"\xff\xd9"
+    info = dict(width=w, height=h, comps=comps, qts=qts, hmax=hmax, vmax=vmax)
+    return bytes(out), info

@@ -122,6 +122,37 @@ def test_bmp_follows_the_reference_reader(lib, tmp_path, w):
         assert np.array_equal(exp, std)
 
 
+JPEG_CASES = [(s, r, i, g) for s in [(1, 1), (2, 1), (2, 2), (1, 2)]
+              for (r, i, g) in [(0, True, False), (3, True, False), (0, False, False), (2, True, True)]]
+
+
+@pytest.mark.parametrize("sampling,restart,interleaved,grey", JPEG_CASES)
+def test_jpeg_matches_the_libjpeg_restatement(lib, tmp_path, sampling, restart, interleaved, grey):
+    """Baseline JPEGs (per-file Huffman tables, every luma sampling of 2x1,
+    2x2, 1x2, restart intervals, one scan per component, grey) decoded by
+    the library equal the restated libjpeg pixel path applied to the
+    encoder's own quantised coefficients; the image is close to its source."""
+    from swegl_gb300.gltf import load_image
+
+    yy, xx = np.mgrid[0:29, 0:37]
+    smooth = np.stack([(xx * 7) % 256, (yy * 9) % 256, ((xx + yy) * 5) % 256], -1).astype(np.uint8)
+    narrow = np.random.default_rng(2).integers(0, 256, size=(21, 5, 3)).astype(np.uint8)  # chroma <= 2 wide
+    for img in (smooth, narrow):
+        for q in (30, 95):
+            data, info = GF.encode_jpeg(img, sampling, q, restart, grey=grey, interleaved=interleaved)
+            path = str(tmp_path / "t.jpg")
+            with open(path, "wb") as fh:
+                fh.write(data)
+            got = load_image(path)
+            assert np.array_equal(got, GO.jpeg_pixels(info)), (img.shape, q)
+    data, info = GF.encode_jpeg(smooth, (1, 1), 95, 0)
+    with open(str(tmp_path / "s.jpeg"), "wb") as fh:
+        fh.write(data)
+    got = load_image(str(tmp_path / "s.jpeg"))
+    rgb = np.stack([(got >> 16) & 255, (got >> 8) & 255, got & 255], -1).astype(int)
+    assert np.abs(rgb - smooth.astype(int)).mean() < 3.0
+
+
 def test_bad_images_are_errors_not_crashes(lib, tmp_path):
     from swegl_gb300.gltf import load_image
     from swegl_gb300.runtime import SglError
