@@ -767,6 +767,31 @@ __device__ __forceinline__ void span_depth(const WalkView &v, int y, uint32_t sl
     }
 }
 
+// Fragment capture of a view with transparency layers (a layered batch has
+// one item): the pool counter and its per-pixel chains.
+__device__ __forceinline__ unsigned long long *frag_counter(const BatchDev *b)
+{
+    return b->counters + C_FRAGS / 2;
+}
+
+// One span's fragments stored from pool entry `at` on, each with its view
+// pixel in the `next` field (k_link chains them afterwards); pixels skipped
+// at the near plane are stored as holes (kFragEnd).
+__device__ __forceinline__ void span_frags(const BatchDev *b, uint32_t row_px, uint32_t slot, int x1, int x2,
+                                           Interp q, float pl, float pr, uint32_t bits, uint32_t at)
+{
+    Frag *pool = b->frags;
+    const float fb = __uint_as_float(bits);
+    for (int x = x1; x < x2; x++, q.step()) {
+        const float z = q.value();
+        const bool keep = !below_near(z) && __float_as_uint(z) < kMaxZBits;
+        const uint32_t k = at + (uint32_t)(x - x1);
+        reinterpret_cast<float4 *>(pool + k)[0] = make_float4(q.alpha, pl, pr, fb);
+        reinterpret_cast<uint4 *>(pool + k)[1] =
+            make_uint4(__float_as_uint(z), slot, keep ? row_px + (uint32_t)x : kFragEnd, 0u);
+    }
+}
+
 typedef uint32_t WalkRow[kWalkPitch];
 
 __device__ __forceinline__ float smf(const WalkRow *S, int f, int o) { return __uint_as_float(S[f][o]); }
@@ -901,6 +926,11 @@ __global__ void __launch_bounds__(256) k_setup(const BatchDev *b)
 // calls it (act = this lane has a row).  Spans wider than the inline limit,
 // and every span of a tall triangle, go to the long-span kernels.  Returns the
 // row's fragments.  `v` caches the item's view (reloaded when it changes).
+// With FRAGS (a view with transparency layers) every fragment is stored
+// instead: the warp reserves its lanes' fragments with one atomic per round
+// of rows, and a binned span carries its first pool entry in the span
+// record's `item` field.
+template <bool FRAGS>
 __device__ __forceinline__ int walk_row(const BatchDev *b, WalkView &v, uint32_t item, uint32_t slot, RowIn &r,
                                         bool act, bool bin_all)
 {
@@ -916,8 +946,29 @@ __device__ __forceinline__ int walk_row(const BatchDev *b, WalkView &v, uint32_t
     if (has)
         span_interp(sp, q, pl, pr);
     const bool want = has && (bin_all || sp.x2 - sp.x1 > v.inline_span);
-    if (!bin_span_warp(b, want, item, slot, r.y, sp, q, pl, pr, r.bits) && has)
-        span_depth(v, r.y, slot, sp.x1, sp.x2, q);
+    if constexpr (FRAGS) {
+        const int lane = threadIdx.x & 31;
+        const uint32_t n = has ? (uint32_t)(sp.x2 - sp.x1) : 0u;
+        uint32_t incl = n;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= d)
+                incl += u;
+        }
+        unsigned long long base = 0;
+        if (lane == 31 && incl)
+            base = atomicAdd(frag_counter(b), (unsigned long long)incl);
+        base = __shfl_sync(0xFFFFFFFFu, base, 31);
+        const unsigned long long at = base + incl - n;
+        const bool fits = at + n <= (unsigned long long)b->frag_cap; // else counted only: the view is redone
+        if (!bin_span_warp(b, want && fits, (uint32_t)at, slot, r.y, sp, q, pl, pr, r.bits) && has && fits)
+            span_frags(b, (uint32_t)((r.y - v.y) * v.w - v.x), slot, sp.x1, sp.x2, q, pl, pr, r.bits,
+                       (uint32_t)at);
+    } else {
+        if (!bin_span_warp(b, want, item, slot, r.y, sp, q, pl, pr, r.bits) && has)
+            span_depth(v, r.y, slot, sp.x1, sp.x2, q);
+    }
     return has ? sp.x2 - sp.x1 : 0;
 }
 
@@ -925,6 +976,7 @@ __device__ __forceinline__ int walk_row(const BatchDev *b, WalkView &v, uint32_t
 // every lane runs the 32 edge steps and keeps the state of its own row, so
 // no lane repeats more than 32 steps per row it walks.  Every span is binned.
 // Returns this lane's fragments.
+template <bool FRAGS>
 __device__ __forceinline__ uint32_t walk_tall(const BatchDev *b, uint32_t i)
 {
     const int lane = threadIdx.x & 31;
@@ -978,20 +1030,23 @@ __device__ __forceinline__ uint32_t walk_tall(const BatchDev *b, uint32_t i)
         r.sx = msx; r.st = mst; r.sb = msb;
         r.ls = 0;
         r.ss = 0;
-        frags += (uint32_t)walk_row(b, v, item, slot, r, act, true);
+        frags += (uint32_t)walk_row<FRAGS>(b, v, item, slot, r, act, true);
     }
     return frags;
 }
 
 // the rare depth walks, defined with the near-clip code below
 __device__ __noinline__ void walk_clip_depth(const BatchDev *b, ItemAcc &acc);
+template <bool FRAGS>
 __device__ __noinline__ void walk_tall_all(const BatchDev *b, ItemAcc &acc);
 
 // Depth walk of the drawable triangles wholly in front of the near plane
 // (fill_triangle's normal case, renderer.cpp:281-285: one sub-triangle, slot
 // 2t).  Each warp takes groups of 32 list entries (warp-strided), loads their
 // set-ups into shared memory (one 128-byte record per load) and deals their
-// rows across its lanes.
+// rows across its lanes.  FRAGS: the fragment capture of a layered view (the
+// near-clipped triangles are captured by k_frags).
+template <bool FRAGS>
 __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(const BatchDev *b)
 {
     __shared__ WalkRow sm[kWalkWarps][2][kWalkFields];
@@ -1058,7 +1113,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
                 const int ex = o > 0 ? (int)S[F_INCL][o - 1] : 0;
                 smem_row_in(r, S, o, p - ex);
             }
-            const int fr = walk_row(b, view, S[F_ITEM][o], S[F_SLOT][o], r, act, false);
+            const int fr = walk_row<FRAGS>(b, view, S[F_ITEM][o], S[F_SLOT][o], r, act, false);
             if (fr)
                 atomicAdd(&S[F_FRAGS][o], (uint32_t)fr);
         }
@@ -1071,8 +1126,9 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
     }
     cp_async_wait<0>();
     // then this warp's share of the near-clip and the tall triangles
-    walk_clip_depth(b, acc);
-    walk_tall_all(b, acc);
+    if (!FRAGS)
+        walk_clip_depth(b, acc);
+    walk_tall_all<FRAGS>(b, acc);
     acc.flush(b);
 }
 
@@ -1203,7 +1259,9 @@ __device__ __noinline__ void walk_clip_depth(const BatchDev *b, ItemAcc &acc)
     }
 }
 
-// Depth walk of the tall triangles, one warp each (warp-strided).
+// Depth walk (or fragment capture) of the tall triangles, one warp each
+// (warp-strided).
+template <bool FRAGS>
 __device__ __noinline__ void walk_tall_all(const BatchDev *b, ItemAcc &acc)
 {
     const uint32_t nt_raw = *counter32(b, C_TALL);
@@ -1211,7 +1269,7 @@ __device__ __noinline__ void walk_tall_all(const BatchDev *b, ItemAcc &acc)
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, n_warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t k = gw; k < nt; k += n_warps) {
         const uint32_t i = b->tall[k];
-        const uint32_t fr = walk_tall(b, i);
+        const uint32_t fr = walk_tall<FRAGS>(b, i);
         acc.add(b, b->recs[i].item, 0ull, fr, true);
     }
 }
@@ -1703,11 +1761,6 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
 // (viewport.cpp:43-86) and post_shader_t's copy of the first layer to the
 // screen (post_shaders.hpp:22-47).  A layered batch holds one view.
 
-__device__ __forceinline__ unsigned long long *frag_counter(const BatchDev *b)
-{
-    return b->counters + C_FRAGS / 2;
-}
-
 // The fragment pool was too small: nothing is written, the host renders again.
 __device__ __forceinline__ bool frags_overflowed(const BatchDev *b)
 {
@@ -1747,9 +1800,9 @@ struct FragCount {
     }
 };
 
-// Chains every fragment of its spans to the pixels, from the triangle's
-// reserved range at `at` (pixels skipped at the near plane leave holes).
-// Spans longer than kFragInline are binned for k_frag_spans.
+// Stores every fragment of its spans from the triangle's reserved range at
+// `at` on (span_frags).  Spans longer than kFragInline are binned for
+// k_frag_spans.
 constexpr int kFragInline = 32;
 struct FragVisitor {
     const BatchDev *b;
@@ -1794,64 +1847,41 @@ struct FragVisitor {
             }
         }
         const ViewDev &v = it->v;
-        uint32_t *head = it->frag_head + ((long long)(y - v.y) * v.w - v.x);
-        Frag *pool = b->frags;
-        const uint32_t sl = slot;
-        const float pl = Ls.it.alpha, pr = Rs.it.alpha, fb = __uint_as_float(bits);
-        auto op = [&](int x, float z, float progress) {
-            const uint32_t at = (uint32_t)k + (uint32_t)(x - x1);
-            const uint32_t next = atomicExch(head + x, at);
-            reinterpret_cast<float4 *>(pool + at)[0] = make_float4(progress, pl, pr, fb);
-            reinterpret_cast<uint4 *>(pool + at)[1] = make_uint4(__float_as_uint(z), sl, next, 0u);
-        };
-        span_pixels(x1, x2, Ls, Rs, op);
+        Interp q;
+        q.init_self(Rs.x - Ls.x, Ls.it.value(), Rs.it.value());
+        q.displace((float)x1 - Ls.x);
+        span_frags(b, (uint32_t)((y - v.y) * v.w - v.x), slot, x1, x2, q, Ls.it.alpha, Rs.it.alpha, bits,
+                   (uint32_t)k);
     }
 };
 
-// Fragment capture: one thread per triangle of the walk list (the walk of
-// fill_triangle_2 from its vertices) and per near-clipped triangle.  Each
-// lane first counts its triangle's fragments; the warp then reserves its
-// lanes' ranges with one atomic and walks again to store them.
+// Fragment capture of the near-clipped triangles (the walk list is captured
+// by k_walk<true>): one thread per triangle runs fill_triangle's clip cases
+// and the fill_triangle_2 walk.  Each lane first counts its triangle's
+// fragments; the warp then reserves its lanes' ranges with one atomic and
+// walks again to store them.
 __global__ void __launch_bounds__(256) k_frags(const BatchDev *b)
 {
-    const uint32_t n_raw = *counter32(b, C_LIST), c_raw = *counter32(b, C_CLIP);
-    const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
+    const uint32_t c_raw = *counter32(b, C_CLIP);
     const uint32_t nc = c_raw < b->clip_cap ? c_raw : b->clip_cap;
     const int lane = threadIdx.x & 31;
     ItemAcc acc;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; i0 < n + nc; i0 += stride) {
+    for (uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; i0 < nc; i0 += stride) {
         const uint32_t i = i0 + (uint32_t)lane;
-        uint32_t item = 0, t = 0;
-        bool clip = false;
-        if (i < n) {
-            const uint2 e = b->list[i];
-            item = e.y;
-            t = e.x;
-        } else if (i < n + nc) {
-            const uint2 e = b->clip[b->clip_cap - 1 - (i - n)];
-            item = e.y;
-            t = e.x;
-            clip = true;
-        }
-        const ItemDev &it = b->items[item];
+        const bool valid = i < nc;
+        uint2 e = make_uint2(0u, 0u);
+        if (valid)
+            e = b->clip[b->clip_cap - 1 - i];
+        const ItemDev &it = b->items[e.y];
         auto walk = [&](auto &vis) {
-            if (i >= n + nc)
+            if (!valid)
                 return;
-            if (!clip) {
-                vis.slot = 2 * t;
-                const uint4 tri = it.s.tris[t];
-                V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
-                int pa = 0, pb = 1, pc = 2;
-                sort_z_desc(a, c1, c2, pa, pb, pc);
-                walk_sub(it.v, a, c1, c2, vis);
-            } else {
-                auto emit = [&](uint32_t slot, const TV &a, const TV &c1, const TV &c2, bool) {
-                    vis.slot = slot;
-                    walk_sub(it.v, a.vp, c1.vp, c2.vp, vis);
-                };
-                clip_triangle(it, t, emit);
-            }
+            auto emit = [&](uint32_t slot, const TV &a, const TV &c1, const TV &c2, bool) {
+                vis.slot = slot;
+                walk_sub(it.v, a.vp, c1.vp, c2.vp, vis);
+            };
+            clip_triangle(it, e.x, emit);
         };
         FragCount cnt{0u, 0ull};
         walk(cnt);
@@ -1868,9 +1898,7 @@ __global__ void __launch_bounds__(256) k_frags(const BatchDev *b)
         base = __shfl_sync(0xFFFFFFFFu, base, 31);
         FragVisitor vis{b, &it, 0u, 0ull, 0ull, base + incl - cnt.n};
         walk(vis);
-        if (!clip)
-            vis.drawn_n = 0; // the set-up counted it
-        acc.add(b, item, vis.drawn_n, vis.fragments, i < n + nc);
+        acc.add(b, e.y, vis.drawn_n, vis.fragments, valid);
     }
     acc.flush(b);
 }
@@ -1892,7 +1920,7 @@ __global__ void __launch_bounds__(256) k_frag_spans(const BatchDev *b)
     for (uint32_t i = warp; i < n; i += n_warps) {
         const SpanRec r = b->spans[i];
         const int y = (int)(r.y_bits & kYMask);
-        uint32_t *head = it.frag_head + ((long long)(y - v.y) * v.w - v.x);
+        const uint32_t row_px = (uint32_t)((y - v.y) * v.w - v.x);
         const float fb = __uint_as_float(r.y_bits & ~kYMask);
         float top = r.top, bottom = r.bottom;
         for (int x0 = r.x1; x0 < r.x2; x0 += 32) {
@@ -1911,13 +1939,30 @@ __global__ void __launch_bounds__(256) k_frag_spans(const BatchDev *b)
                 continue;
             const float alpha = mt / mb;
             const float z = r.v0 + r.dv * alpha;
-            if (below_near(z) || __float_as_uint(z) >= kMaxZBits)
-                continue;
+            const bool keep = !below_near(z) && __float_as_uint(z) < kMaxZBits;
             const uint32_t at = r.item + (uint32_t)(x - r.x1);
-            const uint32_t next = atomicExch(head + x, at);
             reinterpret_cast<float4 *>(pool + at)[0] = make_float4(alpha, r.progL, r.progR, fb);
-            reinterpret_cast<uint4 *>(pool + at)[1] = make_uint4(__float_as_uint(z), r.slot, next, 0u);
+            reinterpret_cast<uint4 *>(pool + at)[1] =
+                make_uint4(__float_as_uint(z), r.slot, keep ? row_px + (uint32_t)x : kFragEnd, 0u);
         }
+    }
+}
+
+// Chains the stored fragments to their pixels: one thread per pool entry
+// swaps itself into its pixel's list head and keeps the previous head as its
+// successor (the chain order is free: the resolve orders by depth and slot).
+__global__ void __launch_bounds__(256) k_link(const BatchDev *b)
+{
+    if (frags_overflowed(b))
+        return;
+    const uint32_t n = (uint32_t)*frag_counter(b);
+    uint32_t *head = b->items[0].frag_head;
+    uint32_t *meta = reinterpret_cast<uint32_t *>(b->frags);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t *next = meta + 8 * (size_t)i + 6; // Frag::next
+        const uint32_t px = *next;
+        if (px != kFragEnd)
+            *next = atomicExch(head + px, i);
     }
 }
 
@@ -1947,11 +1992,33 @@ __device__ __forceinline__ void resolve_pixel(const BatchDev *b, const ItemDev &
     uint32_t wz = kMaxZBits, wc = 0u;
     unsigned long long prev = 0ull;
     bool first = true;
+    // the first kChainRegs fragments of the chain are held in registers
+    constexpr int kChainRegs = 4;
+    unsigned long long ck[kChainRegs];
+    uint32_t cf[kChainRegs];
+    int held = 0;
+    uint32_t rest = head; // the chain beyond the held fragments
+#pragma unroll
+    for (int k = 0; k < kChainRegs; k++) {
+        if (rest != kFragEnd) {
+            const uint4 m = reinterpret_cast<const uint4 *>(pool + rest)[1];
+            ck[k] = ((unsigned long long)m.x << 32) | m.y;
+            cf[k] = rest;
+            held = k + 1;
+            rest = m.z;
+        }
+    }
     for (;;) {
         // the next fragment in (depth, draw order)
         unsigned long long best = ~0ull;
         uint32_t bi = kFragEnd;
-        for (uint32_t f = head; f != kFragEnd;) {
+#pragma unroll
+        for (int k = 0; k < kChainRegs; k++)
+            if (k < held && (first || ck[k] > prev) && ck[k] < best) {
+                best = ck[k];
+                bi = cf[k];
+            }
+        for (uint32_t f = rest; f != kFragEnd;) {
             const uint4 m = reinterpret_cast<const uint4 *>(pool + f)[1];
             const unsigned long long key = ((unsigned long long)m.x << 32) | m.y;
             if ((first || key > prev) && key < best) {
@@ -2201,8 +2268,10 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
         for (int k = PK_WALK; k <= PK_DOF; k++)
             mark(k);
         mark(PK_FRAGS);
-        k_frags<<<sms * 8, 256, 0, st>>>(b);
+        k_walk<true><<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
+        k_frags<<<sms * 2, 256, 0, st>>>(b);
         k_frag_spans<<<sms * 4, 256, 0, st>>>(b);
+        k_link<<<sms * 8, 256, 0, st>>>(b);
         ran(PK_FRAGS);
         mark(PK_LAYERS);
         if (flags & kSeqShaders)
@@ -2216,7 +2285,7 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
         mark(PK_COPY);
         k_copy_layer<<<sms * 8, 256, 0, st>>>(b);
         ran(PK_COPY);
-        n += 5;
+        n += 7;
         if (timed) {
             cudaEventRecord(prof->ev[kProfKernels], st);
             prof->pending = true;
@@ -2226,7 +2295,7 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
         return cudaGetLastError();
     }
     mark(PK_WALK);
-    k_walk<<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
+    k_walk<false><<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
     ran(PK_WALK);
     n++;
     mark(PK_SPANS);

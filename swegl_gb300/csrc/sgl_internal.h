@@ -1,6 +1,7 @@
 // sgl_internal.h — structures shared by the host runtime and the kernels.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -104,9 +105,10 @@ struct __align__(16) Frag {
     float4 rec;   // progress, progL, progR, span bits (as in ItemDev::prec)
     uint32_t z;   // depth bits
     uint32_t slot;
-    uint32_t next;
+    uint32_t next; // the next fragment of the pixel; before linking, the view pixel (kFragEnd: a hole)
     uint32_t pad;
 };
+static_assert(sizeof(Frag) == 32 && offsetof(Frag, next) == 24, "Frag layout");
 constexpr uint32_t kFragEnd = 0xFFFFFFFFu;
 
 constexpr uint8_t kYesDrawn = 1;  // a visible triangle flagged the vertex (renderer.cpp:86-185)
