@@ -167,7 +167,8 @@ typedef struct sgl_view {
     sgl_dof_desc dof;
     int          shader;            /* SGL_SHADER_*; 0 = Phong + bilinear */
     int          layers;            /* transparency layers (viewport_t's transparency_layer_count),
-                                       0 = opaque; 1..SGL_MAX_LAYERS, plain sgl_render only */
+                                       0 = opaque; 1..SGL_MAX_LAYERS in sgl_render and the serving
+                                       loop (not in batches, debug or allocation-free renders) */
 } sgl_view;
 
 #define SGL_MAX_LAYERS 8

@@ -6,6 +6,9 @@
 // Continuous batching: a worker thread keeps up to `streams` batches in
 // flight; whenever one finishes, its memory returns to the budget and the
 // requests that arrived meanwhile form the next batch on the freed stream.
+// A request with transparency layers runs as a batch of its own (its
+// framebuffer is the layers' surface); when its fragment pool turns out too
+// small it is launched again with a larger one before it completes.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -49,6 +52,7 @@ struct Server {
         size_t bytes = 0;
         int slot = 0;
         bool busy = false;
+        bool layered = false; // the batch is one request with transparency layers
     };
     std::vector<std::unique_ptr<LaneState>> lanes;
     std::mutex mu;
@@ -70,7 +74,10 @@ struct Server {
 
 static size_t request_bytes(const Scene *s, const sgl_view &v)
 {
-    return 8 * (size_t)v.w * v.h + view_scratch_bytes(s->n_vertices, s->n_triangles, v.w, v.h);
+    // layered views: a first fragment pool of 4 fragments per pixel (32 B
+    // each), list heads and the merged layer (4 + 4 B per pixel)
+    const size_t layers = v.layers > 0 ? 136 * (size_t)v.w * v.h : 0;
+    return 8 * (size_t)v.w * v.h + view_scratch_bytes(s->n_vertices, s->n_triangles, v.w, v.h) + layers;
 }
 
 void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
@@ -97,14 +104,16 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
         v.x = 0;
         v.y = 0;
         entries.push_back(BatchEntry{j.scene, v, pix, v.w, z});
+        entries.back().surface = pix; // a layered request's surface is its own framebuffer
         bufs.emplace_back(pix, z);
     }
+    ls.layered = jobs.size() == 1 && jobs[0].req.view.layers > 0;
     const double t0 = now_s();
     if (st == SGL_OK)
         st = ls.lane->prepare(c, entries.data(), (int)entries.size(), tile, span_bin, nullptr, &ls.slot);
     int kernels_launched = 0;
     if (st == SGL_OK)
-        st = ls.lane->launch(c, ls.slot, tile, true, &kernels_launched, nullptr);
+        st = ls.lane->launch(c, ls.slot, tile, !ls.layered, &kernels_launched, nullptr);
     {
         std::lock_guard<std::mutex> g(mu);
         batches++;
@@ -136,6 +145,18 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
 
 void Server::finish(LaneState &ls)
 {
+    if (ls.layered && !ls.jobs.empty() && ls.jobs[0].res.status == SGL_OK) {
+        bool fit = true;
+        const sgl_status st = ls.lane->layered_fit(&errors, ls.slot, &fit);
+        if (st == SGL_OK && !fit) {
+            // the fragment pool grew: render the request again (nothing was written)
+            std::vector<Job> again = std::move(ls.jobs);
+            launch_batch_on(ls, std::move(again));
+            return;
+        }
+        if (st != SGL_OK)
+            ls.jobs[0].res.status = st;
+    }
     std::vector<unsigned long long> per_item;
     sgl_status st = ls.lane->read_counters(&errors, ls.slot, nullptr, nullptr, &per_item);
     const double t = now_s();
@@ -194,11 +215,16 @@ void Server::run()
             if (free_lane) {
                 while (!pending.empty() && (int)batch.size() < opts.max_batch) {
                     Job &j = pending.front();
+                    const bool layered = j.req.view.layers > 0;
+                    if (layered && !batch.empty())
+                        break; // a layered request runs alone
                     if (in_flight_bytes + j.bytes > opts.budget_bytes && !(batch.empty() && in_flight_bytes == 0))
                         break; // wait for memory; a lone request larger than what is free still runs alone
                     in_flight_bytes += j.bytes;
                     batch.push_back(j);
                     pending.pop_front();
+                    if (layered)
+                        break;
                 }
             }
             if (batch.empty()) {
@@ -269,10 +295,10 @@ SGL_API sgl_status sgl_server_submit(sgl_server *s, const sgl_request *req, uint
     if (!scene)
         return SGL_ERR_NOT_FOUND;
     const sgl_view &v = req->view;
-    if (v.w <= 0 || v.h <= 0 || (int64_t)v.w * v.h > (1ll << 28))
+    if (v.w <= 0 || v.h <= 0 || (int64_t)v.w * v.h > (1ll << 28) || v.layers < 0 || v.layers > SGL_MAX_LAYERS)
         return SGL_ERR_INVALID;
-    if (v.layers != 0)
-        return SGL_ERR_UNSUPPORTED; // transparency layers render through sgl_render only
+    if (v.layers > 0 && v.dof.enabled)
+        return SGL_ERR_UNSUPPORTED; // depth of field on a layered view is not implemented
     Job j{};
     j.req = *req;
     j.scene = scene;

@@ -2,8 +2,8 @@
 src/render/renderer.cpp:494-550, viewport.cpp:43-86, post_shaders.hpp:22-47)
 against the oracle restatement, which the golden fixtures pin to the
 reference: the fragment pool growing, a surface with content before the
-render, device targets, the statistics, and the entry points that refuse
-layered views.
+render, device targets, the statistics, the serving loop, and the entry
+points that refuse layered views.
 
 Bar: depth bits and winners bit-exact; colour within 2 LSB per channel
 everywhere and within 1 LSB on >= 99.9% of pixels."""
@@ -120,6 +120,40 @@ def test_device_targets_match_host_targets(renderer):
     renderer.release(sid)
 
 
+def test_serving_loop_renders_layered_requests(renderer):
+    """Layered requests mixed with opaque ones in the serving loop (each
+    layered request runs alone, its framebuffer as the surface; the deep
+    stack makes the first fragment pool overflow): every frame equals
+    sgl_render's for the same view."""
+    glass = S.glass_scene()
+    stack = stack_scene()
+    gid, kid = renderer.upload(glass), renderer.upload(stack)
+    m, c = S.look_at((0.3, 0.4, 3.2), (0.0, 0.0, -0.5))
+    reqs = []
+    for k, (w, h, layers) in enumerate([(160, 120, 0), (200, 150, 3), (96, 64, 1), (320, 240, 8), (128, 96, 0),
+                                        (64, 48, 2)]):
+        v = S.view_for(w, h, m, c)
+        v.layers = layers
+        reqs.append((gid, v))
+    big = stack_view(400, 300, 4)  # > 4 fragments per pixel: the pool grows and the request is redone
+    reqs.append((kid, big))
+    srv = renderer.server(budget_bytes=512 << 20, max_batch=4, streams=2, copy_out=True)
+    outs = []
+    for sid, v in reqs:
+        pix = np.zeros((v.h, v.w), np.uint32)
+        z = np.zeros((v.h, v.w), np.float32)
+        outs.append((srv.submit(sid, v, pix, z), pix, z))
+    for (sid, v), (t, pix, z) in zip(reqs, outs):
+        res = srv.wait(t)
+        assert res["status"] == 0
+        frames, _ = renderer.render(sid, [v])
+        assert np.array_equal(pix, frames[0].pixels), (v.w, v.layers)
+        assert np.array_equal(z.view(np.uint32), frames[0].zbuffer.view(np.uint32)), (v.w, v.layers)
+    srv.close()
+    renderer.release(gid)
+    renderer.release(kid)
+
+
 def test_layered_views_are_refused_outside_sgl_render(renderer):
     torch = pytest.importorskip("torch")
     from swegl_gb300 import abi
@@ -137,11 +171,6 @@ def test_layered_views_are_refused_outside_sgl_render(renderer):
     with pytest.raises(SglError) as e:
         renderer.render_debug(sid, v)
     assert e.value.status == -8
-    srv = renderer.server()
-    with pytest.raises(SglError) as e:
-        srv.submit(sid, v)
-    assert e.value.status == -8
-    srv.close()
     v.layers = 9  # above SGL_MAX_LAYERS
     with pytest.raises(SglError) as e:
         renderer.render(sid, [v])
