@@ -313,6 +313,12 @@ typedef struct sgl_request {
     sgl_view  view;          /* x, y ignored: the frame is w x h */
     uint32_t *host_pixels;   /* w*h BGRA8, written when copy_out (may be NULL) */
     float    *host_zbuffer;  /* w*h depth, written when copy_out (may be NULL) */
+    /* Optional pose of this request alone (animated serving): the scene's
+     * n_nodes node transforms to render with, e.g. from sgl_gltf_animate at
+     * the request's time; NULL renders the scene's current nodes.  Copied at
+     * submit. */
+    const sgl_node_desc *nodes;
+    int       n_nodes;
 } sgl_request;
 
 typedef struct sgl_request_result {

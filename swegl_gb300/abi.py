@@ -95,7 +95,7 @@ class ServeOpts(C.Structure):
 
 class Request(C.Structure):
     _fields_ = [("scene_id", C.c_int), ("view", ViewDesc), ("host_pixels", C.POINTER(C.c_uint32)),
-                ("host_zbuffer", C.POINTER(C.c_float))]
+                ("host_zbuffer", C.POINTER(C.c_float)), ("nodes", C.POINTER(NodeDesc)), ("n_nodes", C.c_int)]
 
 
 class RequestResult(C.Structure):

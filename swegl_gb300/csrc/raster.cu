@@ -111,6 +111,23 @@ __global__ void k_world(SceneDev s)
     s.uv[g] = make_float2(p.w, q.w);
 }
 
+// k_world for one posed request: the same transforms under the request's
+// node matrices, into its own arrays (texture coordinates are pose-free and
+// stay the scene's).
+__global__ void k_pose(SceneDev s, const float *node_world, const float *node_rs, float4 *wpos, float4 *wnrm)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= s.n_vertices)
+        return;
+    const uint32_t n = s.vnode[g];
+    const float4 p = s.pos_u[g];
+    const float4 q = s.nrm_v[g];
+    const V3 w = transform3(mk3(p.x, p.y, p.z), node_world + 16 * n);
+    const V3 nw = normalize3(normalize3(rotate_n(mk3(q.x, q.y, q.z), node_rs + 16 * n)));
+    wpos[g] = make_float4(w.x, w.y, w.z, 0.0f);
+    wnrm[g] = make_float4(nw.x, nw.y, nw.z, 0.0f);
+}
+
 // world_to_camera_or_frustum (vertex_shaders.hpp:35-52): view, projection
 // (rows 0-2), x and y divided by |z'|; also clears the visibility flag.  The
 // item's matrices stay in registers while the grid-stride index is inside it.
@@ -2176,6 +2193,15 @@ cudaError_t launch_world(const SceneDev &s, cudaStream_t st)
     if (s.n_vertices == 0)
         return cudaSuccess;
     k_world<<<grid_for(s.n_vertices, 256), 256, 0, st>>>(s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pose(const SceneDev &s, const float *node_world, const float *node_rs, float4 *wpos, float4 *wnrm,
+                        cudaStream_t st)
+{
+    if (s.n_vertices == 0)
+        return cudaSuccess;
+    k_pose<<<grid_for(s.n_vertices, 256), 256, 0, st>>>(s, node_world, node_rs, wpos, wnrm);
     return cudaGetLastError();
 }
 

@@ -234,6 +234,11 @@ void prof_flush(Profiler *p);
 
 // kernel launchers (raster.cu)
 cudaError_t launch_world(const SceneDev &s, cudaStream_t st);
+// The world positions and normals of a scene under other node matrices
+// (`node_world`, `node_rs`, device) into `wpos` / `wnrm` (a posed request);
+// the scene's own arrays are not touched.
+cudaError_t launch_pose(const SceneDev &s, const float *node_world, const float *node_rs, float4 *wpos, float4 *wnrm,
+                        cudaStream_t st);
 // The launch sequence of a batch whose BatchDev lives at `b` (device memory).
 // `flags`: kSeqDof adds the depth-of-field gather, kSeqShaders shades with
 // every pixel shader (a view asks for another than the default).  The depth

@@ -191,6 +191,12 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         const BatchEntry &en = e[i];
         ItemDev it{};
         it.s = en.scene->dev;
+        if (en.wpos) { // a posed request: its own world positions, normals and node matrices
+            it.s.wpos = en.wpos;
+            it.s.wnrm = en.wnrm;
+            it.s.node_world = en.node_world;
+            it.s.node_rs = en.node_rs;
+        }
         it.v = make_view(en.view);
         it.ndc = (float4 *)ndc.ptr + ndc_at[i];
         it.yes = (uint8_t *)yes.ptr + yes_at[i];

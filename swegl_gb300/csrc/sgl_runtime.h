@@ -74,7 +74,16 @@ struct BatchEntry {
     int pitch_px;
     float *zbuf;           // device, w*h, may be null
     uint32_t *surface = nullptr; // device, the whole surface (row 0, column 0): views with transparency layers
+    float4 *wpos = nullptr;      // device: this view's own world positions and normals (a posed request)
+    float4 *wnrm = nullptr;
+    const float *node_world = nullptr; // device: this view's own node matrices (a posed request)
+    const float *node_rs = nullptr;
 };
+
+// node_t::get_local_world_matrix composed with the parents (16 floats per
+// node: the world matrix, and the scaled rotation that turns normals); false
+// for a cycle or a bad parent.
+bool node_matrices(const std::vector<sgl_node_desc> &nodes, std::vector<float> &world, std::vector<float> &rs);
 
 // Scratch bytes a view needs beyond its output buffers: vertex NDC and flags,
 // per-pixel keys and winner records, and its share of the batch lists.

@@ -83,7 +83,7 @@ static const float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0,
 
 // node_t::get_local_world_matrix (swegl/data/model.hpp:56-61) composed with
 // the parents as vertex_shader_t::original_to_world does (vertex_shaders.hpp:16-33)
-static bool node_matrices(const std::vector<sgl_node_desc> &nodes, std::vector<float> &world, std::vector<float> &rs)
+bool node_matrices(const std::vector<sgl_node_desc> &nodes, std::vector<float> &world, std::vector<float> &rs)
 {
     const int n = (int)nodes.size();
     world.assign(16 * (size_t)std::max(n, 1), 0.0f);

@@ -39,6 +39,7 @@ struct Job {
     Scene *scene;
     size_t bytes;
     sgl_request_result res;
+    std::vector<float> pose; // a posed request: node world matrices, then the normal matrices (16 floats per node)
 };
 
 struct Server {
@@ -48,6 +49,7 @@ struct Server {
     struct LaneState {
         std::unique_ptr<Lane> lane;
         DevBuf frames; // framebuffers of the batch in flight: colour then depth per job
+        DevBuf poses;  // posed requests: node matrices, world positions and normals per job
         std::vector<Job> jobs;
         size_t bytes = 0;
         int slot = 0;
@@ -91,9 +93,21 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
         c->fail("serving: framebuffer allocation of %zu bytes failed", fb);
         st = SGL_ERR_OOM;
     }
+    // posed requests: their node matrices and world arrays, then k_pose
+    auto pose_span = [](const Job &j) {
+        return (sizeof(float) * j.pose.size() + 16 + 32 * (size_t)j.scene->n_vertices + 255) & ~(size_t)255;
+    };
+    size_t pose_bytes = 0;
+    for (auto &j : jobs)
+        if (!j.pose.empty())
+            pose_bytes += pose_span(j);
+    if (st == SGL_OK && pose_bytes && ls.poses.ensure(pose_bytes) != cudaSuccess) {
+        c->fail("serving: pose scratch of %zu bytes failed", pose_bytes);
+        st = SGL_ERR_OOM;
+    }
     std::vector<BatchEntry> entries;
     entries.reserve(jobs.size());
-    size_t off = 0;
+    size_t off = 0, pose_off = 0;
     std::vector<std::pair<uint32_t *, float *>> bufs;
     for (auto &j : jobs) {
         const size_t px = (size_t)j.req.view.w * j.req.view.h;
@@ -106,6 +120,24 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
         entries.push_back(BatchEntry{j.scene, v, pix, v.w, z});
         entries.back().surface = pix; // a layered request's surface is its own framebuffer
         bufs.emplace_back(pix, z);
+        if (!j.pose.empty() && st == SGL_OK) {
+            uint8_t *base = (uint8_t *)ls.poses.ptr + pose_off;
+            float *mats = (float *)base;
+            const size_t nm = j.pose.size() / 2;
+            float4 *wpos = (float4 *)(base + ((sizeof(float) * j.pose.size() + 15) & ~(size_t)15));
+            float4 *wnrm = wpos + j.scene->n_vertices;
+            pose_off += pose_span(j);
+            if (cudaMemcpyAsync(mats, j.pose.data(), sizeof(float) * j.pose.size(), cudaMemcpyHostToDevice,
+                                ls.lane->stream) != cudaSuccess ||
+                launch_pose(j.scene->dev, mats, mats + nm, wpos, wnrm, ls.lane->stream) != cudaSuccess) {
+                c->fail("serving: pose of request %llu failed", (unsigned long long)j.ticket);
+                st = SGL_ERR_CUDA;
+            }
+            entries.back().wpos = wpos;
+            entries.back().wnrm = wnrm;
+            entries.back().node_world = mats;
+            entries.back().node_rs = mats + nm;
+        }
     }
     ls.layered = jobs.size() == 1 && jobs[0].req.view.layers > 0;
     const double t0 = now_s();
@@ -303,6 +335,18 @@ SGL_API sgl_status sgl_server_submit(sgl_server *s, const sgl_request *req, uint
     j.req = *req;
     j.scene = scene;
     j.bytes = request_bytes(scene, v);
+    if (req->nodes) {
+        if (req->n_nodes != (int)scene->nodes.size())
+            return SGL_ERR_INVALID; // a pose gives every node of the scene
+        std::vector<sgl_node_desc> nd(req->nodes, req->nodes + req->n_nodes);
+        std::vector<float> world, rs;
+        if (!node_matrices(nd, world, rs))
+            return SGL_ERR_INVALID;
+        j.pose = std::move(world);
+        j.pose.insert(j.pose.end(), rs.begin(), rs.end());
+        j.bytes += sizeof(float) * j.pose.size() + 32 * (size_t)scene->n_vertices + 512;
+    }
+    j.req.nodes = nullptr; // copied
     if (j.bytes > srv->opts.budget_bytes)
         return SGL_ERR_BUDGET;
     j.res.submit_s = now_s();

@@ -250,10 +250,15 @@ class Server:
         self._keep = {}
 
     def submit(self, scene_id: int, view, host_pixels: np.ndarray | None = None,
-               host_zbuffer: np.ndarray | None = None) -> int:
+               host_zbuffer: np.ndarray | None = None, nodes=None) -> int:
+        """`nodes`: an abi.NodeDesc array (every node of the scene) to render
+        this request with, e.g. GltfScene.animate(t)."""
         req = abi.Request()
         req.scene_id = scene_id
         req.view = abi.view_desc(view)
+        if nodes is not None:
+            req.nodes = C.cast(nodes, C.POINTER(abi.NodeDesc))
+            req.n_nodes = len(nodes)
         if host_pixels is not None:
             req.host_pixels = host_pixels.ctypes.data_as(C.POINTER(C.c_uint32))
         if host_zbuffer is not None:

@@ -110,3 +110,48 @@ def test_dropin_load_scene_and_animate(tmp_path):
         z = zs[off:off + v.w * v.h].reshape(v.h, v.w)
         off += v.w * v.h
         assert np.array_equal(z.view(np.uint32), exp.frames[i].zbuffer.view(np.uint32)), i
+
+
+def test_serving_loop_with_posed_requests(renderer, tmp_path):
+    """Animated serving: requests of one resident glTF scene, each with its
+    own pose (sgl_gltf_animate at the request's time, passed with the
+    request), mixed with unposed requests (the scene's current nodes) and a
+    layered one.  Every frame equals sgl_render of a copy of the scene set
+    to that pose; the shared scene's nodes are not changed."""
+    from swegl_gb300.gltf import GltfScene
+
+    path = GF.build_test_scene(str(tmp_path), True)
+    g = GltfScene(path)
+    scene = light(g.scene())
+    from swegl_gb300 import abi
+
+    sid = renderer.upload(scene)     # served
+    check = renderer.upload(scene)   # posed one pose at a time for the expected frames
+    holder = abi.SceneDescHolder(scene)
+    rest = holder.nodes              # the nodes as loaded (what unposed requests render)
+    n = len(scene.node_parent)
+    vs = views()
+    plan = [(0.35, vs[0]), (None, vs[1]), (1.6, vs[1]), (0.9, vs[0]), (None, vs[0]), (2.4, vs[1])]
+    srv = renderer.server(budget_bytes=512 << 20, max_batch=4, streams=2, copy_out=True)
+    subs = []
+    for t, v in plan:
+        nodes = g.animate(t) if t is not None else None
+        pix = np.zeros((v.h, v.w), np.uint32)
+        z = np.zeros((v.h, v.w), np.float32)
+        subs.append((srv.submit(sid, v, pix, z, nodes=nodes), pix, z, nodes))
+    for (t, v), (ticket, pix, z, nodes) in zip(plan, subs):
+        assert srv.wait(ticket)["status"] == 0
+        want = nodes if nodes is not None else rest
+        assert renderer.lib.sgl_scene_set_nodes(renderer.ctx, check, want, n) == 0
+        frames, _ = renderer.render(check, [v])
+        assert np.array_equal(pix, frames[0].pixels), t
+        assert np.array_equal(z.view(np.uint32), frames[0].zbuffer.view(np.uint32)), t
+    srv.close()
+    # the served scene still has its own nodes
+    frames_a, _ = renderer.render(sid, [vs[0]])
+    assert renderer.lib.sgl_scene_set_nodes(renderer.ctx, check, rest, n) == 0
+    frames_b, _ = renderer.render(check, [vs[0]])
+    assert np.array_equal(frames_a[0].pixels, frames_b[0].pixels)
+    renderer.release(sid)
+    renderer.release(check)
+    g.close()
