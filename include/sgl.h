@@ -167,8 +167,8 @@ typedef struct sgl_view {
     sgl_dof_desc dof;
     int          shader;            /* SGL_SHADER_*; 0 = Phong + bilinear */
     int          layers;            /* transparency layers (viewport_t's transparency_layer_count),
-                                       0 = opaque; 1..SGL_MAX_LAYERS in sgl_render and the serving
-                                       loop (not in batches, debug or allocation-free renders) */
+                                       0 = opaque; 1..SGL_MAX_LAYERS (not in debug, autotune or
+                                       allocation-free renders) */
 } sgl_view;
 
 #define SGL_MAX_LAYERS 8
@@ -269,7 +269,9 @@ typedef struct sgl_batch_item {
     sgl_target target; /* device buffers */
 } sgl_batch_item;
 
-/* Asynchronous on `stream` unless `stats` is requested (then it waits). */
+/* Asynchronous on `stream` unless `stats` is requested (then it waits).
+ * Items with transparency layers run after the others, each as its own
+ * launch sequence in item order, and the call waits for them. */
 SGL_API sgl_status sgl_render_batch(sgl_ctx *ctx, const sgl_batch_item *items, int n_items,
                                     const sgl_batch_opts *opts, void *stream, sgl_frame_stats *stats);
 /* Times every tile x span_bin choice on this batch and returns the fastest. */

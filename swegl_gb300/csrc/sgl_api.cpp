@@ -462,8 +462,6 @@ static sgl_status batch_entries(Ctx *ctx, const sgl_batch_item *items, int n, st
             return SGL_ERR_NOT_FOUND;
         }
         sgl_status st = check_view(ctx, items[i].view, items[i].target);
-        if (st == SGL_OK)
-            st = reject_layers(ctx, items[i].view);
         if (st != SGL_OK)
             return st;
         const sgl_target &t = items[i].target;
@@ -484,32 +482,53 @@ SGL_API sgl_status sgl_render_batch(sgl_ctx *c, const sgl_batch_item *items, int
     const int tile = (opts && valid_tile(opts->tile)) ? opts->tile : ctx->tile;
     const int bin = (opts && valid_span_bin(opts->span_bin)) ? opts->span_bin : ctx->inline_span;
     const bool graph = opts ? opts->use_graph != 0 : true;
-    std::vector<BatchEntry> e;
-    sgl_status r = batch_entries(ctx, items, n_items, e);
+    std::vector<BatchEntry> all;
+    sgl_status r = batch_entries(ctx, items, n_items, all);
     if (r != SGL_OK)
         return r;
+    // items with transparency layers run after the others, each as its own
+    // launch sequence, in item order (the call then waits for them)
+    std::vector<BatchEntry> e;
+    std::vector<int> layered;
+    for (int i = 0; i < n_items; i++) {
+        if (all[i].view.layers > 0)
+            layered.push_back(i);
+        else
+            e.push_back(all[i]);
+    }
     Lane *lane = nullptr;
     r = ext_lane(ctx, (cudaStream_t)stream, &lane);
     if (r != SGL_OK)
         return r;
     int slot = 0, launches = 0;
-    r = lane->prepare(ctx, e.data(), n_items, tile, bin, nullptr, &slot);
-    if (r == SGL_OK)
-        r = lane->launch(ctx, slot, tile, graph, &launches, graph ? nullptr : &ctx->prof);
-    if (r != SGL_OK)
-        return r;
-    if (stats) {
-        unsigned long long d = 0, f = 0;
-        r = lane->read_counters(ctx, slot, &d, &f, nullptr);
+    sgl_frame_stats acc{};
+    if (!e.empty()) {
+        r = lane->prepare(ctx, e.data(), (int)e.size(), tile, bin, nullptr, &slot);
+        if (r == SGL_OK)
+            r = lane->launch(ctx, slot, tile, graph, &launches, graph ? nullptr : &ctx->prof);
         if (r != SGL_OK)
             return r;
-        sgl_frame_stats acc{};
-        for (auto &en : e) {
+        if (stats) {
+            unsigned long long d = 0, f = 0;
+            r = lane->read_counters(ctx, slot, &d, &f, nullptr);
+            if (r != SGL_OK)
+                return r;
+            acc.drawn_triangles = d;
+            acc.fragments = f;
+        }
+    }
+    for (int i : layered) {
+        r = render_layered(ctx, lane, all[i], items[i].target, true, &launches, &acc, stats != nullptr);
+        if (r != SGL_OK)
+            return r;
+    }
+    if (stats) {
+        acc.triangles = 0;
+        acc.pixels = 0;
+        for (auto &en : all) {
             acc.triangles += en.scene->n_triangles;
             acc.pixels += (uint64_t)en.view.w * en.view.h;
         }
-        acc.drawn_triangles = d;
-        acc.fragments = f;
         acc.kernel_launches = (uint32_t)launches;
         *stats = acc;
     }
@@ -524,6 +543,8 @@ SGL_API sgl_status sgl_autotune(sgl_ctx *c, const sgl_batch_item *items, int n_i
     cudaSetDevice(ctx->device);
     std::vector<BatchEntry> e;
     sgl_status r = batch_entries(ctx, items, n_items, e);
+    for (int i = 0; r == SGL_OK && i < n_items; i++)
+        r = reject_layers(ctx, items[i].view); // the tuner times one launch sequence
     if (r != SGL_OK)
         return r;
     Lane *lane = nullptr;

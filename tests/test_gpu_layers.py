@@ -154,6 +154,38 @@ def test_serving_loop_renders_layered_requests(renderer):
     renderer.release(kid)
 
 
+def test_batch_with_layered_items(renderer):
+    """sgl_render_batch with opaque and layered items on device targets:
+    every item equals its own sgl_render."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+
+    from swegl_gb300 import abi
+
+    glass = S.glass_scene()
+    gid = renderer.upload(glass)
+    m, c = S.look_at((0.3, 0.4, 3.2), (0.0, 0.0, -0.5))
+    items, bufs = [], []
+    for (w, h, layers) in [(160, 120, 2), (200, 150, 0), (96, 64, 4), (128, 96, 0)]:
+        v = S.view_for(w, h, m, c)
+        v.layers = layers
+        pix = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+        z = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+        t = abi.Target()
+        t.pixels, t.pitch, t.width, t.height = pix.data_ptr(), 4 * w, w, h
+        t.zbuffer = C.cast(C.c_void_p(z.data_ptr()), C.POINTER(C.c_float))
+        items.append((gid, v, t))
+        bufs.append((pix, z))
+    stats = renderer.render_batch(items, stats=True)
+    torch.cuda.synchronize()
+    assert stats["pixels"] == sum(v.w * v.h for _, v, _ in items)
+    for (_, v, _), (pix, z) in zip(items, bufs):
+        frames, _ = renderer.render(gid, [v])
+        assert np.array_equal(pix.cpu().numpy().view(np.uint32), frames[0].pixels), (v.w, v.layers)
+        assert np.array_equal(z.cpu().numpy().view(np.uint32), frames[0].zbuffer.view(np.uint32)), (v.w, v.layers)
+    renderer.release(gid)
+
+
 def test_layered_views_are_refused_outside_sgl_render(renderer):
     torch = pytest.importorskip("torch")
     from swegl_gb300 import abi
@@ -166,7 +198,7 @@ def test_layered_views_are_refused_outside_sgl_render(renderer):
     t = abi.Target()
     t.pixels, t.pitch, t.width, t.height = pix.data_ptr(), 4 * 64, 64, 48
     with pytest.raises(SglError) as e:
-        renderer.render_batch([(sid, v, t)])
+        renderer.autotune([(sid, v, t)])
     assert e.value.status == -8
     with pytest.raises(SglError) as e:
         renderer.render_debug(sid, v)
