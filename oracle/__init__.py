@@ -5,7 +5,7 @@ CPU-baseline leg may import this package; the product never does.
 
 Two renderers share one calling convention:
   * `restatement` — oracle/sgl_oracle.c, a C restatement of gbizzotto/swegl's
-    render path (builds anywhere with gcc; travels to the GPU box as source);
+    render path (builds anywhere with gcc from its source);
   * `reference`   — the reference's own sources compiled headless by
     oracle/ref (only where the reference sources exist).  Its outputs are
     committed as golden fixtures under tests/golden.
