@@ -416,9 +416,15 @@ bool load_uri(const std::string &dir, const std::string &uri, std::vector<uint8_
     return read_file(dir.empty() ? uri : dir + "/" + uri, out);
 }
 
+// A JSON integer; non-numbers, NaN and values outside int give `dflt` or
+// an out-of-range marker that every index check rejects.
 int as_int(const Value *v, int dflt)
 {
-    return (v && v->kind == Value::Number) ? (int)v->num : dflt;
+    if (!v || v->kind != Value::Number || !(v->num == v->num))
+        return dflt;
+    if (v->num >= 2147483647.0 || v->num <= -2147483648.0)
+        return -2147483647;
+    return (int)v->num;
 }
 
 float as_float(const Value *v, float dflt)
