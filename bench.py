@@ -314,6 +314,12 @@ def cpu_frame_baseline(scene, view, args, gpu_frame=None) -> dict:
     import oracle
 
     threads = cpu_threads()
+    # single-thread latency of one frame (median of 3), then throughput on every thread
+    lat = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        oracle.render(scene, [view])
+        lat.append(time.perf_counter() - t1)
     first = oracle.render_parallel(scene, [view] * threads, threads)
     # about args.cpu_seconds of host work, one frame per thread at a time
     n, t0 = 0, time.perf_counter()
@@ -322,7 +328,8 @@ def cpu_frame_baseline(scene, view, args, gpu_frame=None) -> dict:
         n += threads
     dt = time.perf_counter() - t0
     out = {"value": round(n / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
-           "sample": f"{n} frames of the 1080p frame on {threads} threads ({dt:.1f} s)"}
+           "sample": f"{n} frames of the 1080p frame on {threads} threads ({dt:.1f} s)",
+           "single_thread_ms": round(1e3 * statistics.median(lat), 2)}
     if gpu_frame is not None:
         out["parity"] = parity_of([gpu_frame], first[:1])
     return out
