@@ -135,7 +135,7 @@ typedef struct sgl_dof_desc {
     int   enabled;
     float focus;        /* view-space focus distance */
     float aperture;     /* lens aperture in world units */
-    float max_radius;   /* circle of confusion clamp, pixels */
+    float max_radius;   /* circle of confusion clamp, pixels (0..4096) */
     float px_scale;     /* pixels per world unit at unit distance; 0 = P11*h/2 */
 } sgl_dof_desc;
 
@@ -287,7 +287,8 @@ SGL_API sgl_status sgl_autotune(sgl_ctx *ctx, const sgl_batch_item *items, int n
  * rectangle.  Per pixel: view depth z = (z' - P23) / P22 from the z-buffer,
  * circle of confusion r = K * aperture * |z - focus| / z pixels (K =
  * px_scale, or P11 * h / 2 when 0) clamped to [0, max_radius], and the mean of
- * the 32 taps of sgl_dof_taps.h at offsets roundf(r * tap) clamped to the
+ * the 32 taps of sgl_dof_taps.h at offsets r * tap rounded to the nearest
+ * integer (ties to even) and clamped to the
  * view, integer sums rounded half up; alpha is kept.  sgl_render applies the
  * same gather to every view whose dof.enabled is set. */
 SGL_API sgl_status sgl_dof(sgl_ctx *ctx, const sgl_view *view, const sgl_target *in, const sgl_target *out,

@@ -1067,8 +1067,8 @@ static void dof_gather(const sgl_view *view, const uint32_t *src, int src_pitch,
                 r = view->dof.max_radius;
             uint32_t sb = 0, sg = 0, sr = 0;
             for (int t = 0; t < SGL_DOF_TAPS; t++) {
-                int sx = x + (int)roundf(r * sgl_dof_taps[t][0]);
-                int sy = y + (int)roundf(r * sgl_dof_taps[t][1]);
+                int sx = x + (int)lrintf(r * sgl_dof_taps[t][0]); /* nearest, ties to even */
+                int sy = y + (int)lrintf(r * sgl_dof_taps[t][1]);
                 sx = sx < 0 ? 0 : (sx >= w ? w - 1 : sx);
                 sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
                 const uint32_t c = src[(long)sy * src_pitch + sx];

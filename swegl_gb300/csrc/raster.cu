@@ -1666,7 +1666,8 @@ __device__ __forceinline__ uint32_t dof_average(uint32_t centre, uint32_t sb, ui
 // swegl/render/post_shaders.hpp:51-132).  Per pixel: view-space depth from the
 // z-buffer, z = (z' - P23) / P22; circle of confusion r = K*A*|z - F| / z
 // pixels, clamped to [0, max]; the mean of 32 taps of the golden-angle
-// pattern (sgl_dof_taps.h) at offsets roundf(r * tap), clamped to the
+// pattern (sgl_dof_taps.h) at offsets r * tap rounded to the nearest integer
+// (ties to even: one conversion instruction), clamped to the
 // viewport, with integer sums rounded half up.  Every step is exact integer
 // or IEEE float arithmetic, so the CPU oracle gives the same bits.
 //
@@ -1732,7 +1733,7 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
 #pragma unroll 8
                 for (int k = 0; k < SGL_DOF_TAPS; k++) {
                     const float2 t = c_dof_taps[k];
-                    const uint32_t v = c[(int)roundf(r * t.y) * S + (int)roundf(r * t.x)];
+                    const uint32_t v = c[__float2int_rn(r * t.y) * S + __float2int_rn(r * t.x)];
                     br += v & 0x00FF00FFu;
                     ga += (v >> 8) & 0x00FF00FFu;
                 }
@@ -1742,7 +1743,7 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
 #pragma unroll 8
                 for (int k = 0; k < SGL_DOF_TAPS; k++) {
                     const float2 t = c_dof_taps[k];
-                    int sx = x + (int)roundf(r * t.x), sy = y + (int)roundf(r * t.y);
+                    int sx = x + __float2int_rn(r * t.x), sy = y + __float2int_rn(r * t.y);
                     sx = sx < 0 ? 0 : (sx >= w ? w - 1 : sx);
                     sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
                     const uint32_t v = __ldg(it.pixels + (size_t)sy * it.pitch_px + sx);

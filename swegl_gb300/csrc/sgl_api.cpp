@@ -47,6 +47,10 @@ sgl_status check_view(Ctx *ctx, const sgl_view &v, const sgl_target &t)
         ctx->fail("transparency layers %d outside 0..%d", v.layers, SGL_MAX_LAYERS);
         return SGL_ERR_INVALID;
     }
+    if (v.dof.enabled && !(v.dof.max_radius >= 0.0f && v.dof.max_radius <= 4096.0f)) {
+        ctx->fail("depth-of-field max_radius %g outside 0..4096 pixels", (double)v.dof.max_radius);
+        return SGL_ERR_INVALID;
+    }
     if (v.layers > 0 && v.dof.enabled) {
         ctx->fail("depth of field on a view with transparency layers is not implemented");
         return SGL_ERR_UNSUPPORTED;
@@ -600,6 +604,10 @@ SGL_API sgl_status sgl_dof(sgl_ctx *c, const sgl_view *view, const sgl_target *i
     sgl_status r = check_view(ctx, *view, *in);
     if (r == SGL_OK)
         r = check_view(ctx, *view, *out);
+    if (r == SGL_OK && !(view->dof.max_radius >= 0.0f && view->dof.max_radius <= 4096.0f)) {
+        ctx->fail("depth-of-field max_radius %g outside 0..4096 pixels", (double)view->dof.max_radius);
+        r = SGL_ERR_INVALID;
+    }
     if (r != SGL_OK)
         return r;
     const sgl_view &v = *view;

@@ -329,6 +329,8 @@ SGL_API sgl_status sgl_server_submit(sgl_server *s, const sgl_request *req, uint
     const sgl_view &v = req->view;
     if (v.w <= 0 || v.h <= 0 || (int64_t)v.w * v.h > (1ll << 28) || v.layers < 0 || v.layers > SGL_MAX_LAYERS)
         return SGL_ERR_INVALID;
+    if (v.dof.enabled && !(v.dof.max_radius >= 0.0f && v.dof.max_radius <= 4096.0f))
+        return SGL_ERR_INVALID;
     if (v.layers > 0 && v.dof.enabled)
         return SGL_ERR_UNSUPPORTED; // depth of field on a layered view is not implemented
     Job j{};
