@@ -2089,7 +2089,7 @@ __device__ __forceinline__ void resolve_pixel(const BatchDev *b, const ItemDev &
 // Per pixel of the layered view: pixels without fragments get the background
 // at once, the others are queued in shared memory and resolved by full warps.
 template <bool ALL_MODES>
-__global__ void __launch_bounds__(256, 3) k_layers(const BatchDev *b)
+__global__ void __launch_bounds__(256, 4) k_layers(const BatchDev *b)
 {
     if (frags_overflowed(b))
         return;
@@ -2302,9 +2302,9 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
         ran(PK_FRAGS);
         mark(PK_LAYERS);
         if (flags & kSeqShaders)
-            k_layers<true><<<sms * 3, 256, 0, st>>>(b);
+            k_layers<true><<<sms * 4, 256, 0, st>>>(b);
         else
-            k_layers<false><<<sms * 3, 256, 0, st>>>(b);
+            k_layers<false><<<sms * 4, 256, 0, st>>>(b);
         ran(PK_LAYERS);
         mark(PK_FLATTEN);
         k_flatten<<<sms * 8, 256, 0, st>>>(b);
