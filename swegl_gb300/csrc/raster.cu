@@ -1547,7 +1547,7 @@ __device__ __forceinline__ uint32_t shade_rec(const ItemDev &it, uint4 q7, uint3
 // are reset to empty for the next launch sequence (unless kept for debug).
 constexpr int kShadeThreads = 256;
 #ifndef SGL_SHADE_MIN_BLOCKS
-#define SGL_SHADE_MIN_BLOCKS 4 // resident blocks per SM the shade is compiled for
+#define SGL_SHADE_MIN_BLOCKS 5 // resident blocks per SM the shade is compiled for
 #endif
 template <int TILE, bool ALL_MODES>
 __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(const BatchDev *b)
