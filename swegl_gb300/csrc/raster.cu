@@ -130,7 +130,10 @@ __global__ void k_pose(SceneDev s, const float *node_world, const float *node_rs
 
 // world_to_camera_or_frustum (vertex_shaders.hpp:35-52): view, projection
 // (rows 0-2), x and y divided by |z'|; also clears the visibility flag.  The
-// item's matrices stay in registers while the grid-stride index is inside it.
+// item's matrices stay in registers while the index is inside it.  Each
+// thread takes kGeomPer vertices (a warp 32 * kGeomPer consecutive ones) and
+// issues their loads first.
+constexpr int kGeomPer = 4;
 __global__ void __launch_bounds__(256) k_vertex(const BatchDev *b)
 {
     uint32_t lo = 0, hi = 0;
@@ -139,23 +142,21 @@ __global__ void __launch_bounds__(256) k_vertex(const BatchDev *b)
     float4 *ndc = nullptr;
     uint8_t *yes = nullptr;
     const uint32_t total = b->total_vtx;
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-        if (g < lo || g >= hi) {
-            const int item = find_item(b->vtx_base, b->n_items, g);
-            lo = __ldg(b->vtx_base + item);
-            hi = __ldg(b->vtx_base + item + 1);
-            const ItemDev &it = b->items[item];
+    auto bind = [&](uint32_t g) {
+        const int item = find_item(b->vtx_base, b->n_items, g);
+        lo = __ldg(b->vtx_base + item);
+        hi = __ldg(b->vtx_base + item + 1);
+        const ItemDev &it = b->items[item];
 #pragma unroll
-            for (int k = 0; k < 12; k++) {
-                m[k] = it.v.view[k];
-                m[12 + k] = it.v.proj[k];
-            }
-            wpos = it.s.wpos;
-            ndc = it.ndc;
-            yes = it.yes;
+        for (int k = 0; k < 12; k++) {
+            m[k] = it.v.view[k];
+            m[12 + k] = it.v.proj[k];
         }
-        const uint32_t l = g - lo;
-        const float4 w = wpos[l];
+        wpos = it.s.wpos;
+        ndc = it.ndc;
+        yes = it.yes;
+    };
+    auto project = [&](uint32_t l, float4 w) {
         V3 p = transform3(mk3(w.x, w.y, w.z), m);
         p = transform3(p, m + 12);
         if (p.z != 0.0f) {
@@ -164,6 +165,30 @@ __global__ void __launch_bounds__(256) k_vertex(const BatchDev *b)
         }
         ndc[l] = make_float4(p.x, p.y, p.z, 0.0f);
         yes[l] = below_near(p.z) ? kYesBehind : 0; // kYesDrawn is set by k_flags
+    };
+    // a warp takes 32 * kGeomPer consecutive vertices, lane + 32 u each
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x * kGeomPer;
+    for (uint32_t g0 = ((blockIdx.x * blockDim.x + threadIdx.x) & ~31u) * kGeomPer + lane; g0 < total; g0 += stride) {
+        const uint32_t glast = g0 + 32 * (kGeomPer - 1);
+        if (g0 < lo || g0 >= hi)
+            bind(g0);
+        if (glast < hi && glast < total) {
+            const uint32_t l = g0 - lo;
+            float4 w[kGeomPer];
+#pragma unroll
+            for (int u = 0; u < kGeomPer; u++)
+                w[u] = wpos[l + 32 * u];
+#pragma unroll
+            for (int u = 0; u < kGeomPer; u++)
+                project(l + 32 * u, w[u]);
+        } else {
+            for (uint32_t g = g0; g <= glast && g < total; g += 32) {
+                if (g < lo || g >= hi)
+                    bind(g);
+                project(g - lo, wpos[g - lo]);
+            }
+        }
     }
 }
 
