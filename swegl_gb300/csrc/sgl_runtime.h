@@ -19,6 +19,7 @@ constexpr int kMaxBatch = 4096; // views per batch
     do {                                                                                                               \
         cudaError_t _e = (expr);                                                                                       \
         if (_e != cudaSuccess) {                                                                                       \
+            cudaGetLastError(); /* a failed call's error must not surface in a later launch check */                  \
             ctx->fail("%s: %s", #expr, cudaGetErrorString(_e));                                                        \
             return _e == cudaErrorMemoryAllocation ? SGL_ERR_OOM : SGL_ERR_CUDA;                                       \
         }                                                                                                              \

@@ -334,7 +334,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     CUDA_TRY(upload(d_nrm_v, nrm_v.data(), nrm_v.size()));
     CUDA_TRY(upload(d_vnode, vnode.data(), vnode.size()));
     CUDA_TRY(upload(d_tris, tris.data(), tris.size()));
-    CUDA_TRY(upload(d_prims, prims.data(), std::max<size_t>(prims.size(), 1)));
+    CUDA_TRY(upload(d_prims, prims.data(), prims.size()));
     CUDA_TRY(upload(d_mats, mats.data(), mats.size()));
     CUDA_TRY(upload(d_texs, texs.data(), texs.size()));
     CUDA_TRY(d_wpos.ensure(sizeof(float4) * std::max<size_t>(n_vertices, 1)));
