@@ -94,3 +94,38 @@ def test_degenerate_sliver_and_edge_triangles(renderer):
     for k, (x, y) in enumerate([(0, 0), (160, 0), (0, 120), (300, 0)]):
         views[k].x, views[k].y = x, y
     check(renderer, s, views, shared=(320, 240))
+
+
+def test_empty_and_degenerate_scenes_in_every_entry_point(renderer):
+    """Zero-work cases through the layered path, a batch and the serving loop."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+
+    from swegl_gb300 import abi
+
+    empty = lit(S.Scene()).finalize()
+    eid = renderer.upload(empty)
+    v = cam(40, 30, layers=3)
+    frames, _ = renderer.render(eid, [v])
+    assert not frames[0].pixels.any()
+    pix = torch.ones((30, 40), dtype=torch.int32, device="cuda")
+    z = torch.zeros((30, 40), dtype=torch.float32, device="cuda")
+    t = abi.Target()
+    t.pixels, t.pitch, t.width, t.height = pix.data_ptr(), 160, 40, 30
+    t.zbuffer = C.cast(C.c_void_p(z.data_ptr()), C.POINTER(C.c_float))
+    opaque = cam(40, 30)
+    renderer.render_batch([(eid, opaque, t), (eid, v, t)])
+    torch.cuda.synchronize()
+    assert not pix.any().item()
+    srv = renderer.server(budget_bytes=64 << 20, max_batch=4, streams=2, copy_out=True)
+    outs = []
+    for view in (opaque, v):
+        hp = np.full((30, 40), 7, np.uint32)
+        hz = np.zeros((30, 40), np.float32)
+        outs.append((srv.submit(eid, view, hp, hz), hp, hz))
+    for ticket, hp, hz in outs:
+        assert srv.wait(ticket)["status"] == 0
+        assert not hp.any()
+        assert np.all(hz.view(np.uint32) == 0x7F7F7F7F)
+    srv.close()
+    renderer.release(eid)
