@@ -290,6 +290,19 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
             if (ya & yb & yc & kYesDrawn) {
                 // fill_triangle's cases (renderer.cpp:281-318): the smallest z' decides
                 list = ((ya | yb | yc) & kYesBehind) ? 1 : 0;
+                if (list == 0) {
+                    // fill_triangle_2 draws nothing when its first and last rows
+                    // coincide (ceil of the smallest and largest y, renderer.cpp:
+                    // 389-391): such a triangle never reaches the set-up or the walk
+                    const ItemDev &it = b->items[item];
+                    const float y0 = it.v.vm11 * it.ndc[tri.x].y + it.v.vm13;
+                    const float y1 = it.v.vm11 * it.ndc[tri.y].y + it.v.vm13;
+                    const float y2 = it.v.vm11 * it.ndc[tri.z].y + it.v.vm13;
+                    // (finite or infinite y only: with a NaN the set-up's sort decides)
+                    const float lo_y = fminf(y0, fminf(y1, y2)), hi_y = fmaxf(y0, fmaxf(y1, y2));
+                    if (y0 == y0 && y1 == y1 && y2 == y2 && f2i(ceilf(lo_y)) == f2i(ceilf(hi_y)))
+                        list = -1;
+                }
             }
         }
         uint32_t pos = 0;
