@@ -209,6 +209,7 @@ __device__ __forceinline__ V3 ld3(const float4 *a, uint32_t i)
 
 // Visibility flags (renderer.cpp:86-185): inside the frustum and (double sided
 // or front facing, front_face_visible :72-75, on the draw-order triple).
+constexpr int kFlagsPer = 2;
 __global__ void __launch_bounds__(256) k_flags(const BatchDev *b)
 {
     uint32_t lo = 0, hi = 0;
@@ -219,29 +220,64 @@ __global__ void __launch_bounds__(256) k_flags(const BatchDev *b)
     const MatDesc *mats = nullptr;
     int n_mats = 0;
     const uint32_t total = b->total_tri;
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-        if (g < lo || g >= hi) {
-            const int item = find_item(b->tri_base, b->n_items, g);
-            lo = __ldg(b->tri_base + item);
-            hi = __ldg(b->tri_base + item + 1);
-            const ItemDev &it = b->items[item];
-            tris = it.s.tris;
-            ndc = it.ndc;
-            yes = it.yes;
-            prims = it.s.prims;
-            mats = it.s.mats;
-            n_mats = it.s.n_mats;
-        }
-        const uint4 tri = tris[g - lo];
-        const V3 a = ld3(ndc, tri.x), c1 = ld3(ndc, tri.y), c2 = ld3(ndc, tri.z);
+    auto bind = [&](uint32_t g) {
+        const int item = find_item(b->tri_base, b->n_items, g);
+        lo = __ldg(b->tri_base + item);
+        hi = __ldg(b->tri_base + item + 1);
+        const ItemDev &it = b->items[item];
+        tris = it.s.tris;
+        ndc = it.ndc;
+        yes = it.yes;
+        prims = it.s.prims;
+        mats = it.s.mats;
+        n_mats = it.s.n_mats;
+    };
+    auto flag = [&](uint4 tri, V3 a, V3 c1, V3 c2) {
         if (!inside_frustum(a, c1, c2))
-            continue;
-        const int m = prims[tri.w].material;
-        const int ds = (m >= 0 && m < n_mats) ? mats[m].double_sided : 0;
-        if (ds || cross_n_z(sub3(c1, a), sub3(c2, a)) > 0.0f) {
+            return;
+        // front facing, else double sided (the material is read only then)
+        bool vis = cross_n_z(sub3(c1, a), sub3(c2, a)) > 0.0f;
+        if (!vis) {
+            const int m = prims[tri.w].material;
+            vis = m >= 0 && m < n_mats && mats[m].double_sided;
+        }
+        if (vis) {
             yes[tri.x] = kYesDrawn | (below_near(a.z) ? kYesBehind : 0);
             yes[tri.y] = kYesDrawn | (below_near(c1.z) ? kYesBehind : 0);
             yes[tri.z] = kYesDrawn | (below_near(c2.z) ? kYesBehind : 0);
+        }
+    };
+    // a warp takes 32 * kFlagsPer consecutive triangles, lane + 32 u each,
+    // and issues all their loads before the tests
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x * kFlagsPer;
+    for (uint32_t g0 = ((blockIdx.x * blockDim.x + threadIdx.x) & ~31u) * kFlagsPer + lane; g0 < total; g0 += stride) {
+        const uint32_t glast = g0 + 32 * (kFlagsPer - 1);
+        if (g0 < lo || g0 >= hi)
+            bind(g0);
+        if (glast < hi && glast < total) {
+            const uint32_t l = g0 - lo;
+            uint4 t[kFlagsPer];
+#pragma unroll
+            for (int u = 0; u < kFlagsPer; u++)
+                t[u] = tris[l + 32 * u];
+            V3 a[kFlagsPer], c1[kFlagsPer], c2[kFlagsPer];
+#pragma unroll
+            for (int u = 0; u < kFlagsPer; u++) {
+                a[u] = ld3(ndc, t[u].x);
+                c1[u] = ld3(ndc, t[u].y);
+                c2[u] = ld3(ndc, t[u].z);
+            }
+#pragma unroll
+            for (int u = 0; u < kFlagsPer; u++)
+                flag(t[u], a[u], c1[u], c2[u]);
+        } else {
+            for (uint32_t g = g0; g <= glast && g < total; g += 32) {
+                if (g < lo || g >= hi)
+                    bind(g);
+                const uint4 tri = tris[g - lo];
+                flag(tri, ld3(ndc, tri.x), ld3(ndc, tri.y), ld3(ndc, tri.z));
+            }
         }
     }
 }
