@@ -133,12 +133,21 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def frame_alg_bytes(scene, w: int, h: int) -> int:
+def frame_alg_bytes(scene, w: int, h: int, dof: bool = False) -> int:
     """Algorithmic bytes of one frame: 32 B per vertex (position, normal, uv),
     4 B per index, 4 B per texel of every texture, 8 B per viewport pixel
-    (BGRA8 colour + FP32 depth written once)."""
+    (BGRA8 colour + FP32 depth written once); with depth of field 12 B more
+    per pixel (the gather reads colour and depth once and writes colour)."""
     texels = sum(int(t.size) for t in scene.textures)
-    return 32 * len(scene.positions) + 4 * len(scene.indices) + 4 * texels + 8 * w * h
+    return 32 * len(scene.positions) + 4 * len(scene.indices) + 4 * texels + (20 if dof else 8) * w * h
+
+
+# The plain-renderer frame workloads: (config name, viewport, depth of field,
+# committed ncu traffic summary)
+FRAMES = {
+    "frame": ("spheres200_1080p_frame", (1920, 1080), False, "frame_1080p_traffic.md"),
+    "dof": ("spheres200_4k_dof_frame", (3840, 2160), True, "frame_4k_dof_traffic.md"),
+}
 
 
 def cpu_threads() -> int:
@@ -185,14 +194,18 @@ def replica_throughput(frames_per_rank: int, world: int, max_ms: float) -> float
 
 
 # ------------------------------------------------------- single-frame stage --
-def frame_measure(r, torch, steps: int, warmup: int, with_e2e: bool):
-    """The plain renderer on the 1080p 200-sphere frame; 4 resident copies of
-    the scene (~400 MB, above the 129 MB L2) rendered in rotation."""
+def frame_measure(r, torch, steps: int, warmup: int, with_e2e: bool, kind: str = "frame"):
+    """The plain renderer on a frame of the 200-sphere scene (the 1080p
+    frame, or the 3840x2160 frame with depth of field: focus 20, aperture
+    0.05, radius at most 16 px, 32 taps); 4 resident copies of the scene
+    (~400 MB, above the 129 MB L2) rendered in rotation."""
     from swegl_gb300 import abi
     from swegl_gb300 import scenes as S
 
+    _, (w, h), dof, _ = FRAMES[kind]
     scene = S.spheres_scene()
-    v = S.spheres_view(1920, 1080)
+    v = S.spheres_view(w, h)
+    v.dof = dof
     copies = [r.upload(scene) for _ in range(4)]
     stream = torch.cuda.Stream()
     _bufs, tgt = device_target(torch, v.w, v.h)
@@ -220,7 +233,8 @@ def frame_measure(r, torch, steps: int, warmup: int, with_e2e: bool):
     torch.cuda.synchronize()
     prof = r.profile_read()
     r.profile(False)
-    out = {"frame_ms": frame_ms, "stats": stats, "prof": prof, "alg_bytes": frame_alg_bytes(scene, v.w, v.h),
+    out = {"frame_ms": frame_ms, "stats": stats, "prof": prof, "alg_bytes": frame_alg_bytes(scene, v.w, v.h, dof),
+           "kind": kind,
            "gpu_frame": (_bufs[0].cpu().numpy().view(np.uint32), _bufs[1].cpu().numpy())}
     if with_e2e:
         host_pix = torch.zeros((v.h, v.w), dtype=torch.int32).pin_memory()
@@ -251,13 +265,14 @@ def frame_measure(r, torch, steps: int, warmup: int, with_e2e: bool):
 
 def roofline_of(fm: dict) -> dict:
     peaks = measured_peaks()
+    _, (w, h), dof, traffic = FRAMES[fm.get("kind", "frame")]
     achieved = fm["alg_bytes"] / (fm["frame_ms"] / 1e3) / 1e9
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": peaks["source"],
-            "unit_of_work": "one 1920x1080 frame of the 819,200-triangle scene (%d algorithmic bytes)"
-                            % fm["alg_bytes"],
+            "unit_of_work": "one %dx%d frame%s of the 819,200-triangle scene (%d algorithmic bytes)"
+                            % (w, h, " with depth of field" if dof else "", fm["alg_bytes"]),
             "frame_us": round(1e3 * fm["frame_ms"], 2),
-            "traffic": profile_traffic("frame_1080p_traffic.md")}
+            "traffic": profile_traffic(traffic)}
 
 
 def kernels_of(fm: dict) -> dict:
@@ -281,18 +296,20 @@ def run_frame(args, rank, world, local_rank):
     if dist:
         dist.barrier()
     with ClockSampler(local_rank) as clocks:
-        fm = frame_measure(r, torch, args.steps, args.warmup, True)
+        fm = frame_measure(r, torch, args.steps, args.warmup, True, args.workload)
     frame_ms = max_over_ranks(torch, dist, fm["frame_ms"])
+    name, (w, h), dof, _ = FRAMES[args.workload]
     fps = world * 1e3 / frame_ms
     e2e = sum_over_ranks(torch, dist, fm["e2e_fps"]) if dist else fm["e2e_fps"]
     prof = fm["prof"]
     out = {
-        "metric": "frames/s (plain renderer, one 1080p frame per launch sequence)",
+        "metric": "frames/s (plain renderer, one %dx%d frame%s per launch sequence)"
+                  % (w, h, " with depth of field" if dof else ""),
         "value": round(fps, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(frame_ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic (seeded scenes, swegl_gb300/scenes.py)",
-        "config": {"workload": "spheres200_1080p_frame", "triangles": fm["scene"].n_triangles,
-                   "viewport": "1920x1080", "l2": "inputs larger than L2: 4 resident scene copies in rotation"},
+        "config": {"workload": name, "triangles": fm["scene"].n_triangles, "viewport": "%dx%d" % (w, h),
+                   "l2": "inputs larger than L2: 4 resident scene copies in rotation"},
         "gfragments_per_s": round(fm["stats"]["fragments"] * fps / 1e9, 3),
         "kernels": kernels_of(fm),
         "dominant_kernel": max(prof.items(), key=lambda kv: kv[1]["total_ms"])[0] if prof else None,
@@ -328,7 +345,8 @@ def cpu_frame_baseline(scene, view, args, gpu_frame=None) -> dict:
         n += threads
     dt = time.perf_counter() - t0
     out = {"value": round(n / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
-           "sample": f"{n} frames of the 1080p frame on {threads} threads ({dt:.1f} s)",
+           "sample": f"{n} frames of the {view.w}x{view.h} frame{' with depth of field' if view.dof else ''} "
+                     f"on {threads} threads ({dt:.1f} s)",
            "single_thread_ms": round(1e3 * statistics.median(lat), 2)}
     if gpu_frame is not None:
         out["parity"] = parity_of([gpu_frame], first[:1])
@@ -753,14 +771,14 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["serve", "frame", "layers"], default="serve")
+    ap.add_argument("--workload", choices=["serve", "frame", "dof", "layers"], default="serve")
     ap.add_argument("--requests-per-step", type=int, default=256)
     ap.add_argument("--seq-requests", type=int, default=512)
     ap.add_argument("--duration", type=float, default=10.0, help="open-loop latency run, seconds")
     ap.add_argument("--budget", type=int, default=40 << 30)
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--streams", type=int, default=3)
-    ap.add_argument("--cpu-frames", type=int, default=4096, help="CPU baseline: at most this many 1080p frames")
+    ap.add_argument("--cpu-frames", type=int, default=4096, help="CPU baseline: at most this many frames")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline: about this much host work")
     ap.add_argument("--cpu-requests", type=int, default=48)
     ap.add_argument("--cpu-requests-per-step", type=int, default=32)
@@ -770,7 +788,7 @@ def main():
     rank, world, local_rank = env_rank()
     if args.impl == "reference":
         out = run_reference(args, rank, world)
-    elif args.workload == "frame":
+    elif args.workload in FRAMES:
         out = run_frame(args, rank, world, local_rank)
     elif args.workload == "layers":
         out = run_layers(args, rank, world, local_rank)

@@ -69,7 +69,8 @@ typedef struct sgl_node_desc {
 } sgl_node_desc;
 
 /* primitive_t (swegl/data/model.hpp:31-48).  Vertices are owned by the
- * primitive: indices are local to [vertex_offset, vertex_offset+vertex_count). */
+ * primitive: indices are local to [vertex_offset, vertex_offset+vertex_count),
+ * and the vertex ranges of two primitives do not overlap (SGL_ERR_INVALID). */
 typedef struct sgl_primitive_desc {
     int      node;
     int      mode;          /* SGL_TRIANGLES / SGL_TRIANGLE_STRIP / SGL_TRIANGLE_FAN */

@@ -1793,23 +1793,41 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
             __syncthreads();
         }
         for (int p = threadIdx.x; p < kDofTile * kDofTile; p += blockDim.x) {
+            // a warp takes one row of 32 pixels of the tile
             const int x = x0 + (p & (kDofTile - 1)), y = y0 + p / kDofTile;
-            if (x >= w || y >= h)
-                continue;
-            const uint32_t i = (uint32_t)y * (uint32_t)w + (uint32_t)x;
+            if (y >= h)
+                continue; // the whole warp
+            const bool valid = x < w;
+            const int xs = valid ? x : x0; // lanes past the view's right edge work on a pixel inside
+            const uint32_t i = (uint32_t)y * (uint32_t)w + (uint32_t)xs;
             const float r = dof_radius(it, i);
             uint32_t out;
             if (R >= 0) {
                 // the halo holds the view-clamped pixels, so a tap needs no clamp:
                 // |offset| <= ceil(r) <= R keeps it inside
-                const uint32_t *c = halo + (y - y0 + R) * S + (x - x0 + R);
+                const uint32_t *c = halo + (y - y0 + R) * S + (xs - x0 + R);
                 uint32_t br = 0, ga = 0; // two 16-bit lanes each: 32 taps x 255 fit
+                const float r0 = __shfl_sync(0xFFFFFFFFu, r, 0);
+                if (__all_sync(0xFFFFFFFFu, !valid || r == r0)) {
+                    // one radius for the warp (the clamped radius, or the empty
+                    // background's): lane k makes tap k's offset once
+                    static_assert(SGL_DOF_TAPS == 32, "one tap per lane");
+                    const float2 t = c_dof_taps[threadIdx.x & 31];
+                    const int off = __float2int_rn(r0 * t.y) * S + __float2int_rn(r0 * t.x);
 #pragma unroll 8
-                for (int k = 0; k < SGL_DOF_TAPS; k++) {
-                    const float2 t = c_dof_taps[k];
-                    const uint32_t v = c[__float2int_rn(r * t.y) * S + __float2int_rn(r * t.x)];
-                    br += v & 0x00FF00FFu;
-                    ga += (v >> 8) & 0x00FF00FFu;
+                    for (int k = 0; k < SGL_DOF_TAPS; k++) {
+                        const uint32_t v = c[__shfl_sync(0xFFFFFFFFu, off, k)];
+                        br += v & 0x00FF00FFu;
+                        ga += (v >> 8) & 0x00FF00FFu;
+                    }
+                } else {
+#pragma unroll 8
+                    for (int k = 0; k < SGL_DOF_TAPS; k++) {
+                        const float2 t = c_dof_taps[k];
+                        const uint32_t v = c[__float2int_rn(r * t.y) * S + __float2int_rn(r * t.x)];
+                        br += v & 0x00FF00FFu;
+                        ga += (v >> 8) & 0x00FF00FFu;
+                    }
                 }
                 out = dof_average(c[0], br & 0xFFFFu, ga & 0xFFFFu, br >> 16);
             } else {
@@ -1817,7 +1835,7 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
 #pragma unroll 8
                 for (int k = 0; k < SGL_DOF_TAPS; k++) {
                     const float2 t = c_dof_taps[k];
-                    int sx = x + __float2int_rn(r * t.x), sy = y + __float2int_rn(r * t.y);
+                    int sx = xs + __float2int_rn(r * t.x), sy = y + __float2int_rn(r * t.y);
                     sx = sx < 0 ? 0 : (sx >= w ? w - 1 : sx);
                     sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
                     const uint32_t v = __ldg(it.pixels + (size_t)sy * it.pitch_px + sx);
@@ -1825,9 +1843,10 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                     sg += (v >> 8) & 0xFFu;
                     sr += (v >> 16) & 0xFFu;
                 }
-                out = dof_average(it.pixels[(size_t)y * it.pitch_px + x], sb, sg, sr);
+                out = dof_average(it.pixels[(size_t)y * it.pitch_px + xs], sb, sg, sr);
             }
-            it.dof_out[(size_t)y * it.dof_pitch + x] = out;
+            if (valid)
+                it.dof_out[(size_t)y * it.dof_pitch + x] = out;
         }
         if (R >= 0)
             __syncthreads(); // the halo is reused by the next tile

@@ -248,6 +248,25 @@ static sgl_status validate_scene(Ctx *ctx, const sgl_scene_desc *d)
         ctx->fail("too many triangles (%llu)", (unsigned long long)tris);
         return SGL_ERR_UNSUPPORTED;
     }
+    // every primitive owns its vertices (primitive_t::vertices): no two
+    // vertex ranges overlap
+    std::vector<std::pair<uint32_t, int>> ranges;
+    ranges.reserve(d->n_primitives);
+    for (int p = 0; p < d->n_primitives; p++)
+        if (d->primitives[p].vertex_count)
+            ranges.emplace_back(d->primitives[p].vertex_offset, p);
+    std::sort(ranges.begin(), ranges.end());
+    uint64_t end = 0;
+    int end_prim = -1;
+    for (const auto &r : ranges) {
+        if (r.first < end) {
+            ctx->fail("primitives %d and %d share vertices (each primitive owns its vertex range)", end_prim,
+                      r.second);
+            return SGL_ERR_INVALID;
+        }
+        end = (uint64_t)r.first + d->primitives[r.second].vertex_count;
+        end_prim = r.second;
+    }
     return SGL_OK;
 }
 
