@@ -289,6 +289,69 @@ __device__ __forceinline__ V3 load_vp(const ItemDev &it, uint32_t g)
     return mk3(it.v.vm00 * n.x + it.v.vm03, it.v.vm11 * n.y + it.v.vm13, n.z);
 }
 
+// Per-item counters of a warp: lanes grouped by item, one atomic per group.
+__device__ __forceinline__ void item_add(unsigned long long *dst, uint32_t item, unsigned long long v, bool valid)
+{
+    const unsigned act = __ballot_sync(0xFFFFFFFFu, valid);
+    if (!valid)
+        return;
+    const unsigned grp = __match_any_sync(act, item);
+    unsigned long long sum = 0;
+    for (unsigned m = grp; m; m &= m - 1)
+        sum += __shfl_sync(grp, v, __ffs(m) - 1);
+    if ((threadIdx.x & 31) == __ffs(grp) - 1 && sum)
+        atomicAdd(dst + 2 * (size_t)item, sum);
+}
+
+__device__ __forceinline__ void warp_add(unsigned long long *dst, unsigned long long v)
+{
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+    if ((threadIdx.x & 31) == 0 && v)
+        atomicAdd(dst, v);
+}
+
+// Per-item counters (drawn triangles, fragments) of a warp, summed in
+// registers while all of the warp's lanes work on one item and added to the
+// item's counters when the item changes (one atomic per counter then); an
+// iteration whose lanes span several items adds per item at once.  Every
+// lane of the warp calls add() and flush().
+struct ItemAcc {
+    uint32_t item = 0xFFFFFFFFu;
+    unsigned long long v0 = 0, v1 = 0;
+
+    __device__ __forceinline__ void flush(const BatchDev *b)
+    {
+        if (item != 0xFFFFFFFFu) {
+            warp_add(b->item_counters + 2 * (size_t)item, v0);
+            warp_add(b->item_counters + 2 * (size_t)item + 1, v1);
+        }
+        item = 0xFFFFFFFFu;
+        v0 = v1 = 0;
+    }
+    __device__ __forceinline__ void add(const BatchDev *b, uint32_t it, unsigned long long a0, unsigned long long a1,
+                                        bool valid)
+    {
+        const unsigned act = __ballot_sync(0xFFFFFFFFu, valid);
+        if (!act)
+            return;
+        const uint32_t first = __shfl_sync(0xFFFFFFFFu, it, __ffs(act) - 1);
+        if (__all_sync(0xFFFFFFFFu, !valid || it == first)) {
+            if (first != item) {
+                flush(b);
+                item = first;
+            }
+            if (valid) {
+                v0 += a0;
+                v1 += a1;
+            }
+        } else {
+            item_add(b->item_counters, it, a0, valid);
+            item_add(b->item_counters + 1, it, a1, valid);
+        }
+    }
+};
+
 // Drawable triangles (all three vertices flagged, renderer.cpp:248-253) into
 // the walk list; triangles crossing the near plane go to their own list and
 // are marked in the record map.  One global atomic per list per block.
@@ -302,6 +365,7 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
     const uint4 *tris = nullptr;
     const uint8_t *yes = nullptr;
     const uint32_t total = b->total_tri;
+    ItemAcc acc; // triangles counted as drawn here (no pixel column)
     // every thread of the block runs the same number of iterations (barriers inside)
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t g0 = blockIdx.x * blockDim.x; g0 < total; g0 += stride) {
@@ -310,6 +374,7 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
         __syncthreads();
         const uint32_t g = g0 + threadIdx.x;
         int list = -1;
+        bool xsliver = false;
         uint32_t t = 0;
         if (g < total) {
             if (g < lo || g >= hi) {
@@ -327,20 +392,49 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
                 // fill_triangle's cases (renderer.cpp:281-318): the smallest z' decides
                 list = ((ya | yb | yc) & kYesBehind) ? 1 : 0;
                 if (list == 0) {
-                    // fill_triangle_2 draws nothing when its first and last rows
-                    // coincide (ceil of the smallest and largest y, renderer.cpp:
-                    // 389-391): such a triangle never reaches the set-up or the walk
                     const ItemDev &it = b->items[item];
                     const float y0 = it.v.vm11 * it.ndc[tri.x].y + it.v.vm13;
                     const float y1 = it.v.vm11 * it.ndc[tri.y].y + it.v.vm13;
                     const float y2 = it.v.vm11 * it.ndc[tri.z].y + it.v.vm13;
-                    // (finite or infinite y only: with a NaN the set-up's sort decides)
                     const float lo_y = fminf(y0, fminf(y1, y2)), hi_y = fmaxf(y0, fmaxf(y1, y2));
-                    if (y0 == y0 && y1 == y1 && y2 == y2 && f2i(ceilf(lo_y)) == f2i(ceilf(hi_y)))
-                        list = -1;
+                    // (finite or infinite y only: with a NaN the set-up's sort decides)
+                    if (y0 == y0 && y1 == y1 && y2 == y2) {
+                        if (f2i(ceilf(lo_y)) == f2i(ceilf(hi_y))) {
+                            // fill_triangle_2 draws nothing when its first and last
+                            // rows coincide (ceil of the smallest and largest y,
+                            // renderer.cpp:389-391): such a triangle never reaches
+                            // the set-up or the walk, and is not counted
+                            list = -1;
+                        } else {
+                            // No pixel column either: every row's span [ceil(xl),
+                            // ceil(xr)) is empty when the triangle's x range, widened
+                            // by the walk's rounding, holds no integer boundary.  The
+                            // walked edge positions are the exact ones (inside the
+                            // range) up to the start's rounding and one rounding per
+                            // row step, (rows + 17) u (max |x| + eps) in all (u =
+                            // 2^-24); eps is over twice that.  Such a triangle reached
+                            // the set-up in the reference, so it is counted as drawn,
+                            // but it covers no pixel and gets no set-up record.
+                            const float x0 = it.v.vm00 * it.ndc[tri.x].x + it.v.vm03;
+                            const float x1 = it.v.vm00 * it.ndc[tri.y].x + it.v.vm03;
+                            const float x2 = it.v.vm00 * it.ndc[tri.z].x + it.v.vm03;
+                            const float mx = fmaxf(fabsf(x0), fmaxf(fabsf(x1), fabsf(x2)));
+                            const float rows = ceilf(hi_y) - ceilf(lo_y);
+                            const float eps = (rows + 32.0f) * 0x1p-23f * (mx + 1.0f);
+                            const float lo_x = fminf(x0, fminf(x1, x2)) - eps;
+                            const float hi_x = fmaxf(x0, fmaxf(x1, x2)) + eps;
+                            if (ceilf(lo_x) == ceilf(hi_x)) {
+                                list = -1;
+                                xsliver = true;
+                                if (b->slot_flags)
+                                    b->slot_flags[2 * t] = 1;
+                            }
+                        }
+                    }
                 }
             }
         }
+        acc.add(b, (uint32_t)item, 1ull, 0ull, xsliver);
         uint32_t pos = 0;
 #pragma unroll
         for (int k = 0; k < 2; k++) {
@@ -373,6 +467,7 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
         }
         __syncthreads();
     }
+    acc.flush(b);
 }
 
 // ------------------------------------------------------------ triangle walk --
@@ -592,69 +687,6 @@ struct WinnerVisitor {
                 rec[x] = make_float4(progress, pl, pr, __uint_as_float(bits));
         };
         span_pixels(x1, x2, Ls, Rs, op);
-    }
-};
-
-// Per-item counters of a warp: lanes grouped by item, one atomic per group.
-__device__ __forceinline__ void item_add(unsigned long long *dst, uint32_t item, unsigned long long v, bool valid)
-{
-    const unsigned act = __ballot_sync(0xFFFFFFFFu, valid);
-    if (!valid)
-        return;
-    const unsigned grp = __match_any_sync(act, item);
-    unsigned long long sum = 0;
-    for (unsigned m = grp; m; m &= m - 1)
-        sum += __shfl_sync(grp, v, __ffs(m) - 1);
-    if ((threadIdx.x & 31) == __ffs(grp) - 1 && sum)
-        atomicAdd(dst + 2 * (size_t)item, sum);
-}
-
-__device__ __forceinline__ void warp_add(unsigned long long *dst, unsigned long long v)
-{
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_down_sync(0xFFFFFFFFu, v, o);
-    if ((threadIdx.x & 31) == 0 && v)
-        atomicAdd(dst, v);
-}
-
-// Per-item counters (drawn triangles, fragments) of a warp, summed in
-// registers while all of the warp's lanes work on one item and added to the
-// item's counters when the item changes (one atomic per counter then); an
-// iteration whose lanes span several items adds per item at once.  Every
-// lane of the warp calls add() and flush().
-struct ItemAcc {
-    uint32_t item = 0xFFFFFFFFu;
-    unsigned long long v0 = 0, v1 = 0;
-
-    __device__ __forceinline__ void flush(const BatchDev *b)
-    {
-        if (item != 0xFFFFFFFFu) {
-            warp_add(b->item_counters + 2 * (size_t)item, v0);
-            warp_add(b->item_counters + 2 * (size_t)item + 1, v1);
-        }
-        item = 0xFFFFFFFFu;
-        v0 = v1 = 0;
-    }
-    __device__ __forceinline__ void add(const BatchDev *b, uint32_t it, unsigned long long a0, unsigned long long a1,
-                                        bool valid)
-    {
-        const unsigned act = __ballot_sync(0xFFFFFFFFu, valid);
-        if (!act)
-            return;
-        const uint32_t first = __shfl_sync(0xFFFFFFFFu, it, __ffs(act) - 1);
-        if (__all_sync(0xFFFFFFFFu, !valid || it == first)) {
-            if (first != item) {
-                flush(b);
-                item = first;
-            }
-            if (valid) {
-                v0 += a0;
-                v1 += a1;
-            }
-        } else {
-            item_add(b->item_counters, it, a0, valid);
-            item_add(b->item_counters + 1, it, a1, valid);
-        }
     }
 };
 

@@ -152,17 +152,37 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
         kernels += (uint64_t)kernels_launched;
     }
     if (st == SGL_OK && opts.copy_out) {
-        for (size_t i = 0; i < jobs.size() && st == SGL_OK; i++) {
+        // colour then depth of each request, in framebuffer order; copies whose
+        // host and device ranges both continue the previous one are merged (a
+        // caller whose host buffers follow the same layout gets one copy per batch)
+        struct Span {
+            uint8_t *dst;
+            const uint8_t *src;
+            size_t n;
+        };
+        std::vector<Span> spans;
+        spans.reserve(2 * jobs.size());
+        auto add = [&](void *dst, const void *src, size_t n) {
+            if (!dst)
+                return;
+            if (!spans.empty()) {
+                Span &b = spans.back();
+                if (b.dst + b.n == (uint8_t *)dst && b.src + b.n == (const uint8_t *)src) {
+                    b.n += n;
+                    return;
+                }
+            }
+            spans.push_back(Span{(uint8_t *)dst, (const uint8_t *)src, n});
+        };
+        for (size_t i = 0; i < jobs.size(); i++) {
             const size_t px = (size_t)jobs[i].req.view.w * jobs[i].req.view.h;
-            if (jobs[i].req.host_pixels &&
-                cudaMemcpyAsync(jobs[i].req.host_pixels, bufs[i].first, 4 * px, cudaMemcpyDeviceToHost,
-                                ls.lane->stream) != cudaSuccess)
-                st = SGL_ERR_CUDA;
-            if (jobs[i].req.host_zbuffer &&
-                cudaMemcpyAsync(jobs[i].req.host_zbuffer, bufs[i].second, 4 * px, cudaMemcpyDeviceToHost,
-                                ls.lane->stream) != cudaSuccess)
-                st = SGL_ERR_CUDA;
+            add(jobs[i].req.host_pixels, bufs[i].first, 4 * px);
+            add(jobs[i].req.host_zbuffer, bufs[i].second, 4 * px);
         }
+        for (const Span &sp : spans)
+            if (st == SGL_OK &&
+                cudaMemcpyAsync(sp.dst, sp.src, sp.n, cudaMemcpyDeviceToHost, ls.lane->stream) != cudaSuccess)
+                st = SGL_ERR_CUDA;
         // the lane's done event must come after the copies
         if (st == SGL_OK && cudaEventRecord(ls.lane->slots[ls.slot].done, ls.lane->stream) != cudaSuccess)
             st = SGL_ERR_CUDA;

@@ -136,3 +136,37 @@ def test_serving_budget_and_poll(renderer):
     srv.drain(10.0)
     srv.close()
     renderer.release(sid)
+
+
+def test_serving_copy_out_into_one_pool(renderer):
+    """Host buffers carved from one pool in framebuffer order (colour, depth,
+    next request): the loop merges the copies of a batch into one; every
+    request still receives exactly its own frame."""
+    scenes = [S.spheres_scene(n_spheres=k, seed=60 + k, tex_size=128) for k in (4, 9)]
+    sids = [renderer.upload(sc) for sc in scenes]
+    rng = S.Rng(91)
+    reqs = []
+    for i in range(24):
+        w = S.log_uniform_int(rng, 64, 400)
+        h = S.log_uniform_int(rng, 64, 300)
+        m, c = S.camera_on_sphere(rng, 35.0)
+        reqs.append((i % 2, S.view_for(w, h, m, c)))
+    pool = np.zeros(sum(2 * v.w * v.h for (_, v) in reqs), np.uint32)
+    srv = renderer.server(budget_bytes=256 << 20, max_batch=8, streams=2, copy_out=True)
+    outs, tickets, off = [], [], 0
+    for k, v in reqs:
+        px = v.w * v.h
+        pix = pool[off:off + px].reshape(v.h, v.w)
+        z = pool[off + px:off + 2 * px].view(np.float32).reshape(v.h, v.w)
+        off += 2 * px
+        outs.append((pix, z))
+        tickets.append(srv.submit(sids[k], v, pix, z))
+    results = [srv.wait(t, 60.0) for t in tickets]
+    srv.close()
+    assert all(r["status"] == 0 for r in results)
+    for (k, v), (pix, z) in zip(reqs, outs):
+        alone, _ = renderer.render(sids[k], [v])
+        assert np.array_equal(pix, alone[0].pixels)
+        assert np.array_equal(z.view(np.uint32), alone[0].zbuffer.view(np.uint32))
+    for sid in sids:
+        renderer.release(sid)
