@@ -106,7 +106,7 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     const size_t o_item = off;
     off += up256(sizeof(ItemDev));
     const size_t o_bases = off;
-    off += up256(10 * sizeof(uint32_t));
+    off += up256(16 * sizeof(uint32_t));
     const size_t o_counters = off;
     off += up256(kCounterWords * sizeof(unsigned long long));
     const size_t o_item_counters = off;
@@ -177,7 +177,11 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     }
     const uint32_t dof_tiles =
         dof ? (uint32_t)((v.w + kDofTile - 1) / kDofTile) * (uint32_t)((v.h + kDofTile - 1) / kDofTile) : 0u;
-    const uint32_t bases[10] = {0u, (uint32_t)nv, 0u, (uint32_t)nt, 0u, (uint32_t)px, 0u, (uint32_t)tiles, 0u, dof_tiles};
+    const bool fused = s->dev.fused != 0;
+    const uint32_t bases[16] = {0u, (uint32_t)nv,                 0u, (uint32_t)nt,
+                                0u, (uint32_t)px,                 0u, (uint32_t)tiles,
+                                0u, dof_tiles,                    0u, fused ? 0u : (uint32_t)nv,
+                                0u, fused ? 0u : (uint32_t)nt,    0u, fused ? s->dev.n_prims : 0u};
     BatchDev b{};
     b.items = (const ItemDev *)(base + o_item);
     b.vtx_base = (const uint32_t *)(base + o_bases);
@@ -185,6 +189,12 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     b.px_base = b.vtx_base + 4;
     b.tile_base = b.vtx_base + 6;
     b.dof_base = b.vtx_base + 8;
+    b.g_vtx_base = b.vtx_base + 10;
+    b.g_tri_base = b.vtx_base + 12;
+    b.prim_base = b.vtx_base + 14;
+    b.total_gvtx = fused ? 0u : (uint32_t)nv;
+    b.total_gtri = fused ? 0u : (uint32_t)nt;
+    b.total_prims = fused ? s->dev.n_prims : 0u;
     b.n_items = 1;
     b.inline_span = ctx->inline_span;
     b.total_vtx = (uint32_t)nv;
@@ -215,7 +225,8 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     CUDA_TRY(cudaMemsetAsync(base + o_item_counters, 0, 2 * sizeof(unsigned long long), st));
     CUDA_TRY(cudaMemsetAsync(base + o_key, 0xFF, 8 * px, st)); // kEmptyKey
 
-    const int seq = (dof ? kSeqDof : 0) | (v.shader != SGL_SHADER_PHONG_BILINEAR ? kSeqShaders : 0);
+    const int seq = (dof ? kSeqDof : 0) | (v.shader != SGL_SHADER_PHONG_BILINEAR ? kSeqShaders : 0) |
+                    (fused ? kSeqFused : kSeqSplit);
     CUDA_TRY(launch_batch((const BatchDev *)(base + o_batch), tile, seq, st, nullptr, nullptr));
     return SGL_OK;
 }

@@ -141,11 +141,11 @@ __global__ void __launch_bounds__(256) k_vertex(const BatchDev *b)
     const float4 *wpos = nullptr;
     float4 *ndc = nullptr;
     uint8_t *yes = nullptr;
-    const uint32_t total = b->total_vtx;
+    const uint32_t total = b->total_gvtx;
     auto bind = [&](uint32_t g) {
-        const int item = find_item(b->vtx_base, b->n_items, g);
-        lo = __ldg(b->vtx_base + item);
-        hi = __ldg(b->vtx_base + item + 1);
+        const int item = find_item(b->g_vtx_base, b->n_items, g);
+        lo = __ldg(b->g_vtx_base + item);
+        hi = __ldg(b->g_vtx_base + item + 1);
         const ItemDev &it = b->items[item];
 #pragma unroll
         for (int k = 0; k < 12; k++) {
@@ -219,11 +219,11 @@ __global__ void __launch_bounds__(256) k_flags(const BatchDev *b)
     const PrimDesc *prims = nullptr;
     const MatDesc *mats = nullptr;
     int n_mats = 0;
-    const uint32_t total = b->total_tri;
+    const uint32_t total = b->total_gtri;
     auto bind = [&](uint32_t g) {
-        const int item = find_item(b->tri_base, b->n_items, g);
-        lo = __ldg(b->tri_base + item);
-        hi = __ldg(b->tri_base + item + 1);
+        const int item = find_item(b->g_tri_base, b->n_items, g);
+        lo = __ldg(b->g_tri_base + item);
+        hi = __ldg(b->g_tri_base + item + 1);
         const ItemDev &it = b->items[item];
         tris = it.s.tris;
         ndc = it.ndc;
@@ -352,6 +352,18 @@ struct ItemAcc {
     }
 };
 
+// Reserve n0 walk-list and n1 clip-list entries with one atomic: the two
+// 32-bit counters C_LIST and C_CLIP are the halves of one 64-bit counter word
+// (a list holds fewer than 2^31 entries, so the low half never carries).
+// Returns the previous values (C_LIST low, C_CLIP high).
+static_assert(C_LIST % 2 == 0 && C_CLIP == C_LIST + 1, "list counters share a 64-bit word");
+__device__ __forceinline__ unsigned long long reserve_lists(const BatchDev *b, uint32_t n0, uint32_t n1)
+{
+    if (!(n0 | n1))
+        return 0ull;
+    return atomicAdd(b->counters + C_LIST / 2, ((unsigned long long)n1 << 32) | n0);
+}
+
 // Drawable triangles (all three vertices flagged, renderer.cpp:248-253) into
 // the walk list; triangles crossing the near plane go to their own list and
 // are marked in the record map.  One global atomic per list per block.
@@ -364,7 +376,7 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
     uint32_t lo = 0, hi = 0;
     const uint4 *tris = nullptr;
     const uint8_t *yes = nullptr;
-    const uint32_t total = b->total_tri;
+    const uint32_t total = b->total_gtri;
     ItemAcc acc; // triangles counted as drawn here (no pixel column)
     // every thread of the block runs the same number of iterations (barriers inside)
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -378,9 +390,9 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
         uint32_t t = 0;
         if (g < total) {
             if (g < lo || g >= hi) {
-                item = find_item(b->tri_base, b->n_items, g);
-                lo = __ldg(b->tri_base + item);
-                hi = __ldg(b->tri_base + item + 1);
+                item = find_item(b->g_tri_base, b->n_items, g);
+                lo = __ldg(b->g_tri_base + item);
+                hi = __ldg(b->g_tri_base + item + 1);
                 const ItemDev &it = b->items[item];
                 tris = it.s.tris;
                 yes = it.yes;
@@ -450,16 +462,16 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            uint32_t *c32 = reinterpret_cast<uint32_t *>(b->counters);
-            base[0] = cnt[0] ? atomicAdd(&c32[C_LIST], cnt[0]) : 0u;
-            base[1] = cnt[1] ? atomicAdd(&c32[C_CLIP], cnt[1]) : 0u;
+            const unsigned long long old = reserve_lists(b, cnt[0], cnt[1]);
+            base[0] = (uint32_t)old;
+            base[1] = (uint32_t)(old >> 32);
         }
         __syncthreads();
         if (list == 1) {
             const uint32_t j = base[1] + pos;
             if (j < b->clip_cap)
                 b->clip[b->clip_cap - 1 - j] = make_uint2(t, (uint32_t)item); // filled from the end
-            b->recmap[g] = kRecClip;
+            b->recmap[__ldg(b->tri_base + item) + t] = kRecClip;
         } else if (list == 0) {
             const uint32_t j = base[0] + pos;
             if (j < b->list_cap)
@@ -468,6 +480,244 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
         __syncthreads();
     }
     acc.flush(b);
+}
+
+// The geometry of fused scenes (every primitive within kFuseVerts vertices
+// and kFuseTris triangles): one warp per primitive runs k_vertex, k_flags and
+// k_compact on it with the vertex positions and flags in shared memory.  A
+// primitive owns its vertices (no two vertex ranges overlap), so its
+// triangles are the only ones that flag them (renderer.cpp:86-185 flags a
+// node's primitives before any is drawn, and each primitive's vertices are
+// its own), and its compaction needs nothing from other warps.  A block's 8
+// warps take 8 consecutive primitives; their list entries are counted first
+// and placed with one global atomic per list per block.
+constexpr int kGeomWarps = 8;
+constexpr int kGeomPrims = 1; // primitives per warp and block iteration
+__global__ void __launch_bounds__(kGeomWarps * 32, 4) k_geom(const BatchDev *b)
+{
+    __shared__ float s_pos[kGeomWarps][3 * kFuseVerts]; // x, y, z' of each vertex
+    __shared__ uint8_t s_yes[kGeomWarps][kFuseVerts];
+    __shared__ uint8_t s_dec[kGeomWarps][kGeomPrims][kFuseTris]; // 0 none, 1 walk list, 2 clip list, 3 no pixel
+    __shared__ uint32_t s_cnt[kGeomWarps][2];
+    __shared__ float s_m[kGeomWarps][24]; // view and projection rows 0-2 of the warp's item
+    const int warp = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    float *pos = s_pos[warp];
+    uint8_t *sy = s_yes[warp];
+    float *m = s_m[warp];
+    int cur = -1;              // item whose matrices and pointers are loaded
+    uint32_t p_lo = 0, p_hi = 0; // its primitives
+    const float4 *wpos = nullptr;
+    float4 *ndc = nullptr;
+    const uint4 *tris = nullptr;
+    const PrimDesc *prims = nullptr;
+    const MatDesc *mats = nullptr;
+    int n_mats = 0;
+    float vm00 = 0.0f, vm03 = 0.0f, vm11 = 0.0f, vm13 = 0.0f;
+    uint32_t tri_lo = 0;
+    int acc_item = -1; // triangles counted as drawn here, per item (warp-uniform)
+    unsigned long long acc_n = 0;
+    const uint32_t total = b->total_prims;
+    const uint32_t step = gridDim.x * (kGeomWarps * kGeomPrims);
+    // every warp of the block runs the same iterations (barriers inside)
+    for (uint32_t p0 = blockIdx.x * (kGeomWarps * kGeomPrims); p0 < total; p0 += step) {
+        uint32_t c0 = 0, c1 = 0;
+        int items[kGeomPrims];
+        uint32_t first[kGeomPrims], count[kGeomPrims], tlo[kGeomPrims];
+#pragma unroll
+        for (int u = 0; u < kGeomPrims; u++) {
+            const uint32_t p = p0 + warp * kGeomPrims + u;
+            items[u] = -1;
+            first[u] = count[u] = tlo[u] = 0;
+            if (p >= total)
+                continue;
+            if (p < p_lo || p >= p_hi) {
+                const int item = find_item(b->prim_base, b->n_items, p);
+                p_lo = __ldg(b->prim_base + item);
+                p_hi = __ldg(b->prim_base + item + 1);
+                if (item != cur) {
+                    const ItemDev &it = b->items[item];
+                    __syncwarp();
+                    if (lane < 12) {
+                        m[lane] = it.v.view[lane];
+                        m[12 + lane] = it.v.proj[lane];
+                    }
+                    __syncwarp();
+                    wpos = it.s.wpos;
+                    ndc = it.ndc;
+                    tris = it.s.tris;
+                    prims = it.s.prims;
+                    mats = it.s.mats;
+                    n_mats = it.s.n_mats;
+                    vm00 = it.v.vm00;
+                    vm03 = it.v.vm03;
+                    vm11 = it.v.vm11;
+                    vm13 = it.v.vm13;
+                    tri_lo = __ldg(b->tri_base + item);
+                    cur = item;
+                }
+            }
+            const uint32_t q = p - p_lo;
+            uint4 gq = b->items[cur].s.pgeo[q]; // first vertex, vertex count, first triangle, triangle count
+            gq.y = min(gq.y, kFuseVerts);     // (a fused scene's primitives are within both limits)
+            gq.w = min(gq.w, kFuseTris);
+            items[u] = cur;
+            first[u] = gq.z;
+            count[u] = gq.w;
+            tlo[u] = tri_lo;
+            uint8_t *dec = s_dec[warp][u];
+            // the first 64 triangles are loaded before the vertices, so that both
+            // loads are in flight together, and kept for both passes
+            uint4 tr[2];
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+                if (lane + 32 * k < gq.w)
+                    tr[k] = tris[gq.z + lane + 32 * k];
+            __syncwarp(); // the previous primitive's reads of pos and sy are done
+            // world_to_camera_or_frustum (vertex_shaders.hpp:35-52), as k_vertex
+            for (uint32_t i = lane; i < gq.y; i += 32) {
+                const float4 w = wpos[gq.x + i];
+                V3 v = transform3(mk3(w.x, w.y, w.z), m);
+                v = transform3(v, m + 12);
+                if (v.z != 0.0f) {
+                    v.x = v.x / fabsf(v.z);
+                    v.y = v.y / fabsf(v.z);
+                }
+                ndc[gq.x + i] = make_float4(v.x, v.y, v.z, 0.0f);
+                pos[3 * i] = v.x;
+                pos[3 * i + 1] = v.y;
+                pos[3 * i + 2] = v.z;
+                sy[i] = below_near(v.z) ? kYesBehind : 0;
+            }
+            __syncwarp();
+            // visibility flags (renderer.cpp:86-185), as k_flags; every store
+            // to a vertex writes the same value
+            const int mat = prims[q].material;
+            const bool ds = mat >= 0 && mat < n_mats && mats[mat].double_sided;
+            for (uint32_t t = lane; t < gq.w; t += 32) {
+                const uint4 tri = t < 32 ? tr[0] : (t < 64 ? tr[1] : tris[gq.z + t]);
+                const uint32_t ia = tri.x - gq.x, ib = tri.y - gq.x, ic = tri.z - gq.x;
+                const V3 a = mk3(pos[3 * ia], pos[3 * ia + 1], pos[3 * ia + 2]);
+                const V3 c1v = mk3(pos[3 * ib], pos[3 * ib + 1], pos[3 * ib + 2]);
+                const V3 c2v = mk3(pos[3 * ic], pos[3 * ic + 1], pos[3 * ic + 2]);
+                if (inside_frustum(a, c1v, c2v) && (ds || cross_n_z(sub3(c1v, a), sub3(c2v, a)) > 0.0f)) {
+                    sy[ia] = kYesDrawn | (below_near(a.z) ? kYesBehind : 0);
+                    sy[ib] = kYesDrawn | (below_near(c1v.z) ? kYesBehind : 0);
+                    sy[ic] = kYesDrawn | (below_near(c2v.z) ? kYesBehind : 0);
+                }
+            }
+            __syncwarp();
+            // the compaction's decisions, as k_compact
+            uint32_t nx = 0;
+            for (uint32_t t = lane; t < gq.w; t += 32) {
+                const uint4 tri = t < 32 ? tr[0] : (t < 64 ? tr[1] : tris[gq.z + t]);
+                const uint32_t ia = tri.x - gq.x, ib = tri.y - gq.x, ic = tri.z - gq.x;
+                const uint32_t ya = sy[ia], yb = sy[ib], yc = sy[ic];
+                uint8_t d = 0;
+                if (ya & yb & yc & kYesDrawn) {
+                    if ((ya | yb | yc) & kYesBehind) {
+                        d = 2;
+                    } else {
+                        d = 1;
+                        const float y0 = vm11 * pos[3 * ia + 1] + vm13;
+                        const float y1 = vm11 * pos[3 * ib + 1] + vm13;
+                        const float y2 = vm11 * pos[3 * ic + 1] + vm13;
+                        const float lo_y = fminf(y0, fminf(y1, y2)), hi_y = fmaxf(y0, fmaxf(y1, y2));
+                        if (y0 == y0 && y1 == y1 && y2 == y2) {
+                            if (f2i(ceilf(lo_y)) == f2i(ceilf(hi_y))) {
+                                d = 0; // no row
+                            } else {
+                                const float x0 = vm00 * pos[3 * ia] + vm03;
+                                const float x1 = vm00 * pos[3 * ib] + vm03;
+                                const float x2 = vm00 * pos[3 * ic] + vm03;
+                                const float mx = fmaxf(fabsf(x0), fmaxf(fabsf(x1), fabsf(x2)));
+                                const float rows = ceilf(hi_y) - ceilf(lo_y);
+                                const float eps = (rows + 32.0f) * 0x1p-23f * (mx + 1.0f);
+                                const float lo_x = fminf(x0, fminf(x1, x2)) - eps;
+                                const float hi_x = fmaxf(x0, fmaxf(x1, x2)) + eps;
+                                if (ceilf(lo_x) == ceilf(hi_x)) {
+                                    d = 3; // no pixel column
+                                    if (b->slot_flags)
+                                        b->slot_flags[2 * (gq.z + t)] = 1;
+                                }
+                            }
+                        }
+                    }
+                }
+                dec[t] = d;
+                c0 += d == 1;
+                c1 += d == 2;
+                nx += d == 3;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                nx += __shfl_xor_sync(0xFFFFFFFFu, nx, o);
+            if (nx) {
+                if (cur != acc_item) {
+                    if (acc_item >= 0 && lane == 0)
+                        atomicAdd(b->item_counters + 2 * (size_t)acc_item, acc_n);
+                    acc_item = cur;
+                    acc_n = 0;
+                }
+                acc_n += nx;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            c0 += __shfl_xor_sync(0xFFFFFFFFu, c0, o);
+            c1 += __shfl_xor_sync(0xFFFFFFFFu, c1, o);
+        }
+        if (lane == 0) {
+            s_cnt[warp][0] = c0;
+            s_cnt[warp][1] = c1;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t n0 = 0, n1 = 0;
+            for (int w = 0; w < kGeomWarps; w++) {
+                const uint32_t a0 = s_cnt[w][0], a1 = s_cnt[w][1];
+                s_cnt[w][0] = n0;
+                s_cnt[w][1] = n1;
+                n0 += a0;
+                n1 += a1;
+            }
+            const unsigned long long old = reserve_lists(b, n0, n1);
+            const uint32_t g0 = (uint32_t)old, g1 = (uint32_t)(old >> 32);
+            for (int w = 0; w < kGeomWarps; w++) {
+                s_cnt[w][0] += g0;
+                s_cnt[w][1] += g1;
+            }
+        }
+        __syncthreads();
+        uint32_t o0 = s_cnt[warp][0], o1 = s_cnt[warp][1];
+        const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+        for (int u = 0; u < kGeomPrims; u++) {
+            if (items[u] < 0)
+                continue;
+            const uint8_t *dec = s_dec[warp][u];
+            for (uint32_t t0 = 0; t0 < count[u]; t0 += 32) {
+                const uint32_t t = t0 + lane;
+                const uint8_t d = t < count[u] ? dec[t] : 0;
+                const unsigned m1 = __ballot_sync(0xFFFFFFFFu, d == 1), m2 = __ballot_sync(0xFFFFFFFFu, d == 2);
+                if (d == 1) {
+                    const uint32_t j = o0 + __popc(m1 & below);
+                    if (j < b->list_cap)
+                        b->list[j] = make_uint2(first[u] + t, (uint32_t)items[u]);
+                } else if (d == 2) {
+                    const uint32_t j = o1 + __popc(m2 & below);
+                    if (j < b->clip_cap)
+                        b->clip[b->clip_cap - 1 - j] = make_uint2(first[u] + t, (uint32_t)items[u]); // from the end
+                    b->recmap[tlo[u] + first[u] + t] = kRecClip;
+                }
+                o0 += __popc(m1);
+                o1 += __popc(m2);
+            }
+        }
+        __syncthreads(); // s_cnt is rewritten by the next iteration
+    }
+    if (acc_item >= 0 && lane == 0)
+        atomicAdd(b->item_counters + 2 * (size_t)acc_item, acc_n);
 }
 
 // ------------------------------------------------------------ triangle walk --
@@ -2333,9 +2583,9 @@ cudaError_t launch_pose(const SceneDev &s, const float *node_world, const float 
 
 const char *prof_kernel_name(int k)
 {
-    static const char *names[kProfKernels] = {"k_vertex", "k_flags",   "k_compact", "k_setup",  "k_walk",
-                                              "k_spans",  "k_winners", "k_shade",   "k_dof",    "k_frags",
-                                              "k_layers", "k_flatten", "k_copy_layer"};
+    static const char *names[kProfKernels] = {"k_geom",    "k_vertex",  "k_flags",  "k_compact", "k_setup",
+                                              "k_walk",    "k_spans",   "k_winners", "k_shade",  "k_dof",
+                                              "k_frags",   "k_layers",  "k_flatten", "k_copy_layer"};
     return (k >= 0 && k < kProfKernels) ? names[k] : "?";
 }
 
@@ -2400,18 +2650,27 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
     };
     const int sms = sm_count();
     int n = 0;
+    mark(PK_GEOM);
+    if (flags & kSeqFused) {
+        k_geom<<<sms * 8, kGeomWarps * 32, 0, st>>>(b);
+        ran(PK_GEOM);
+        n++;
+    }
     mark(PK_VERTEX);
-    k_vertex<<<sms * 8, 256, 0, st>>>(b);
-    ran(PK_VERTEX);
-    n++;
-    mark(PK_FLAGS);
-    k_flags<<<sms * 8, 256, 0, st>>>(b);
-    ran(PK_FLAGS);
-    n++;
-    mark(PK_COMPACT);
-    k_compact<<<sms * 4, kCompactBlock, 0, st>>>(b);
-    ran(PK_COMPACT);
-    n++;
+    if (flags & kSeqSplit) {
+        k_vertex<<<sms * 8, 256, 0, st>>>(b);
+        ran(PK_VERTEX);
+        mark(PK_FLAGS);
+        k_flags<<<sms * 8, 256, 0, st>>>(b);
+        ran(PK_FLAGS);
+        mark(PK_COMPACT);
+        k_compact<<<sms * 4, kCompactBlock, 0, st>>>(b);
+        ran(PK_COMPACT);
+        n += 3;
+    } else {
+        mark(PK_FLAGS);
+        mark(PK_COMPACT);
+    }
     mark(PK_SETUP);
     k_setup<<<sms * 8, 256, 0, st>>>(b);
     ran(PK_SETUP);

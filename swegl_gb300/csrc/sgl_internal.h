@@ -30,6 +30,11 @@ struct PrimDesc {
     int node;
 };
 
+// Scenes whose every primitive has at most kFuseVerts vertices and
+// kFuseTris triangles take the fused geometry pass (one warp per primitive:
+// vertex transform, visibility flags and compaction in shared memory).
+constexpr uint32_t kFuseVerts = 256, kFuseTris = 512;
+
 struct LightsDev {
     float ambient;
     float sun[3];
@@ -53,8 +58,11 @@ struct SceneDev {
     float4 *wpos;            // v_world
     float4 *wnrm;            // normal_world
     float2 *uv;              // tex_coords
+    const uint4 *pgeo;       // draw-order primitives: first vertex, vertex count, first triangle, triangle count
     uint32_t n_vertices;
     uint32_t n_triangles;
+    uint32_t n_prims;
+    int fused;               // every primitive within kFuseVerts / kFuseTris
     int n_mats;
     int n_texs;
     MatDesc default_mat;
@@ -194,6 +202,11 @@ struct BatchDev {
     const uint32_t *px_base;   // n_items + 1 prefix of pixel counts
     const uint32_t *tile_base; // n_items + 1 prefix of shade-tile counts
     const uint32_t *dof_base;  // n_items + 1 prefix of depth-of-field tile counts (0 for items without)
+    // the geometry passes: items of fused scenes by primitive (prim_base),
+    // the others by vertex and triangle (g_vtx_base, g_tri_base); each item
+    // counts in one of the two
+    const uint32_t *g_vtx_base, *g_tri_base, *prim_base;
+    uint32_t total_gvtx, total_gtri, total_prims;
     int n_items;
     int inline_span;           // spans wider than this go to the long-span bins
     uint32_t total_vtx, total_tri, total_px, total_tiles, total_dof_tiles;
@@ -216,9 +229,9 @@ struct BatchDev {
 
 // Optional per-kernel timing: CUDA events recorded on the launching stream
 // around each stage of a launch sequence (enabled with sgl_profile).
-constexpr int kProfKernels = 13;
+constexpr int kProfKernels = 14;
 enum ProfKernel {
-    PK_VERTEX = 0, PK_FLAGS, PK_COMPACT, PK_SETUP, PK_WALK, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF,
+    PK_GEOM = 0, PK_VERTEX, PK_FLAGS, PK_COMPACT, PK_SETUP, PK_WALK, PK_SPANS, PK_WINNER, PK_SHADE, PK_DOF,
     PK_FRAGS, PK_LAYERS, PK_FLATTEN, PK_COPY
 };
 struct Profiler {
@@ -249,7 +262,9 @@ cudaError_t launch_pose(const SceneDev &s, const float *node_world, const float 
 // flatten and copy passes; its fragment pool must have been big enough
 // (C_FRAGS <= frag_cap) for the outputs to be written, else they are left
 // untouched and the host renders again with a bigger pool.
-constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqLayers = 4, kSeqVariants = 8;
+// kSeqFused: items of fused scenes (k_geom); kSeqSplit: other items (k_vertex,
+// k_flags, k_compact).
+constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqLayers = 4, kSeqFused = 8, kSeqSplit = 16, kSeqVariants = 32;
 cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st, int *launches, Profiler *prof);
 // The depth-of-field gather alone (items prepared by the caller).
 cudaError_t launch_dof(const BatchDev *b, cudaStream_t st);

@@ -77,12 +77,12 @@ sgl_status Lane::init(Ctx *ctx, int max_items_, cudaStream_t external, bool bloc
     }
     for (auto &sl : slots) {
         CUDA_TRY(sl.d_items.ensure(sizeof(ItemDev) * (size_t)max_items));
-        CUDA_TRY(sl.d_bases.ensure(sizeof(uint32_t) * 5 * ((size_t)max_items + 1)));
+        CUDA_TRY(sl.d_bases.ensure(sizeof(uint32_t) * kBaseArrays * ((size_t)max_items + 1)));
         CUDA_TRY(sl.d_batch.ensure(sizeof(BatchDev)));
         CUDA_TRY(sl.d_counters.ensure(sizeof(unsigned long long) * kCounterWords));
         CUDA_TRY(sl.d_item_counters.ensure(2 * sizeof(unsigned long long) * (size_t)max_items));
         CUDA_TRY(sl.h_items.ensure(sizeof(ItemDev) * (size_t)max_items));
-        CUDA_TRY(sl.h_bases.ensure(sizeof(uint32_t) * 5 * ((size_t)max_items + 1)));
+        CUDA_TRY(sl.h_bases.ensure(sizeof(uint32_t) * kBaseArrays * ((size_t)max_items + 1)));
         CUDA_TRY(sl.h_batch.ensure(sizeof(BatchDev)));
         CUDA_TRY(sl.h_counters.ensure(sizeof(unsigned long long) * (kCounterWords + 2 * (size_t)max_items)));
         CUDA_TRY(cudaEventCreateWithFlags(&sl.staged, cudaEventDisableTiming));
@@ -106,7 +106,9 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     // prefixes and pool offsets
     uint32_t *hb = (uint32_t *)sl.h_bases.ptr;
     uint32_t *vb = hb, *tb = hb + (n + 1), *pb = hb + 2 * (n + 1), *gb = hb + 3 * (n + 1), *fb = hb + 4 * (n + 1);
-    uint64_t tv = 0, tt = 0, tp = 0, tg = 0, tf = 0, dof_px = 0, dofz_px = 0;
+    uint32_t *gvb = hb + 5 * (n + 1), *gtb = hb + 6 * (n + 1), *qb = hb + 7 * (n + 1);
+    uint64_t tv = 0, tt = 0, tp = 0, tg = 0, tf = 0, dof_px = 0, dofz_px = 0, tgv = 0, tgt = 0, tq = 0;
+    int geom_flags = 0;
     size_t ndc_off = 0, yes_off = 0;
     std::vector<size_t> ndc_at(n), yes_at(n), dof_at(n), dofz_at(n);
     for (int i = 0; i < n; i++) {
@@ -117,6 +119,17 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         pb[i] = (uint32_t)tp;
         gb[i] = (uint32_t)tg;
         fb[i] = (uint32_t)tf;
+        gvb[i] = (uint32_t)tgv;
+        gtb[i] = (uint32_t)tgt;
+        qb[i] = (uint32_t)tq;
+        if (s.dev.fused) {
+            tq += s.dev.n_prims;
+            geom_flags |= kSeqFused;
+        } else {
+            tgv += s.n_vertices;
+            tgt += s.n_triangles;
+            geom_flags |= kSeqSplit;
+        }
         tv += s.n_vertices;
         tt += s.n_triangles;
         tp += (uint64_t)v.w * v.h;
@@ -135,7 +148,8 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
                 dofz_px += align_up((size_t)v.w * v.h, 64);
         }
     }
-    if (tv >= (1ull << 32) || tt >= (1ull << 31) || tp >= (1ull << 32) || tg >= (1ull << 32) || tf >= (1ull << 32)) {
+    if (tv >= (1ull << 32) || tt >= (1ull << 31) || tp >= (1ull << 32) || tg >= (1ull << 32) || tf >= (1ull << 32) ||
+        tq >= (1ull << 32)) {
         ctx->fail("batch too large (%llu vertices, %llu triangles, %llu pixels)", (unsigned long long)tv,
                   (unsigned long long)tt, (unsigned long long)tp);
         return SGL_ERR_UNSUPPORTED;
@@ -145,6 +159,9 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     pb[n] = (uint32_t)tp;
     gb[n] = (uint32_t)tg;
     fb[n] = (uint32_t)tf;
+    gvb[n] = (uint32_t)tgv;
+    gtb[n] = (uint32_t)tgt;
+    qb[n] = (uint32_t)tq;
     const size_t span_cap = std::max<size_t>(65536, tp / 8);
     CUDA_TRY(ndc.ensure(sizeof(float4) * std::max<size_t>(ndc_off, 1)));
     CUDA_TRY(yes.ensure(std::max<size_t>(yes_off, 1)));
@@ -166,7 +183,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         if (dofz_px)
             CUDA_TRY(dofz.ensure(4 * dofz_px));
     }
-    int seq_flags = 0;
+    int seq_flags = geom_flags;
     int layers = 0;
     for (int i = 0; i < n; i++)
         layers = std::max(layers, e[i].view.layers);
@@ -246,6 +263,12 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.px_base = db + 2 * (n + 1);
     bd.tile_base = db + 3 * (n + 1);
     bd.dof_base = db + 4 * (n + 1);
+    bd.g_vtx_base = db + 5 * (n + 1);
+    bd.g_tri_base = db + 6 * (n + 1);
+    bd.prim_base = db + 7 * (n + 1);
+    bd.total_gvtx = (uint32_t)tgv;
+    bd.total_gtri = (uint32_t)tgt;
+    bd.total_prims = (uint32_t)tq;
     bd.n_items = n;
     bd.inline_span = inline_span;
     bd.total_vtx = (uint32_t)tv;
@@ -271,7 +294,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.frag_cap = (uint32_t)frag_cap;
     *hbd = bd;
     CUDA_TRY(cudaMemcpyAsync(sl.d_items.ptr, hi, sizeof(ItemDev) * n, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(sl.d_bases.ptr, hb, sizeof(uint32_t) * 5 * (n + 1), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(sl.d_bases.ptr, hb, sizeof(uint32_t) * kBaseArrays * (n + 1), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(sl.d_batch.ptr, hbd, sizeof(BatchDev), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemsetAsync(sl.d_counters.ptr, 0, sizeof(unsigned long long) * kCounterWords, stream));
     CUDA_TRY(cudaMemsetAsync(sl.d_item_counters.ptr, 0, 2 * sizeof(unsigned long long) * n, stream));

@@ -289,6 +289,8 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
             order.insert(order.end(), v.begin(), v.end());
     }
     std::vector<PrimDesc> prims(order.size());
+    std::vector<uint4> pgeo(order.size());
+    bool fused = true;
     std::vector<uint4> tris;
     std::vector<uint32_t> vnode(d->n_vertices, 0);
     uint64_t total = 0;
@@ -304,6 +306,9 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
         const uint32_t *idx = d->indices + p.index_offset;
         const uint32_t base = p.vertex_offset;
         const uint32_t nt = prim_triangles(p);
+        pgeo[q] = make_uint4(p.vertex_offset, p.vertex_count, (uint32_t)tris.size(), nt);
+        if (p.vertex_count > kFuseVerts || nt > kFuseTris)
+            fused = false;
         for (uint32_t t = 0; t < nt; t++) {
             uint32_t i0, i1, i2;
             if (p.mode == SGL_TRIANGLE_STRIP) { // renderer.cpp:198-207, with the parity swap
@@ -354,6 +359,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     CUDA_TRY(upload(d_vnode, vnode.data(), vnode.size()));
     CUDA_TRY(upload(d_tris, tris.data(), tris.size()));
     CUDA_TRY(upload(d_prims, prims.data(), prims.size()));
+    CUDA_TRY(upload(d_pgeo, pgeo.data(), pgeo.size()));
     CUDA_TRY(upload(d_mats, mats.data(), mats.size()));
     CUDA_TRY(upload(d_texs, texs.data(), texs.size()));
     CUDA_TRY(d_wpos.ensure(sizeof(float4) * std::max<size_t>(n_vertices, 1)));
@@ -370,6 +376,9 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     dev.wpos = (float4 *)d_wpos.ptr;
     dev.wnrm = (float4 *)d_wnrm.ptr;
     dev.uv = (float2 *)d_uv.ptr;
+    dev.pgeo = (const uint4 *)d_pgeo.ptr;
+    dev.n_prims = (uint32_t)pgeo.size();
+    dev.fused = fused ? 1 : 0;
     dev.n_vertices = n_vertices;
     dev.n_triangles = n_triangles;
     dev.n_mats = d->n_materials;
@@ -385,7 +394,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     if (st != SGL_OK)
         return st;
     device_bytes = d_pos_u.bytes + d_nrm_v.bytes + d_vnode.bytes + d_tris.bytes + d_prims.bytes + d_mats.bytes +
-                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_uv.bytes + d_node_world.bytes + d_node_rs.bytes + d_lights.bytes;
+                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_uv.bytes + d_node_world.bytes + d_node_rs.bytes + d_lights.bytes + d_pgeo.bytes;
     return SGL_OK;
 }
 
