@@ -73,6 +73,44 @@ def test_batch_equals_single_frames(rig):
             assert st["fragments"] > 0
 
 
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_mixing_both_geometry_paths(rig, use_graph):
+    """Scenes whose primitives fit the fused geometry pass (spheres, cube) and
+    a scene that does not (the grid floor: one 3,200-triangle list) in one
+    batch, in both orders: every view matches the oracle, and the triangle
+    counts of both paths add up."""
+    r, torch = rig
+    scenes = [G.scene("grid"), G.scene("spheres200"), G.scene("cube")]
+    sids = [r.upload(sc) for sc in scenes]
+    views, owner = [], []
+    for i, (pos, w, h) in enumerate([((0.5, 0.3, 3.0), 320, 240), ((3.0, 8.0, 30.0), 400, 300),
+                                     ((1.5, 1.2, 3.5), 200, 160), ((-4.0, 1.0, 2.0), 256, 200),
+                                     ((-20.0, 10.0, 25.0), 300, 200), ((2.0, -1.5, 3.0), 180, 140)]):
+        k = [0, 1, 2, 0, 1, 2][i]
+        target = (0.0, -0.4, 0.0) if k == 0 else (0.0, 0.0, 0.0)
+        m, c = S.look_at(pos, target)
+        views.append(S.view_for(w, h, m, c))
+        owner.append(k)
+    for order in (list(range(6)), list(reversed(range(6)))):
+        vs = [views[i] for i in order]
+        ow = [owner[i] for i in order]
+        bufs, tgts = device_targets(torch, vs)
+        st = r.render_batch([(sids[ow[i]], v, t) for i, (v, t) in enumerate(zip(vs, tgts))], use_graph=use_graph,
+                            stats=True)
+        torch.cuda.synchronize()
+        got = frames_of(bufs)
+        drawn = 0
+        for i, v in enumerate(vs):
+            ref = oracle.render(scenes[ow[i]], [v])
+            assert np.array_equal(got[i][1].view(np.uint32), ref.zbuffer.view(np.uint32)), (order, i)
+            d = np.abs(got[i][0].view(np.uint8).astype(np.int16) - ref.pixels.view(np.uint8).astype(np.int16))
+            assert int(d.max()) <= 2, (order, i)
+            drawn += ref.stats[0][0]
+        assert st["drawn_triangles"] == drawn
+    for sid in sids:
+        r.release(sid)
+
+
 def test_graph_replay_and_autotune(rig):
     r, torch = rig
     sc = G.scene("spheres200")
