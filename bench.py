@@ -613,7 +613,7 @@ def latency_run(srv, sids, duration: float, seed: int) -> dict:
 def e2e_run(r, torch, sids, timed, M: int, args):
     """Closed-loop steps with copy-out of every frame to pinned host memory."""
     srv = r.server(budget_bytes=args.budget, max_batch=args.max_batch, streams=args.streams, copy_out=True)
-    steps = max(1, min(args.steps, 3))
+    steps = max(1, min(args.steps, 8))
     chunks = [timed[s * M:(s + 1) * M] for s in range(steps)]
     need = max(sum(8 * v.w * v.h for (_, _, v) in ch) for ch in chunks)
     pool = torch.empty(need // 4 + 16, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
