@@ -111,6 +111,42 @@ def test_batch_mixing_both_geometry_paths(rig, use_graph):
         r.release(sid)
 
 
+def test_64_viewports_full_size(rig):
+    """The batched configuration at full size: 64 seeded cameras on a sphere
+    of radius 35 around the 200-sphere scene, viewports log-uniform from
+    128x128 to 1920x1080, rendered in one graph-captured launch sequence
+    with the tile and span bin the autotuner picks.  Every viewport equals
+    the one-frame-per-launch render of it (bit for bit) and the oracle
+    (depth bit-exact, colour within 2 LSB and within 1 LSB on >= 99.9 % of
+    pixels)."""
+    import os
+
+    r, torch = rig
+    sc = G.scene("spheres200")
+    sid = r.upload(sc)
+    views = S.batch_views(64)
+    bufs, tgts = device_targets(torch, views)
+    items = [(sid, v, t) for v, t in zip(views, tgts)]
+    chosen = r.autotune(items)
+    r.render_batch(items, tile=chosen["tile"], span_bin=chosen["span_bin"], use_graph=True)
+    torch.cuda.synchronize()
+    got = frames_of(bufs)
+    exp = oracle.render_parallel(sc, views, max(1, min(16, os.cpu_count() or 1)))
+    within1 = total = 0
+    for i, v in enumerate(views):
+        alone, _ = r.render(sid, [v])
+        assert np.array_equal(got[i][0], alone[0].pixels), i
+        assert np.array_equal(got[i][1].view(np.uint32), alone[0].zbuffer.view(np.uint32)), i
+        assert np.array_equal(got[i][1].view(np.uint32), exp[i].zbuffer.view(np.uint32)), i
+        d = np.abs(got[i][0].view(np.uint8).astype(np.int16) - exp[i].pixels.view(np.uint8).astype(np.int16))
+        assert int(d.max()) <= 2, i
+        per_px = d.reshape(-1, 4).max(axis=1)
+        within1 += int((per_px <= 1).sum())
+        total += per_px.size
+    assert within1 >= 0.999 * total
+    r.release(sid)
+
+
 def test_graph_replay_and_autotune(rig):
     r, torch = rig
     sc = G.scene("spheres200")
