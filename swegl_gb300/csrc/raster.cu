@@ -490,7 +490,8 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
 // node's primitives before any is drawn, and each primitive's vertices are
 // its own), and its compaction needs nothing from other warps.  A block's 8
 // warps take 8 consecutive primitives; their list entries are counted first
-// and placed with one global atomic per list per block.
+// and both lists are reserved with one global atomic per block
+// (reserve_lists).
 constexpr int kGeomWarps = 8;
 constexpr int kGeomPrims = 1; // primitives per warp and block iteration
 __global__ void __launch_bounds__(kGeomWarps * 32, 4) k_geom(const BatchDev *b)
