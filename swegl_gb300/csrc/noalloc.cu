@@ -184,21 +184,19 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
                                 0u, fused ? 0u : (uint32_t)nt,    0u, fused ? s->dev.n_prims : 0u};
     BatchDev b{};
     b.items = (const ItemDev *)(base + o_item);
-    b.vtx_base = (const uint32_t *)(base + o_bases);
-    b.tri_base = b.vtx_base + 2;
-    b.px_base = b.vtx_base + 4;
-    b.tile_base = b.vtx_base + 6;
-    b.dof_base = b.vtx_base + 8;
-    b.g_vtx_base = b.vtx_base + 10;
-    b.g_tri_base = b.vtx_base + 12;
-    b.prim_base = b.vtx_base + 14;
+    const uint32_t *bp = (const uint32_t *)(base + o_bases);
+    b.tri_base = bp + 2;
+    b.px_base = bp + 4;
+    b.tile_base = bp + 6;
+    b.dof_base = bp + 8;
+    b.g_vtx_base = bp + 10;
+    b.g_tri_base = bp + 12;
+    b.prim_base = bp + 14;
     b.total_gvtx = fused ? 0u : (uint32_t)nv;
     b.total_gtri = fused ? 0u : (uint32_t)nt;
     b.total_prims = fused ? s->dev.n_prims : 0u;
     b.n_items = 1;
     b.inline_span = ctx->inline_span;
-    b.total_vtx = (uint32_t)nv;
-    b.total_tri = (uint32_t)nt;
     b.total_px = (uint32_t)px;
     b.total_tiles = (uint32_t)tiles;
     b.total_dof_tiles = dof_tiles;

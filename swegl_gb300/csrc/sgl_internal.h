@@ -197,7 +197,6 @@ constexpr int kCounterWords = (C_SHADE_Q + 32 * kQueues) / 2; // 64-bit words
 // A batch of views rendered by one launch sequence (lives in device memory).
 struct BatchDev {
     const ItemDev *items;
-    const uint32_t *vtx_base;  // n_items + 1 prefix of vertex counts
     const uint32_t *tri_base;  // n_items + 1 prefix of triangle counts
     const uint32_t *px_base;   // n_items + 1 prefix of pixel counts
     const uint32_t *tile_base; // n_items + 1 prefix of shade-tile counts
@@ -209,7 +208,7 @@ struct BatchDev {
     uint32_t total_gvtx, total_gtri, total_prims;
     int n_items;
     int inline_span;           // spans wider than this go to the long-span bins
-    uint32_t total_vtx, total_tri, total_px, total_tiles, total_dof_tiles;
+    uint32_t total_px, total_tiles, total_dof_tiles;
     uint2 *list;               // drawable triangles {t, item}
     uint32_t list_cap;
     uint2 *clip;               // drawable triangles crossing the near plane {t, item}: entry j at clip[clip_cap - 1 - j]

@@ -258,8 +258,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     BatchDev bd{};
     bd.items = (const ItemDev *)sl.d_items.ptr;
     const uint32_t *db = (const uint32_t *)sl.d_bases.ptr;
-    bd.vtx_base = db;
-    bd.tri_base = db + (n + 1);
+    bd.tri_base = db + (n + 1); // (db[0 .. n]: the vertex prefix, read by nothing on the device)
     bd.px_base = db + 2 * (n + 1);
     bd.tile_base = db + 3 * (n + 1);
     bd.dof_base = db + 4 * (n + 1);
@@ -271,8 +270,6 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.total_prims = (uint32_t)tq;
     bd.n_items = n;
     bd.inline_span = inline_span;
-    bd.total_vtx = (uint32_t)tv;
-    bd.total_tri = (uint32_t)tt;
     bd.total_px = (uint32_t)tp;
     bd.total_tiles = (uint32_t)tg;
     bd.total_dof_tiles = (uint32_t)tf;
