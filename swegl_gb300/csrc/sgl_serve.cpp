@@ -179,13 +179,21 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
             add(jobs[i].req.host_pixels, bufs[i].first, 4 * px);
             add(jobs[i].req.host_zbuffer, bufs[i].second, 4 * px);
         }
-        for (const Span &sp : spans)
-            if (st == SGL_OK &&
-                cudaMemcpyAsync(sp.dst, sp.src, sp.n, cudaMemcpyDeviceToHost, ls.lane->stream) != cudaSuccess)
+        bool issued = false;
+        for (const Span &sp : spans) {
+            if (cudaMemcpyAsync(sp.dst, sp.src, sp.n, cudaMemcpyDeviceToHost, ls.lane->stream) != cudaSuccess) {
+                cudaGetLastError(); // reported through the requests' status, not a later call
                 st = SGL_ERR_CUDA;
-        // the lane's done event must come after the copies
-        if (st == SGL_OK && cudaEventRecord(ls.lane->slots[ls.slot].done, ls.lane->stream) != cudaSuccess)
+                break;
+            }
+            issued = true;
+        }
+        // the lane's done event must come after every copy that was issued, so
+        // that no request is reported done while its host buffers are written
+        if (issued && cudaEventRecord(ls.lane->slots[ls.slot].done, ls.lane->stream) != cudaSuccess) {
+            cudaGetLastError();
             st = SGL_ERR_CUDA;
+        }
     }
     for (auto &j : jobs) {
         j.res.start_s = t0;
