@@ -235,10 +235,11 @@ SGL_API sgl_status sgl_render(sgl_ctx *ctx, int scene_id, const sgl_view *views,
  * allocates nothing on a GPU because it has none).  All scratch comes from one
  * 64 MiB static device array that every GPU loading the library keeps until
  * exit; views needing more are refused with SGL_ERR_BUDGET.  Targets are
- * device buffers; asynchronous on `stream`.  The array is shared: calls that
- * overlap on the GPU race, so order them.  The first call on a device looks
- * up the array's address (cudaGetSymbolAddress); make it before any stream
- * capture. */
+ * device buffers; asynchronous on `stream`.  The array is shared by every
+ * call in a CUDA context (each context has its own copy): calls that overlap
+ * on the GPU in one context race, so order them.  The first call in a context
+ * looks up the array's address there (cudaGetSymbolAddress) and caches it
+ * under the context's id; make that first call before any stream capture. */
 SGL_API sgl_status sgl_render_noalloc(sgl_ctx *ctx, int scene_id, const sgl_view *view, const sgl_target *target,
                                       void *stream);
 

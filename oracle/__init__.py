@@ -23,7 +23,8 @@ from swegl_gb300 import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libsgl_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libswegl_ref.so")
-REFERENCE_SRC = "/root/reference"
+# where the reference sources lie (a build-container checkout; absent elsewhere)
+REFERENCE_SRC = os.environ.get("SWEGL_REFERENCE", "/root/reference")
 
 KIND_FULL, KIND_ORDINAL, KIND_PROGRESS, KIND_PHONG, KIND_TEXTURE = 0, 1, 2, 3, 4
 
@@ -36,7 +37,7 @@ def build(reference: bool | None = None) -> None:
     if reference is None:
         reference = os.path.isdir(os.path.join(REFERENCE_SRC, "src", "render"))
     if reference:
-        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "-j8"], check=True)
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "-j8", "REF=" + REFERENCE_SRC], check=True)
 
 
 def restatement() -> C.CDLL:

@@ -14,24 +14,30 @@
 // kNoAllocScratchBytes (64 MiB).  Every GPU that loads the library holds it
 // until the process exits.  Views whose scratch does not fit are refused with
 // SGL_ERR_BUDGET and a message giving the bytes needed.  The call makes no
-// cudaMalloc, cudaFree or other allocating call; its descriptors are built on
-// the host stack and copied into the array.
+// cudaMalloc, cudaFree or other allocating call.  Its descriptors are passed
+// by value to a one-block kernel that writes them into the array (kernel
+// arguments are copied at launch, so no host buffer has to outlive the call).
 //
-// The array is shared by every call on a device and keeps the last call's
-// contents; each call clears what must start cleared (the counters, and the
-// depth keys to all ones) with cudaMemsetAsync; the visibility flags are
-// cleared by the kernels.  Calls
-// that overlap on the GPU — on different streams, or from different contexts
-// of the same device — race on the array: the caller must order them.
+// The array is shared by every call in a CUDA context and keeps the last
+// call's contents; each call clears what must start cleared (the counters in
+// the descriptor kernel, the depth keys to all ones with cudaMemsetAsync; the
+// visibility flags are cleared by the kernels).  Calls that overlap on the
+// GPU in one context (on different streams, or from different host threads)
+// race on the array: the caller must order them.  Each CUDA context has its
+// own copy of the array, so calls in different contexts do not share it.
 //
-// Set-up: the first call on a device, with that device current, looks up the
-// array's device address with cudaGetSymbolAddress (the array's name is only
-// a host-side stand-in) and caches it for that device.  Make that first call
-// before any stream capture.
+// Set-up: the first call in a context (the device's primary context, or a
+// caller's own driver-API context made current) looks up the array's device
+// address in that context with cudaGetSymbolAddress — the array's name is
+// only a host-side stand-in — and caches it under the context's unique id
+// (cuCtxGetId: ids are never reused in a process, so a context created after
+// cudaDeviceReset gets a fresh look-up).  Make that first call before any
+// stream capture.
 #include <cstdint>
 #include <cstring>
 #include <mutex>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "sgl.h"
@@ -41,28 +47,92 @@
 namespace sgl {
 
 constexpr size_t kNoAllocScratchBytes = 64ull << 20;
-constexpr int kNoAllocMaxDevices = 64;
+constexpr int kNoAllocMaxContexts = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 static std::mutex g_noalloc_mu;
-static void *g_noalloc_addr[kNoAllocMaxDevices];
+static unsigned long long g_noalloc_ctx_id[kNoAllocMaxContexts]; // 0: free entry
+static void *g_noalloc_addr[kNoAllocMaxContexts];
+static int g_noalloc_next;
 
-// The device address of the scratch array on `device` (which must be current).
-static cudaError_t noalloc_scratch(int device, unsigned char **out)
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// The unique id of the current CUDA context (the runtime's current context,
+// after cudaSetDevice: the device's primary context unless the caller made
+// its own current).  The driver functions are looked up through the runtime,
+// so the library does not link the driver library itself.
+static cudaError_t current_context_id(unsigned long long *id)
 {
-    if (device < 0 || device >= kNoAllocMaxDevices)
-        return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_addr[device]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *f0 = nullptr, *f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0, q1;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 4000, cudaEnableDefault, &q0);
+        if (e == cudaSuccess)
+            e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1);
         if (e != cudaSuccess)
             return e;
-        g_noalloc_addr[device] = p;
+        if (q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+            return cudaErrorSymbolNotFound;
+        get_current = (CtxGetCurrentFn)f0;
+        get_id = (CtxGetIdFn)f1;
     }
-    *out = (unsigned char *)g_noalloc_addr[device];
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c)
+        return cudaErrorDeviceUninitialized;
+    if (get_id(c, id) != CUDA_SUCCESS)
+        return cudaErrorDeviceUninitialized;
     return cudaSuccess;
+}
+
+// The device address of the scratch array in the current context, looked up
+// once per context and cached under the context's id.
+static cudaError_t noalloc_scratch(unsigned char **out)
+{
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    unsigned long long id = 0;
+    cudaError_t e = current_context_id(&id);
+    if (e != cudaSuccess)
+        return e;
+    for (int i = 0; i < kNoAllocMaxContexts; i++)
+        if (g_noalloc_ctx_id[i] == id) {
+            *out = (unsigned char *)g_noalloc_addr[i];
+            return cudaSuccess;
+        }
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        return e;
+    const int slot = g_noalloc_next; // the oldest entry makes room (its context is looked up again if used)
+    g_noalloc_next = (g_noalloc_next + 1) % kNoAllocMaxContexts;
+    g_noalloc_ctx_id[slot] = id;
+    g_noalloc_addr[slot] = p;
+    *out = (unsigned char *)p;
+    return cudaSuccess;
+}
+
+// The call's descriptors, passed by value: the item, the batch, the prefix
+// arrays and the counters to zero.
+struct NoAllocBases {
+    uint32_t v[16];
+};
+__global__ void k_noalloc_setup(ItemDev it, BatchDev b, NoAllocBases bases, ItemDev *item_dst, BatchDev *batch_dst,
+                                uint32_t *bases_dst, unsigned long long *counters, unsigned long long *item_counters)
+{
+    const int t = threadIdx.x;
+    if (t == 0) {
+        *item_dst = it;
+        *batch_dst = b;
+    }
+    if (t < 16)
+        bases_dst[t] = bases.v[t];
+    for (int i = t; i < kCounterWords; i += blockDim.x)
+        counters[i] = 0ull;
+    if (t < 2)
+        item_counters[t] = 0ull;
 }
 
 static size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -139,7 +209,7 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
         return SGL_ERR_BUDGET;
     }
     unsigned char *base = nullptr;
-    cudaError_t e = noalloc_scratch(ctx->device, &base);
+    cudaError_t e = noalloc_scratch(&base);
     if (e != cudaSuccess) {
         ctx->fail("sgl_render_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
         return SGL_ERR_CUDA;
@@ -178,10 +248,10 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     const uint32_t dof_tiles =
         dof ? (uint32_t)((v.w + kDofTile - 1) / kDofTile) * (uint32_t)((v.h + kDofTile - 1) / kDofTile) : 0u;
     const bool fused = s->dev.fused != 0;
-    const uint32_t bases[16] = {0u, (uint32_t)nv,                 0u, (uint32_t)nt,
-                                0u, (uint32_t)px,                 0u, (uint32_t)tiles,
-                                0u, dof_tiles,                    0u, fused ? 0u : (uint32_t)nv,
-                                0u, fused ? 0u : (uint32_t)nt,    0u, fused ? s->dev.n_prims : 0u};
+    const NoAllocBases bases = {{0u, (uint32_t)nv,              0u, (uint32_t)nt,
+                                 0u, (uint32_t)px,              0u, (uint32_t)tiles,
+                                 0u, dof_tiles,                 0u, fused ? 0u : (uint32_t)nv,
+                                 0u, fused ? 0u : (uint32_t)nt, 0u, fused ? s->dev.n_prims : 0u}};
     BatchDev b{};
     b.items = (const ItemDev *)(base + o_item);
     const uint32_t *bp = (const uint32_t *)(base + o_bases);
@@ -214,13 +284,11 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     b.item_counters = (unsigned long long *)(base + o_item_counters);
     b.slot_flags = nullptr;
     cudaStream_t st = (cudaStream_t)stream;
-    // descriptors from the host stack (pageable copies return once staged)
-    CUDA_TRY(cudaMemcpyAsync(base + o_item, &it, sizeof it, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(base + o_bases, bases, sizeof bases, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(base + o_batch, &b, sizeof b, cudaMemcpyHostToDevice, st));
-    // the counters must start at zero on every call
-    CUDA_TRY(cudaMemsetAsync(base + o_counters, 0, kCounterWords * sizeof(unsigned long long), st));
-    CUDA_TRY(cudaMemsetAsync(base + o_item_counters, 0, 2 * sizeof(unsigned long long), st));
+    // descriptors by value; the counters start at zero on every call
+    k_noalloc_setup<<<1, 256, 0, st>>>(it, b, bases, (ItemDev *)(base + o_item), (BatchDev *)(base + o_batch),
+                                       (uint32_t *)(base + o_bases), (unsigned long long *)(base + o_counters),
+                                       (unsigned long long *)(base + o_item_counters));
+    CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemsetAsync(base + o_key, 0xFF, 8 * px, st)); // kEmptyKey
 
     const int seq = (dof ? kSeqDof : 0) | (v.shader != SGL_SHADER_PHONG_BILINEAR ? kSeqShaders : 0) |

@@ -147,6 +147,45 @@ def test_64_viewports_full_size(rig):
     r.release(sid)
 
 
+def test_64_viewports_of_the_cube(rig):
+    """The batched configuration on the literal textured-cube scene (the
+    640x480 configuration's cube): 64 seeded cameras on a sphere of radius
+    35 around it, viewports log-uniform from 128x128 to 1920x1080, one
+    graph-captured launch sequence with the autotuner's tile and span bin.
+    Every viewport equals its one-frame-per-launch render bit for bit and the
+    oracle (depth bit-exact, colour within 2 LSB, within 1 LSB on >= 99.9 %
+    of pixels)."""
+    import os
+
+    r, torch = rig
+    sc = G.scene("cube")
+    sid = r.upload(sc)
+    views = S.batch_views(64, seed=31)
+    bufs, tgts = device_targets(torch, views)
+    items = [(sid, v, t) for v, t in zip(views, tgts)]
+    chosen = r.autotune(items)
+    st = r.render_batch(items, tile=chosen["tile"], span_bin=chosen["span_bin"], use_graph=True, stats=True)
+    torch.cuda.synchronize()
+    assert st["fragments"] > 0
+    got = frames_of(bufs)
+    exp = oracle.render_parallel(sc, views, max(1, min(16, os.cpu_count() or 1)))
+    within1 = total = covered = 0
+    for i, v in enumerate(views):
+        alone, _ = r.render(sid, [v])
+        assert np.array_equal(got[i][0], alone[0].pixels), i
+        assert np.array_equal(got[i][1].view(np.uint32), alone[0].zbuffer.view(np.uint32)), i
+        assert np.array_equal(got[i][1].view(np.uint32), exp[i].zbuffer.view(np.uint32)), i
+        d = np.abs(got[i][0].view(np.uint8).astype(np.int16) - exp[i].pixels.view(np.uint8).astype(np.int16))
+        assert int(d.max()) <= 2, i
+        per_px = d.reshape(-1, 4).max(axis=1)
+        within1 += int((per_px <= 1).sum())
+        total += per_px.size
+        covered += int((got[i][1].view(np.uint32) != 0x7F7F7F7F).sum())
+    assert within1 >= 0.999 * total
+    assert covered > 1000  # the cube is seen
+    r.release(sid)
+
+
 def test_graph_replay_and_autotune(rig):
     r, torch = rig
     sc = G.scene("spheres200")

@@ -118,6 +118,57 @@ def test_serving_same_alone_and_in_the_mix(renderer):
         renderer.release(sid)
 
 
+def test_serving_full_size_scenes_alone_and_in_the_mix(renderer):
+    """The serving configuration's own inputs at a bounded request count: the
+    8 resident scenes of 10k ... 2M triangles, and the first 32 requests of
+    its seeded stream (viewports log-uniform 64x64 ... 3840x2160, depth of
+    field on half of them), submitted at once to the continuous-batching loop
+    under the 40 GB budget.  Each frame equals the one-frame-per-launch
+    render of the same request alone (bit for bit) and the oracle (depth
+    bit-exact, colour within 2 LSB and within 1 LSB on >= 99.9 % of
+    pixels)."""
+    import os
+
+    scenes = S.serving_scenes()
+    sids = [renderer.upload(sc) for sc in scenes]
+    reqs = S.serving_requests(32, seed=61)
+    assert any(v.dof for (_, _, v) in reqs) and any(not v.dof for (_, _, v) in reqs)
+    assert max(v.w * v.h for (_, _, v) in reqs) > 1_000_000
+    srv = renderer.server(budget_bytes=40 << 30, max_batch=16, streams=3, copy_out=True)
+    outs, tickets = [], []
+    for (_, k, v) in reqs:
+        pix = np.zeros((v.h, v.w), np.uint32)
+        z = np.zeros((v.h, v.w), np.float32)
+        outs.append((pix, z))
+        tickets.append(srv.submit(sids[k], v, pix, z))
+    results = [srv.wait(t, 300.0) for t in tickets]
+    srv.close()
+    assert all(r["status"] == 0 for r in results)
+    threads = max(1, min(16, os.cpu_count() or 1))
+    by_scene = {}
+    for j, (_, k, v) in enumerate(reqs):
+        by_scene.setdefault(k, []).append(j)
+    within1 = total = 0
+    for k, js in by_scene.items():
+        exp = oracle.render_parallel(scenes[k], [reqs[j][2] for j in js], threads)
+        for j, e in zip(js, exp):
+            v = reqs[j][2]
+            pix, z = outs[j]
+            alone, st = renderer.render(sids[k], [v], stats=True)
+            assert np.array_equal(pix, alone[0].pixels), ("frame differs in the mix", j)
+            assert np.array_equal(z.view(np.uint32), alone[0].zbuffer.view(np.uint32)), j
+            assert results[j]["fragments"] == st["fragments"], j
+            assert np.array_equal(z.view(np.uint32), e.zbuffer.view(np.uint32)), ("depth differs from the oracle", j)
+            d = np.abs(pix.view(np.uint8).astype(np.int16) - e.pixels.view(np.uint8).astype(np.int16))
+            assert int(d.max()) <= 2, j
+            per_px = d.reshape(-1, 4).max(axis=1)
+            within1 += int((per_px <= 1).sum())
+            total += per_px.size
+    assert within1 >= 0.999 * total
+    for sid in sids:
+        renderer.release(sid)
+
+
 def test_serving_budget_and_poll(renderer):
     from swegl_gb300.runtime import SglError
 
