@@ -8,16 +8,20 @@ camera on a sphere of radius 35, viewport sides log-uniform 64..3840 x
 64..2160, depth of field with probability 0.5) served by the library's
 continuous-batching loop under a 40 GB budget.
 
-  value     served frames/s at saturation: each step submits 256 requests of
-            the stream at once and drains them (closed loop).  Timed with
+  value     served frames/s at saturation: each step submits 4096 requests
+            of the stream at once and drains them (closed loop).  Timed with
             CUDA events on the default stream, which the serving streams are
             ordered with.
   sequential_frames_per_s  the same requests through the plain
             one-frame-per-launch renderer, one call after another.
   latency   p50/p99/p999 with the requests submitted at their Poisson
-            arrival times (open loop) for --duration seconds.
-  e2e       closed-loop steps again, every frame (colour + depth) copied to
-            pinned host memory through the public API.
+            arrival times (open loop) for --duration seconds (60 by
+            default), every frame copied to pinned host memory: delivered
+            (frame in the caller's buffers) and rendered (frame complete in
+            device memory) latencies of the same run.
+  e2e       closed loop through the public API, every frame (colour + depth)
+            copied to pinned host memory, in pipelined chunks of 256
+            requests for at least 2 s.
   roofline  the plain renderer's 1080p frame of the 200-sphere scene
             (819,200 triangles): algorithmic bytes / device time, against the
             measured HBM copy bandwidth; per-stage times from CUDA events.
@@ -27,6 +31,9 @@ torchrun (N > 1) every rank serves its own stream (replicas, no collective);
 value sums the frames of all ranks over the max-over-ranks time.
 
 --workload frame times the plain renderer alone on the 1080p frame.
+--workload batch64 times 64 viewports of uneven size in one graph-captured
+launch sequence (autotuned tile and span bin) against the same views one
+frame per launch sequence.
 --workload layers times a 1080p frame with 4 transparency layers of the
 200-sphere scene whose textures carry block alpha (translucent spheres).
 --impl reference times the reference's CPU algorithm (the oracle's C
@@ -458,6 +465,134 @@ def run_layers(args, rank, world, local_rank):
     return out if rank == 0 else None
 
 
+# ----------------------------------------------------------- 64-view batch --
+def run_batch64(args, rank, world, local_rank):
+    """64 viewports of the 200-sphere scene (seeded cameras on a sphere of
+    radius 35, sizes log-uniform 128x128 ... 1920x1080) in one graph-captured
+    launch sequence with the autotuner's tile and span bin, against the same
+    64 views through the plain one-frame-per-launch renderer."""
+    import torch
+
+    from swegl_gb300 import scenes as S
+    from swegl_gb300.runtime import Renderer
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    r = Renderer(local_rank)
+    scene = S.spheres_scene()
+    views = S.batch_views(64)
+    copies = [r.upload(scene) for _ in range(4)]  # ~400 MB in rotation, above L2
+    bufs, tgts = [], []
+    for v in views:
+        b, t = device_target(torch, v.w, v.h)
+        bufs.append(b)
+        tgts.append(t)
+    items = lambda c: [(c, v, t) for v, t in zip(views, tgts)]  # noqa: E731
+    chosen = r.autotune(items(copies[0]))
+    stream = torch.cuda.Stream()
+
+    def step(k):
+        r.render_batch(items(copies[k % len(copies)]), tile=chosen["tile"], span_bin=chosen["span_bin"],
+                       use_graph=True, stream=stream.cuda_stream)
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    st = r.render_batch(items(copies[0]), tile=chosen["tile"], span_bin=chosen["span_bin"], use_graph=True,
+                        stream=stream.cuda_stream, stats=True)
+    torch.cuda.synchronize()
+    gpu_frames = [(p.cpu().numpy().view(np.uint32).copy(), z.cpu().numpy().copy()) for (p, z) in bufs]
+    if dist:
+        dist.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local_rank) as clocks:
+        for k in range(args.steps):
+            starts[k].record(stream)
+            step(k)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    batch_ms = max_over_ranks(torch, dist, sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps)
+    # the same 64 views one frame per launch sequence
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for k in range(2):
+        for i, v in enumerate(views):
+            r.render_device(copies[k % len(copies)], [v], [tgts[i]], stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    seq = []
+    for k in range(args.steps):
+        e0.record(stream)
+        for i, v in enumerate(views):
+            r.render_device(copies[k % len(copies)], [v], [tgts[i]], stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        seq.append(e0.elapsed_time(e1))
+    seq_ms = max_over_ranks(torch, dist, sum(seq) / len(seq))
+    # end to end: the batch, then every frame (colour + depth) to pinned host memory
+    host = [(torch.empty((v.h, v.w), dtype=torch.int32).pin_memory(),
+             torch.empty((v.h, v.w), dtype=torch.float32).pin_memory()) for v in views]
+    d2h = sum(8 * v.w * v.h for v in views)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step(k)
+        with torch.cuda.stream(stream):
+            for (hp, hz), (dp, dz) in zip(host, bufs):
+                hp.copy_(dp, non_blocking=True)
+                hz.copy_(dz, non_blocking=True)
+        stream.synchronize()
+    e2e_fps = 64 * args.steps / (time.perf_counter() - t0)
+    from swegl_gb300 import abi
+
+    fps = world * 64 * 1e3 / batch_ms
+    px = sum(v.w * v.h for v in views)
+    alg = sum(frame_alg_bytes(scene, v.w, v.h) for v in views)
+    peaks = measured_peaks()
+    achieved = alg / (batch_ms / 1e3) / 1e9
+    out = {
+        "metric": "frames/s (64 viewports of uneven size in one graph-captured launch sequence)",
+        "value": round(fps, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(batch_ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic (seeded scene and cameras, swegl_gb300/scenes.py)",
+        "config": {"workload": "spheres200_64_viewports_batch", "triangles": scene.n_triangles, "views": 64,
+                   "pixels": px, "viewports": "log-uniform 128x128..1920x1080, cameras on a sphere of radius 35",
+                   "autotuned": chosen,
+                   "l2": "inputs larger than L2: 4 resident scene copies in rotation, 64 frames of %d MB"
+                         % (8 * px // 1000000)},
+        "sequential_frames_per_s": round(world * 64 * 1e3 / seq_ms, 2),
+        "batched_over_sequential": round(seq_ms / batch_ms, 3),
+        "gfragments_per_s": round(st["fragments"] * world * 1e3 / batch_ms / 1e9, 3),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": peaks["source"],
+                     "unit_of_work": "64 views, each charged the algorithmic bytes of a frame of the scene "
+                                     "(%d bytes in all)" % alg, "traffic": None},
+        "e2e": {"value": round(e2e_fps, 2), "unit": "frames/s", "h2d_bytes_per_step": 64 * C.sizeof(abi.BatchItem),
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(st["kernel_launches"]) * args.steps,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+
+        threads = cpu_threads()
+        t1 = time.perf_counter()
+        cpu_frames = oracle.render_parallel(scene, views, threads)
+        dt = time.perf_counter() - t1
+        out["cpu_baseline"] = {"value": round(64 / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+                               "sample": f"the 64 views on {threads} threads ({dt:.1f} s)",
+                               "parity": parity_of(gpu_frames, cpu_frames)}
+    for c in copies:
+        r.release(c)
+    r.close()
+    if dist:
+        dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
 def serve_config(args) -> dict:
     from swegl_gb300 import scenes as S
 
@@ -465,6 +600,7 @@ def serve_config(args) -> dict:
             "scene_triangles": list(S.SERVE_TRIANGLES), "requests_per_step": args.requests_per_step,
             "budget_bytes": args.budget, "max_batch": args.max_batch, "streams": args.streams,
             "latency_duration_s": args.duration, "arrival_rate": 2000,
+            "timed_requests": args.steps * args.requests_per_step,
             "l2": "inputs larger than L2: 8 resident scenes of ~1.9 GB"}
 
 
@@ -539,12 +675,12 @@ def run_serve(args, rank, world, local_rank):
     torch.cuda.synchronize()
     batched_same_fps = n_seq / (e0.elapsed_time(e1) / 1e3)
 
-    # open-loop latency at the Poisson arrival times
-    lat = latency_run(srv, sids, args.duration, seed=70 + rank)
+    srv.close()
+    # open-loop latency at the Poisson arrival times, frames delivered to the host
+    lat = latency_run(r, torch, sids, args.duration, 70 + rank, args)
 
     # e2e: closed loop with every frame copied to pinned host memory
-    e2e_fps, h2d, d2h = e2e_run(r, torch, sids, timed, M, args)
-    srv.close()
+    e2e = e2e_run(r, torch, sids, timed, args)
 
     fm = frame_measure(r, torch, 10, 3, False)
     gpu_launches = int(b1["kernels"] - b0["kernels"])
@@ -561,8 +697,9 @@ def run_serve(args, rank, world, local_rank):
         "batches": int(b1["batches"] - b0["batches"]),
         "frame_1080p": {"frames_per_s": round(1e3 / fm["frame_ms"], 1), "kernels": kernels_of(fm)},
         "roofline": roofline_of(fm),
-        "e2e": {"value": round(e2e_fps, 2), "unit": "frames/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+        "e2e": {"value": round(e2e["fps"], 2), "unit": "frames/s", "h2d_bytes_per_step": e2e["h2d"],
+                "d2h_bytes_per_step": e2e["d2h"], "step": "%d requests submitted together" % args.e2e_chunk,
+                "chunks": e2e["chunks"], "requests": e2e["requests"], "seconds": round(e2e["seconds"], 2)},
         "gpu_launches": gpu_launches,
         "clocks": clocks.summary(),
     }
@@ -586,11 +723,66 @@ def _retarget(tgt, v):
     return t
 
 
-def latency_run(srv, sids, duration: float, seed: int) -> dict:
+def _pct(a: np.ndarray) -> dict:
+    return {"p50": round(float(np.percentile(a, 50)), 3), "p99": round(float(np.percentile(a, 99)), 3),
+            "p999": round(float(np.percentile(a, 99.9)), 3), "mean": round(float(a.mean()), 3)}
+
+
+class PinnedRing:
+    """Host frame buffers for the requests in flight, carved in order from one
+    pinned pool; a region is reused once the requests holding it are done
+    (their results are collected then)."""
+
+    def __init__(self, torch, srv, nbytes: int):
+        self.pool = torch.empty(nbytes // 4, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+        self.n = self.pool.size
+        self.srv = srv
+        self.head = 0
+        self.live = []  # (ticket, start, end) in submission order
+        self.results = {}
+
+    def _retire_first(self):
+        t, _, _ = self.live.pop(0)
+        self.results[t] = self.srv.wait(t, 600.0)
+
+    def take(self, words: int):
+        if words > self.n:
+            raise RuntimeError("frame larger than the pinned ring")
+        if self.head + words > self.n:
+            self.head = 0
+        lo, hi = self.head, self.head + words
+        while self.live and any(not (e <= lo or s >= hi) for (_, s, e) in self.live):
+            self._retire_first()
+        self.head = hi
+        return lo, hi
+
+    def submit(self, sid, v):
+        px = v.w * v.h
+        lo, hi = self.take(2 * px)
+        pix = self.pool[lo:lo + px].reshape(v.h, v.w)
+        z = self.pool[lo + px:hi].view(np.float32).reshape(v.h, v.w)
+        t = self.srv.submit(sid, v, pix, z)
+        self.live.append((t, lo, hi))
+        return t
+
+    def finish(self):
+        while self.live:
+            self._retire_first()
+        return self.results
+
+
+def latency_run(r, torch, sids, duration: float, seed: int, args) -> dict:
+    """Open loop: the requests of a seeded stream submitted at their Poisson
+    arrival times for `duration` seconds, through a server that copies every
+    frame (colour + depth) to pinned host memory.  Two latencies per request:
+    delivered (submit -> frame in the caller's host buffers) and rendered
+    (submit -> frame complete in device memory, before its copy)."""
     from swegl_gb300 import scenes as S
 
-    stream_reqs = S.serving_requests(int(2000 * duration) + 1, seed=seed)
+    stream_reqs = S.serving_requests(int(2000 * duration * 1.05) + 16, seed=seed)
     stream_reqs = [q for q in stream_reqs if q[0] <= duration]
+    srv = r.server(budget_bytes=args.budget, max_batch=args.max_batch, streams=args.streams, copy_out=True)
+    ring = PinnedRing(torch, srv, args.ring_bytes)
     t0 = time.perf_counter()
     tickets = []
     for (arrival, k, v) in stream_reqs:
@@ -600,45 +792,69 @@ def latency_run(srv, sids, duration: float, seed: int) -> dict:
                 break
             if dt > 0.0005:
                 time.sleep(dt - 0.0003)
-        tickets.append(srv.submit(sids[k], v))
-    results = [srv.wait(t, 600.0) for t in tickets]
+        tickets.append(ring.submit(sids[k], v))
+    res = ring.finish()
     wall = time.perf_counter() - t0
-    lats = np.array([1e3 * (x["done_s"] - x["submit_s"]) for x in results])
-    return {"p50": round(float(np.percentile(lats, 50)), 3), "p99": round(float(np.percentile(lats, 99)), 3),
-            "p999": round(float(np.percentile(lats, 99.9)), 3), "mean": round(float(lats.mean()), 3),
-            "requests": len(results), "served_frames_per_s": round(len(results) / wall, 1),
-            "offered_rate": 2000}
+    srv.close()
+    results = [res[t] for t in tickets]
+    assert all(x["status"] == 0 for x in results)
+    delivered = np.array([1e3 * (x["done_s"] - x["submit_s"]) for x in results])
+    rendered = np.array([1e3 * (x["rendered_s"] - x["submit_s"]) for x in results])
+    return {"delivered": _pct(delivered), "rendered": _pct(rendered), "requests": len(results),
+            "duration_s": duration, "served_frames_per_s": round(len(results) / wall, 1), "offered_rate": 2000,
+            "delivered_bytes": int(sum(8 * v.w * v.h for (_, _, v) in stream_reqs))}
 
 
-def e2e_run(r, torch, sids, timed, M: int, args):
-    """Closed-loop steps with copy-out of every frame to pinned host memory."""
+def e2e_run(r, torch, sids, timed, args):
+    """Closed loop through the public API with every frame (colour + depth)
+    copied to pinned host memory: chunks of args.e2e_chunk requests of the
+    stream, each chunk's frames into one half of a pinned pool (chunk k + 2
+    reuses chunk k's half once chunk k is delivered, so the GPU is never left
+    idle between chunks); chunks are taken from the timed requests in turn
+    until at least args.e2e_seconds have passed (and at least 8 chunks)."""
+    M = args.e2e_chunk
+    chunks = [timed[i:i + M] for i in range(0, len(timed) - M + 1, M)] or [timed[:M]]
+    half = max(sum(2 * v.w * v.h for (_, _, v) in ch) for ch in chunks) + 16
+    pool = torch.empty(2 * half, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
     srv = r.server(budget_bytes=args.budget, max_batch=args.max_batch, streams=args.streams, copy_out=True)
-    steps = max(1, min(args.steps, 8))
-    chunks = [timed[s * M:(s + 1) * M] for s in range(steps)]
-    need = max(sum(8 * v.w * v.h for (_, _, v) in ch) for ch in chunks)
-    pool = torch.empty(need // 4 + 16, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
 
-    def run_chunk(ch):
-        off = 0
+    def submit_chunk(ch, h):
+        off, tk = h * half, []
         for (_, k, v) in ch:
             px = v.w * v.h
             pix = pool[off:off + px].reshape(v.h, v.w)
             z = pool[off + px:off + 2 * px].view(np.float32).reshape(v.h, v.w)
             off += 2 * px
-            srv.submit(sids[k], v, pix, z)
-        srv.drain(600.0)
+            tk.append(srv.submit(sids[k], v, pix, z))
+        return tk
 
-    run_chunk(chunks[0])  # warm-up
+    def collect(tk):
+        for t in tk:
+            assert srv.wait(t, 600.0)["status"] == 0
+
+    collect(submit_chunk(chunks[0], 0))  # warm-up
+    inflight = []
+    n = nbytes = 0
     t0 = time.perf_counter()
-    for ch in chunks:
-        run_chunk(ch)
+    k = 0
+    while True:
+        if len(inflight) == 2:
+            collect(inflight.pop(0))
+        if k >= 8 and time.perf_counter() - t0 >= args.e2e_seconds:
+            break
+        ch = chunks[k % len(chunks)]
+        inflight.append(submit_chunk(ch, k % 2))
+        n += len(ch)
+        nbytes += sum(8 * v.w * v.h for (_, _, v) in ch)
+        k += 1
+    for tk in inflight:
+        collect(tk)
     dt = time.perf_counter() - t0
     srv.close()
     from swegl_gb300 import abi
 
-    h2d = C.sizeof(abi.Request) * M
-    d2h = int(sum(8 * v.w * v.h for ch in chunks for (_, _, v) in ch) / steps)
-    return steps * M / dt, h2d, d2h
+    return {"fps": n / dt, "h2d": C.sizeof(abi.Request) * M, "d2h": int(nbytes / k), "chunks": k, "seconds": dt,
+            "requests": n}
 
 
 def parity_of(gpu_frames, cpu_frames) -> dict:
@@ -704,8 +920,19 @@ def cpu_serve_baseline(scenes, timed, args, gpu_frames=None) -> dict:
         render_chunk(timed[n:n + chunk], False)
         n += chunk
     dt = time.perf_counter() - t0
+    # single-thread latency: requests of the stream one at a time on one thread
+    lat, t1 = [], time.perf_counter()
+    for (_, k, v) in timed:
+        ta = time.perf_counter()
+        oracle.render(scenes[k], [v])
+        lat.append(time.perf_counter() - ta)
+        if len(lat) >= 64 or time.perf_counter() - t1 >= args.cpu_seconds / 2:
+            break
     out = {"value": round(n / dt, 3), "unit": "frames/s", "cores": threads, "kind": "port",
-           "sample": f"the first {n} requests of the stream on {threads} threads ({dt:.1f} s)"}
+           "sample": f"the first {n} requests of the stream on {threads} threads ({dt:.1f} s)",
+           "single_thread_ms": {"mean": round(1e3 * float(np.mean(lat)), 2),
+                                "p50": round(1e3 * float(np.median(lat)), 2),
+                                "requests": len(lat)}}
     if gpu_frames is not None:
         out["parity"] = parity_of(gpu_frames, cpu_frames)
     return out
@@ -720,7 +947,19 @@ def run_reference(args, rank, world):
     from swegl_gb300 import scenes as S
 
     threads = cpu_threads()
-    if args.workload == "frame":
+    if args.workload == "batch64":
+        scene = S.spheres_scene()
+        views = S.batch_views(64)
+        cfg = {"workload": "spheres200_64_viewports_batch", "triangles": scene.n_triangles, "views": 64}
+        metric = "frames/s (64 viewports of uneven size in one graph-captured launch sequence)"
+        oracle.render_parallel(scene, views[:threads], threads)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            oracle.render_parallel(scene, views, threads)
+            times.append(time.perf_counter() - t0)
+        n_per_step = len(views)
+    elif args.workload == "frame":
         scene = S.spheres_scene()
         views = [S.spheres_view(1920, 1080)] * threads
         cfg = {"workload": "spheres200_1080p_frame", "triangles": scene.n_triangles, "viewport": "1920x1080"}
@@ -771,10 +1010,13 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["serve", "frame", "dof", "layers"], default="serve")
-    ap.add_argument("--requests-per-step", type=int, default=256)
+    ap.add_argument("--workload", choices=["serve", "frame", "dof", "layers", "batch64"], default="serve")
+    ap.add_argument("--requests-per-step", type=int, default=4096)
     ap.add_argument("--seq-requests", type=int, default=512)
-    ap.add_argument("--duration", type=float, default=10.0, help="open-loop latency run, seconds")
+    ap.add_argument("--duration", type=float, default=60.0, help="open-loop latency run, seconds")
+    ap.add_argument("--ring-bytes", type=int, default=4 << 30, help="latency run: pinned host frames in flight")
+    ap.add_argument("--e2e-chunk", type=int, default=256, help="e2e: requests submitted together")
+    ap.add_argument("--e2e-seconds", type=float, default=2.0, help="e2e: at least this long")
     ap.add_argument("--budget", type=int, default=40 << 30)
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--streams", type=int, default=3)
@@ -792,6 +1034,8 @@ def main():
         out = run_frame(args, rank, world, local_rank)
     elif args.workload == "layers":
         out = run_layers(args, rank, world, local_rank)
+    elif args.workload == "batch64":
+        out = run_batch64(args, rank, world, local_rank)
     else:
         out = run_serve(args, rank, world, local_rank)
     if out is not None:

@@ -328,7 +328,11 @@ typedef struct sgl_request {
 
 typedef struct sgl_request_result {
     sgl_status status;
-    double     submit_s, start_s, done_s; /* steady host clock, seconds */
+    double     submit_s, start_s, done_s; /* steady host clock, seconds; done_s: delivered (after the copy to
+                                             the host buffers when the server copies out) */
+    double     rendered_s;                /* when the frame was complete in device memory: done_s less the
+                                             device time of the batch's copies to the host (= done_s
+                                             without copy-out) */
     uint64_t   fragments;                 /* covered (triangle, pixel) pairs */
 } sgl_request_result;
 

@@ -100,7 +100,7 @@ class Request(C.Structure):
 
 class RequestResult(C.Structure):
     _fields_ = [("status", C.c_int), ("submit_s", C.c_double), ("start_s", C.c_double), ("done_s", C.c_double),
-                ("fragments", C.c_uint64)]
+                ("rendered_s", C.c_double), ("fragments", C.c_uint64)]
 
 
 def _ptr(a: np.ndarray, ctype):

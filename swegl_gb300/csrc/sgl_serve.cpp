@@ -55,6 +55,17 @@ struct Server {
         int slot = 0;
         bool busy = false;
         bool layered = false; // the batch is one request with transparency layers
+        // copy-out: timing events around the batch's copies to the host, so that
+        // a result also says when its frame was complete on the device
+        cudaEvent_t ev_rendered = nullptr, ev_copied = nullptr;
+        bool timed_copy = false;
+        ~LaneState()
+        {
+            if (ev_rendered)
+                cudaEventDestroy(ev_rendered);
+            if (ev_copied)
+                cudaEventDestroy(ev_copied);
+        }
     };
     std::vector<std::unique_ptr<LaneState>> lanes;
     std::mutex mu;
@@ -180,6 +191,8 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
             add(jobs[i].req.host_zbuffer, bufs[i].second, 4 * px);
         }
         bool issued = false;
+        ls.timed_copy = ls.ev_rendered && ls.ev_copied &&
+                        cudaEventRecord(ls.ev_rendered, ls.lane->stream) == cudaSuccess;
         for (const Span &sp : spans) {
             if (cudaMemcpyAsync(sp.dst, sp.src, sp.n, cudaMemcpyDeviceToHost, ls.lane->stream) != cudaSuccess) {
                 cudaGetLastError(); // reported through the requests' status, not a later call
@@ -194,6 +207,12 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
             cudaGetLastError();
             st = SGL_ERR_CUDA;
         }
+        if (ls.timed_copy && cudaEventRecord(ls.ev_copied, ls.lane->stream) != cudaSuccess) {
+            cudaGetLastError();
+            ls.timed_copy = false;
+        }
+    } else {
+        ls.timed_copy = false;
     }
     for (auto &j : jobs) {
         j.res.start_s = t0;
@@ -220,10 +239,21 @@ void Server::finish(LaneState &ls)
     std::vector<unsigned long long> per_item;
     sgl_status st = ls.lane->read_counters(&errors, ls.slot, nullptr, nullptr, &per_item);
     const double t = now_s();
+    double copy_s = 0.0; // device time of the batch's copies to the host
+    if (ls.timed_copy) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(ls.ev_copied) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, ls.ev_rendered, ls.ev_copied) == cudaSuccess && ms > 0.0f)
+            copy_s = 1e-3 * (double)ms;
+        else
+            cudaGetLastError();
+        ls.timed_copy = false;
+    }
     std::lock_guard<std::mutex> g(mu);
     for (size_t i = 0; i < ls.jobs.size(); i++) {
         Job &j = ls.jobs[i];
         j.res.done_s = t;
+        j.res.rendered_s = t - copy_s;
         if (j.res.status == SGL_OK)
             j.res.status = st;
         j.res.fragments = (2 * i + 1 < per_item.size()) ? per_item[2 * i + 1] : 0;
@@ -339,6 +369,11 @@ SGL_API sgl_status sgl_server_create(sgl_ctx *c, const sgl_serve_opts *opts, sgl
         if (st != SGL_OK) {
             delete srv;
             return st;
+        }
+        if (srv->opts.copy_out && (cudaEventCreate(&ls.ev_rendered) != cudaSuccess ||
+                                   cudaEventCreate(&ls.ev_copied) != cudaSuccess)) {
+            cudaGetLastError(); // results then carry rendered_s = done_s
+            ls.ev_rendered = ls.ev_copied = nullptr;
         }
     }
     srv->worker = std::thread([srv] { srv->run(); });

@@ -272,6 +272,7 @@ class Server:
 
     def _result(self, res: abi.RequestResult) -> dict:
         return {"status": res.status, "submit_s": res.submit_s, "start_s": res.start_s, "done_s": res.done_s,
+                "rendered_s": res.rendered_s,
                 "fragments": res.fragments}
 
     def poll(self, ticket: int):

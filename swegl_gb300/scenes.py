@@ -21,6 +21,7 @@ Scenes mirror swegl's data model (swegl/data/model.hpp:20-178):
 """
 from __future__ import annotations
 
+import functools
 import math
 from dataclasses import dataclass, field
 
@@ -129,9 +130,14 @@ def rot_x(a: float) -> np.ndarray:
     return m
 
 
-def projection(w: int, h: int, fov_y_deg: float = 60.0, near: float = 0.1, far: float = 100.0) -> np.ndarray:
+@functools.lru_cache(maxsize=16)
+def _cot_half_fov(fov_y_deg: float) -> float:
     s, c = sincos(math.radians(fov_y_deg) / 2.0)
-    cot = c / s
+    return float(c / s)
+
+
+def projection(w: int, h: int, fov_y_deg: float = 60.0, near: float = 0.1, far: float = 100.0) -> np.ndarray:
+    cot = _cot_half_fov(fov_y_deg)
     aspect = w / h
     p = np.eye(4)
     p[0, 0] = cot / aspect
@@ -193,8 +199,12 @@ def camera_on_sphere(rng: Rng, radius: float) -> tuple[np.ndarray, np.ndarray]:
     z = rng.uniform(-1.0, 1.0, 1)[0]
     yaw = rng.uniform(0.0, 2.0 * math.pi, 1)[0]
     sy, cy = sincos(yaw)
+    return _camera_at(z, float(sy), float(cy), radius)
+
+
+def _camera_at(z: float, sy: float, cy: float, radius: float) -> tuple[np.ndarray, np.ndarray]:
     rxz = math.sqrt(max(0.0, 1.0 - z * z))
-    d = np.array([rxz * float(cy), z, rxz * float(sy)])
+    d = np.array([rxz * cy, z, rxz * sy])
     return look_at_origin(radius * d)
 
 
@@ -662,18 +672,27 @@ def serving_requests(n: int, seed: int = 60, rate: float = 2000.0, n_scenes: int
     """A seeded request stream: Poisson arrivals at `rate`/s, a uniform scene,
     a camera on a sphere of `radius`, viewport sides log-uniform between
     min_wh and max_wh, depth of field with probability dof_p (focus 20,
-    aperture 0.05, at most 16 px).  Returns [(arrival_s, scene_index, View)]."""
+    aperture 0.05, at most 16 px).  Returns [(arrival_s, scene_index, View)].
+
+    Request i takes draws 7i ... 7i + 6 of the stream `seed`, in this order:
+    inter-arrival time, scene, width, height, camera z, camera yaw, depth of
+    field.  The draws are made in one vectorised pass (the same counter-hash
+    values a draw-at-a-time Rng would give)."""
     rng = Rng(seed)
+    bits = rng.bits(7 * n).reshape(n, 7) if n > 0 else np.zeros((0, 7), np.uint64)
+    u = (bits >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    scene = (bits[:, 1] % np.uint64(n_scenes)).astype(np.int64)
+    cz = -1.0 + 2.0 * u[:, 4]
+    yaw = 0.0 + (2.0 * math.pi - 0.0) * u[:, 5]
+    sy, cy = sincos(yaw)
     t = 0.0
     out = []
-    for _ in range(n):
-        u = rng.uniform(0.0, 1.0, 1)[0]
-        t += -math.log(1.0 - u) / rate
-        k = int(rng.integers(0, n_scenes - 1, 1)[0])
-        w = log_uniform_int(rng, min_wh[0], max_wh[0])
-        h = log_uniform_int(rng, min_wh[1], max_wh[1])
-        m, c = camera_on_sphere(rng, radius)
+    for i in range(n):
+        t += -math.log(1.0 - float(u[i, 0])) / rate
+        w = int(min(max_wh[0], math.floor(min_wh[0] * (max_wh[0] / min_wh[0]) ** u[i, 2])))
+        h = int(min(max_wh[1], math.floor(min_wh[1] * (max_wh[1] / min_wh[1]) ** u[i, 3])))
+        m, c = _camera_at(float(cz[i]), float(sy[i]), float(cy[i]), radius)
         v = view_for(w, h, m, c)
-        v.dof = bool(rng.uniform(0.0, 1.0, 1)[0] < dof_p)
-        out.append((t, k, v))
+        v.dof = bool(u[i, 6] < dof_p)
+        out.append((t, int(scene[i]), v))
     return out
