@@ -142,3 +142,76 @@ def dof(view, pixels: np.ndarray, zbuffer: np.ndarray) -> np.ndarray:
     if rc != 0:
         raise RuntimeError("oracle dof failed")
     return out
+
+
+# ------------------------------------------------------------------ glTF --
+class RefGltf:
+    """The scene_t the reference's own glTF loader (src/data/gltf.cpp, built
+    by oracle/ref with its nlohmann/json include resolved to a stand-in)
+    builds, as written by ref_gltf_dump (oracle/ref/ref_gltf.cpp)."""
+
+    def __init__(self):
+        self.images = 0
+        self.materials = []   # (colour uint32, metallic, roughness, texture, double sided)
+        self.nodes = []       # dicts: scale, translation, rotation, root, children, primitives
+        self.roots = []
+        self.animations = []  # (end, [(node, path, [(t, (x, y, z, w))])])
+
+
+def reference_gltf(path: str) -> RefGltf:
+    """Load `path` with the compiled reference loader."""
+    import tempfile
+
+    lib = reference()
+    lib.ref_gltf_dump.restype = C.c_int
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "dump.txt")
+        if lib.ref_gltf_dump(path.encode(), out.encode()) != 0:
+            raise RuntimeError("reference glTF dump failed")
+        tok = open(out).read().split()
+    at = 0
+
+    def word():
+        nonlocal at
+        at += 1
+        return tok[at - 1]
+
+    def num():
+        return int(word())
+
+    def f32():
+        return np.float32(float.fromhex(word()))
+
+    r = RefGltf()
+    assert word() == "images"
+    r.images = num()
+    assert word() == "materials"
+    for _ in range(num()):
+        r.materials.append((num() & 0xFFFFFFFF, f32(), f32(), num(), num()))
+    assert word() == "nodes"
+    for _ in range(num()):
+        n = {"scale": np.array([f32() for _ in range(3)], np.float32),
+             "translation": np.array([f32() for _ in range(3)], np.float32),
+             "rotation": np.array([f32() for _ in range(16)], np.float32).reshape(4, 4)}
+        n["root"] = num()
+        n["children"] = [num() for _ in range(num())]
+        prims = []
+        for _ in range(num()):
+            mode, mat, nv, ni = num(), num(), num(), num()
+            v = np.array([f32() for _ in range(8 * nv)], np.float32).reshape(nv, 8)
+            idx = np.array([num() for _ in range(ni)], np.uint32)
+            prims.append({"mode": mode, "material": mat, "vertices": v, "indices": idx})
+        n["primitives"] = prims
+        r.nodes.append(n)
+    assert word() == "roots"
+    r.roots = [num() for _ in range(num())]
+    assert word() == "animations"
+    for _ in range(num()):
+        end = f32()
+        chans = []
+        for _ in range(num()):
+            node, pth, ns = num(), num(), num()
+            steps = [(f32(), (f32(), f32(), f32(), f32())) for _ in range(ns)]
+            chans.append((node, pth, steps))
+        r.animations.append((end, chans))
+    return r

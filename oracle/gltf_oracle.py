@@ -14,11 +14,12 @@ Follows, in the reference (gbizzotto/swegl):
   read_png_file (libpng's transforms)             src/misc/image.cpp:92-172
   read_jpeg_file (libjpeg default decompression) src/misc/image.cpp:183-255
 Arithmetic is numpy float32 in the reference's order of operations.  The
-parser (nlohmann/json) is not vendored with the reference, so the loader
-cannot be compiled here: the loader restatement is pinned by the scenes it
-produces (rendered against the compiled reference's renderer) and its
-quaternion and animation arithmetic by the compiled reference's
-from_quaternion and scene_t::animate (oracle/ref/ref_harness.cpp).  PNG is
+reference's own loader is compiled too (oracle/ref, with a stand-in for its
+un-vendored nlohmann/json include, shim/json.hpp) and the library's loader is
+checked against its output (tests/test_gltf_cpu.py,
+test_loader_matches_the_reference_loader); its quaternion and animation
+arithmetic against the compiled reference's from_quaternion and
+scene_t::animate (oracle/ref/ref_harness.cpp).  PNG is
 lossless (any correct decoder gives libpng's texels); the JPEG pixel path
 restates libjpeg's published default decompression, and with libjpeg absent
 here its parity with libjpeg is unpinned.

@@ -24,8 +24,9 @@
  * Also exported: matrix44_t::from_quaternion
  * (swegl/projection/matrix44.hpp:34-43) and scene_t::animate
  * (swegl/data/model.hpp:146-177) on flat inputs, which pin the glTF node and
- * animation arithmetic of the restatement (the reference's glTF parser
- * itself needs the un-vendored nlohmann/json and is not built).
+ * animation arithmetic of the restatement.  The reference's glTF loader
+ * itself is driven by ref_gltf.cpp (its nlohmann/json include resolves to
+ * the stand-in in shim/json.hpp).
  */
 #include <cstring>
 #include <memory>

@@ -117,7 +117,7 @@ static cudaError_t noalloc_scratch(unsigned char **out)
 // The call's descriptors, passed by value: the item, the batch, the prefix
 // arrays and the counters to zero.
 struct NoAllocBases {
-    uint32_t v[16];
+    uint32_t v[20];
 };
 __global__ void k_noalloc_setup(ItemDev it, BatchDev b, NoAllocBases bases, ItemDev *item_dst, BatchDev *batch_dst,
                                 uint32_t *bases_dst, unsigned long long *counters, unsigned long long *item_counters)
@@ -127,7 +127,7 @@ __global__ void k_noalloc_setup(ItemDev it, BatchDev b, NoAllocBases bases, Item
         *item_dst = it;
         *batch_dst = b;
     }
-    if (t < 16)
+    if (t < 20)
         bases_dst[t] = bases.v[t];
     for (int i = t; i < kCounterWords; i += blockDim.x)
         counters[i] = 0ull;
@@ -176,7 +176,7 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     const size_t o_item = off;
     off += up256(sizeof(ItemDev));
     const size_t o_bases = off;
-    off += up256(16 * sizeof(uint32_t));
+    off += up256(20 * sizeof(uint32_t));
     const size_t o_counters = off;
     off += up256(kCounterWords * sizeof(unsigned long long));
     const size_t o_item_counters = off;
@@ -193,8 +193,6 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     off += up256(8 * (nt ? nt : 1));
     const size_t o_recs = off;
     off += up256(sizeof(TriRec) * (nt ? nt : 1));
-    const size_t o_recmap = off;
-    off += up256(4 * (nt ? nt : 1));
     const size_t o_tall = off;
     off += up256(4 * (nt ? nt : 1));
     const size_t o_dof = off;
@@ -248,10 +246,15 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     const uint32_t dof_tiles =
         dof ? (uint32_t)((v.w + kDofTile - 1) / kDofTile) * (uint32_t)((v.h + kDofTile - 1) / kDofTile) : 0u;
     const bool fused = s->dev.fused != 0;
+    // prefixes of one item (vertices, triangles, pixels, tiles, depth-of-field
+    // tiles, the general geometry pass's vertices and triangles), then the
+    // fused pass's one group: its chunks, its items, the item
+    const uint32_t chunks = fused ? (s->dev.n_prims + kGeomWarps - 1) / kGeomWarps : 0u;
     const NoAllocBases bases = {{0u, (uint32_t)nv,              0u, (uint32_t)nt,
                                  0u, (uint32_t)px,              0u, (uint32_t)tiles,
                                  0u, dof_tiles,                 0u, fused ? 0u : (uint32_t)nv,
-                                 0u, fused ? 0u : (uint32_t)nt, 0u, fused ? s->dev.n_prims : 0u}};
+                                 0u, fused ? 0u : (uint32_t)nt, 0u, chunks,
+                                 0u, fused ? 1u : 0u,           0u, 0u}};
     BatchDev b{};
     b.items = (const ItemDev *)(base + o_item);
     const uint32_t *bp = (const uint32_t *)(base + o_bases);
@@ -261,10 +264,13 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     b.dof_base = bp + 8;
     b.g_vtx_base = bp + 10;
     b.g_tri_base = bp + 12;
-    b.prim_base = bp + 14;
+    b.grp_chunk_base = bp + 14;
+    b.grp_item_base = bp + 16;
+    b.grp_items = bp + 18;
+    b.n_groups = fused ? 1 : 0;
     b.total_gvtx = fused ? 0u : (uint32_t)nv;
     b.total_gtri = fused ? 0u : (uint32_t)nt;
-    b.total_prims = fused ? s->dev.n_prims : 0u;
+    b.total_chunks = chunks;
     b.n_items = 1;
     b.inline_span = ctx->inline_span;
     b.total_px = (uint32_t)px;
@@ -275,7 +281,6 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     b.clip = b.list;
     b.clip_cap = b.list_cap;
     b.recs = (TriRec *)(base + o_recs);
-    b.recmap = (uint32_t *)(base + o_recmap);
     b.tall = (uint32_t *)(base + o_tall);
     b.keep_keys = 0;
     b.spans = (SpanRec *)(base + o_spans);

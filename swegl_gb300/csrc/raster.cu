@@ -352,6 +352,18 @@ struct ItemAcc {
     }
 };
 
+// The record slot of a near-clipped batch triangle: flags = kRecClip.
+__device__ __forceinline__ void mark_clip(const BatchDev *b, uint32_t r)
+{
+    reinterpret_cast<uint32_t *>(b->recs + r)[kRecFlagsWord] = kRecClip;
+}
+
+// 32-bit batch counter w (C_*)
+__device__ __forceinline__ uint32_t *counter32(const BatchDev *b, int w)
+{
+    return reinterpret_cast<uint32_t *>(b->counters) + w;
+}
+
 // Reserve n0 walk-list and n1 clip-list entries with one atomic: the two
 // 32-bit counters C_LIST and C_CLIP are the halves of one 64-bit counter word
 // (a list holds fewer than 2^31 entries, so the low half never carries).
@@ -471,11 +483,11 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
             const uint32_t j = base[1] + pos;
             if (j < b->clip_cap)
                 b->clip[b->clip_cap - 1 - j] = make_uint2(t, (uint32_t)item); // filled from the end
-            b->recmap[__ldg(b->tri_base + item) + t] = kRecClip;
+            mark_clip(b, __ldg(b->tri_base + item) + t);
         } else if (list == 0) {
             const uint32_t j = base[0] + pos;
             if (j < b->list_cap)
-                b->list[j] = make_uint2(t, (uint32_t)item);
+                b->list[j] = make_uint2(__ldg(b->tri_base + item) + t, (uint32_t)item);
         }
         __syncthreads();
     }
@@ -488,237 +500,267 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
 // primitive owns its vertices (no two vertex ranges overlap), so its
 // triangles are the only ones that flag them (renderer.cpp:86-185 flags a
 // node's primitives before any is drawn, and each primitive's vertices are
-// its own), and its compaction needs nothing from other warps.  A block's 8
-// warps take 8 consecutive primitives; their list entries are counted first
-// and both lists are reserved with one global atomic per block
-// (reserve_lists).
-constexpr int kGeomWarps = 8;
-constexpr int kGeomPrims = 1; // primitives per warp and block iteration
-__global__ void __launch_bounds__(kGeomWarps * 32, 4) k_geom(const BatchDev *b)
+// its own), and its compaction needs nothing from other warps.
+//
+// Items are taken in groups that read the same vertex data (the views of one
+// scene in the batch; the reference likewise transforms a scene to world
+// space once for all the viewports of a render call, renderer.hpp:27-34).
+// A block takes a chunk of kGeomWarps consecutive primitives of a group and
+// loads each warp's primitive once — world positions into registers, its
+// triangles as local vertex indices into shared memory — then runs it for
+// every item of the group.  The items go in passes of kGeomPass: per item the
+// warp records its walk-list and clip-list decisions as ballot masks, and
+// after the pass one global atomic reserves both lists for all the pass's
+// items and warps (reserve_lists).
+constexpr int kGeomPass = 8;                // items per list reservation
+constexpr int kGeomVPL = kFuseVerts / 32;   // vertices per lane
+constexpr int kGeomTG = kFuseTris / 32;     // groups of 32 triangles
+struct GeomShared {
+    float pos[kGeomWarps][3 * kFuseVerts];  // x, y, z' of each vertex (for the item in hand)
+    uint32_t tri[kGeomWarps][kFuseTris];    // local vertex indices a | b << 8 | c << 16
+    uint8_t yes[kGeomWarps][kFuseVerts];
+    uint32_t walk[kGeomPass][kGeomWarps][kGeomTG]; // per 32 triangles: ballot of the walk list
+    uint32_t clip[kGeomPass][kGeomWarps][kGeomTG]; // ... of the clip list
+    uint32_t cnt[kGeomPass][kGeomWarps][2];        // entries of each list, then their first positions
+    uint32_t nx[kGeomPass][kGeomWarps];            // drawable triangles without a pixel column
+    float m[kGeomPass][24];                        // view and projection rows 0-2 of each item of the pass
+    float vm[kGeomPass][4];                        // vm00, vm03, vm11, vm13
+    float4 *ndc[kGeomPass];
+    uint32_t item[kGeomPass], tri_lo[kGeomPass];
+    uint32_t next;                                 // the block's next chunk
+};
+static_assert(kFuseVerts <= 256, "local vertex indices are bytes");
+constexpr size_t kGeomSmem = sizeof(GeomShared);
+
+__global__ void __launch_bounds__(kGeomWarps * 32, 3) k_geom(const BatchDev *b)
 {
-    __shared__ float s_pos[kGeomWarps][3 * kFuseVerts]; // x, y, z' of each vertex
-    __shared__ uint8_t s_yes[kGeomWarps][kFuseVerts];
-    __shared__ uint8_t s_dec[kGeomWarps][kGeomPrims][kFuseTris]; // 0 none, 1 walk list, 2 clip list, 3 no pixel
-    __shared__ uint32_t s_cnt[kGeomWarps][2];
-    __shared__ float s_m[kGeomWarps][24]; // view and projection rows 0-2 of the warp's item
+    extern __shared__ __align__(16) unsigned char geom_smem[];
+    GeomShared &S = *reinterpret_cast<GeomShared *>(geom_smem);
     const int warp = threadIdx.x >> 5;
     const uint32_t lane = threadIdx.x & 31;
-    float *pos = s_pos[warp];
-    uint8_t *sy = s_yes[warp];
-    float *m = s_m[warp];
-    int cur = -1;              // item whose matrices and pointers are loaded
-    uint32_t p_lo = 0, p_hi = 0; // its primitives
-    const float4 *wpos = nullptr;
-    float4 *ndc = nullptr;
-    const uint4 *tris = nullptr;
-    const PrimDesc *prims = nullptr;
-    const MatDesc *mats = nullptr;
-    int n_mats = 0;
-    float vm00 = 0.0f, vm03 = 0.0f, vm11 = 0.0f, vm13 = 0.0f;
-    uint32_t tri_lo = 0;
-    int acc_item = -1; // triangles counted as drawn here, per item (warp-uniform)
-    unsigned long long acc_n = 0;
-    const uint32_t total = b->total_prims;
-    const uint32_t step = gridDim.x * (kGeomWarps * kGeomPrims);
-    // every warp of the block runs the same iterations (barriers inside)
-    for (uint32_t p0 = blockIdx.x * (kGeomWarps * kGeomPrims); p0 < total; p0 += step) {
-        uint32_t c0 = 0, c1 = 0;
-        int items[kGeomPrims];
-        uint32_t first[kGeomPrims], count[kGeomPrims], tlo[kGeomPrims];
+    const unsigned below = (1u << lane) - 1u;
+    float *pos = S.pos[warp];
+    uint8_t *sy = S.yes[warp];
+    uint32_t *stri = S.tri[warp];
+    int g = -1;
+    uint32_t c_lo = 0, c_hi = 0;
+    const uint32_t total = b->total_chunks;
+    // chunks: the block's index first, then from a shared counter; every
+    // thread of the block runs the same iterations (barriers inside)
+    if (threadIdx.x == 0)
+        S.next = blockIdx.x;
+    for (;;) {
+        __syncthreads();
+        const uint32_t c = S.next;
+        if (c >= total)
+            break;
+        __syncthreads(); // every thread has read S.next
+        if (threadIdx.x == 0)
+            S.next = gridDim.x + atomicAdd(counter32(b, C_GEOM_Q), 1u);
+        if (c < c_lo || c >= c_hi) {
+            g = find_item(b->grp_chunk_base, b->n_groups, c);
+            c_lo = __ldg(b->grp_chunk_base + g);
+            c_hi = __ldg(b->grp_chunk_base + g + 1);
+        }
+        const uint32_t i_lo = __ldg(b->grp_item_base + g), i_hi = __ldg(b->grp_item_base + g + 1);
+        const SceneDev &sc = b->items[__ldg(b->grp_items + i_lo)].s; // vertex data shared by the group
+        const uint32_t q = (c - c_lo) * kGeomWarps + warp;             // this warp's primitive
+        const bool has = q < sc.n_prims;
+        uint4 gq = make_uint4(0u, 0u, 0u, 0u); // first vertex, vertex count, first triangle, triangle count
+        bool ds = false;
+        float wx[kGeomVPL], wy[kGeomVPL], wz[kGeomVPL];
+        __syncwarp(); // the previous chunk's reads of stri are done
+        if (has) {
+            gq = sc.pgeo[q];
+            gq.y = min(gq.y, kFuseVerts); // (a fused scene's primitives are within both limits)
+            gq.w = min(gq.w, kFuseTris);
+            const float4 *wpos = sc.wpos + gq.x;
 #pragma unroll
-        for (int u = 0; u < kGeomPrims; u++) {
-            const uint32_t p = p0 + warp * kGeomPrims + u;
-            items[u] = -1;
-            first[u] = count[u] = tlo[u] = 0;
-            if (p >= total)
-                continue;
-            if (p < p_lo || p >= p_hi) {
-                const int item = find_item(b->prim_base, b->n_items, p);
-                p_lo = __ldg(b->prim_base + item);
-                p_hi = __ldg(b->prim_base + item + 1);
-                if (item != cur) {
-                    const ItemDev &it = b->items[item];
-                    __syncwarp();
-                    if (lane < 12) {
-                        m[lane] = it.v.view[lane];
-                        m[12 + lane] = it.v.proj[lane];
+            for (int k = 0; k < kGeomVPL; k++) {
+                wx[k] = wy[k] = wz[k] = 0.0f;
+                if (lane + 32 * k < gq.y) {
+                    const float4 w = wpos[lane + 32 * k];
+                    wx[k] = w.x;
+                    wy[k] = w.y;
+                    wz[k] = w.z;
+                }
+            }
+            for (uint32_t t = lane; t < gq.w; t += 32) {
+                const uint4 tri = sc.tris[gq.z + t];
+                stri[t] = (tri.x - gq.x) | ((tri.y - gq.x) << 8) | ((tri.z - gq.x) << 16);
+            }
+            ds = sc.pshade[q].double_sided != 0;
+        }
+        for (uint32_t v0 = i_lo; v0 < i_hi; v0 += kGeomPass) {
+            const int nv = (int)min((uint32_t)kGeomPass, i_hi - v0);
+            __syncthreads(); // the previous pass is done with the view data and the counts
+            if (warp < nv) { // warp vi loads item vi's view
+                const uint32_t item = __ldg(b->grp_items + v0 + warp);
+                const ItemDev &it = b->items[item];
+                if (lane < 12) {
+                    S.m[warp][lane] = it.v.view[lane];
+                    S.m[warp][12 + lane] = it.v.proj[lane];
+                } else if (lane == 12) {
+                    S.vm[warp][0] = it.v.vm00;
+                    S.vm[warp][1] = it.v.vm03;
+                    S.vm[warp][2] = it.v.vm11;
+                    S.vm[warp][3] = it.v.vm13;
+                } else if (lane == 13) {
+                    S.ndc[warp] = it.ndc;
+                    S.item[warp] = item;
+                    S.tri_lo[warp] = __ldg(b->tri_base + item);
+                }
+            }
+            __syncthreads();
+            for (int vi = 0; vi < nv; vi++) {
+                uint32_t c0 = 0, c1 = 0, nx = 0;
+                if (has) {
+                    const float *m = S.m[vi];
+                    float4 *ndc = S.ndc[vi] + gq.x;
+                    __syncwarp(); // the previous item's reads of pos and sy are done
+                    // world_to_camera_or_frustum (vertex_shaders.hpp:35-52), as k_vertex
+#pragma unroll
+                    for (int k = 0; k < kGeomVPL; k++) {
+                        const uint32_t i = lane + 32 * k;
+                        if (i < gq.y) {
+                            V3 v = transform3(mk3(wx[k], wy[k], wz[k]), m);
+                            v = transform3(v, m + 12);
+                            if (v.z != 0.0f) {
+                                v.x = v.x / fabsf(v.z);
+                                v.y = v.y / fabsf(v.z);
+                            }
+                            ndc[i] = make_float4(v.x, v.y, v.z, 0.0f);
+                            pos[3 * i] = v.x;
+                            pos[3 * i + 1] = v.y;
+                            pos[3 * i + 2] = v.z;
+                            sy[i] = below_near(v.z) ? kYesBehind : 0;
+                        }
                     }
                     __syncwarp();
-                    wpos = it.s.wpos;
-                    ndc = it.ndc;
-                    tris = it.s.tris;
-                    prims = it.s.prims;
-                    mats = it.s.mats;
-                    n_mats = it.s.n_mats;
-                    vm00 = it.v.vm00;
-                    vm03 = it.v.vm03;
-                    vm11 = it.v.vm11;
-                    vm13 = it.v.vm13;
-                    tri_lo = __ldg(b->tri_base + item);
-                    cur = item;
-                }
-            }
-            const uint32_t q = p - p_lo;
-            uint4 gq = b->items[cur].s.pgeo[q]; // first vertex, vertex count, first triangle, triangle count
-            gq.y = min(gq.y, kFuseVerts);     // (a fused scene's primitives are within both limits)
-            gq.w = min(gq.w, kFuseTris);
-            items[u] = cur;
-            first[u] = gq.z;
-            count[u] = gq.w;
-            tlo[u] = tri_lo;
-            uint8_t *dec = s_dec[warp][u];
-            // the first 64 triangles are loaded before the vertices, so that both
-            // loads are in flight together, and kept for both passes
-            uint4 tr[2];
-#pragma unroll
-            for (int k = 0; k < 2; k++)
-                if (lane + 32 * k < gq.w)
-                    tr[k] = tris[gq.z + lane + 32 * k];
-            __syncwarp(); // the previous primitive's reads of pos and sy are done
-            // world_to_camera_or_frustum (vertex_shaders.hpp:35-52), as k_vertex
-            for (uint32_t i = lane; i < gq.y; i += 32) {
-                const float4 w = wpos[gq.x + i];
-                V3 v = transform3(mk3(w.x, w.y, w.z), m);
-                v = transform3(v, m + 12);
-                if (v.z != 0.0f) {
-                    v.x = v.x / fabsf(v.z);
-                    v.y = v.y / fabsf(v.z);
-                }
-                ndc[gq.x + i] = make_float4(v.x, v.y, v.z, 0.0f);
-                pos[3 * i] = v.x;
-                pos[3 * i + 1] = v.y;
-                pos[3 * i + 2] = v.z;
-                sy[i] = below_near(v.z) ? kYesBehind : 0;
-            }
-            __syncwarp();
-            // visibility flags (renderer.cpp:86-185), as k_flags; every store
-            // to a vertex writes the same value
-            const int mat = prims[q].material;
-            const bool ds = mat >= 0 && mat < n_mats && mats[mat].double_sided;
-            for (uint32_t t = lane; t < gq.w; t += 32) {
-                const uint4 tri = t < 32 ? tr[0] : (t < 64 ? tr[1] : tris[gq.z + t]);
-                const uint32_t ia = tri.x - gq.x, ib = tri.y - gq.x, ic = tri.z - gq.x;
-                const V3 a = mk3(pos[3 * ia], pos[3 * ia + 1], pos[3 * ia + 2]);
-                const V3 c1v = mk3(pos[3 * ib], pos[3 * ib + 1], pos[3 * ib + 2]);
-                const V3 c2v = mk3(pos[3 * ic], pos[3 * ic + 1], pos[3 * ic + 2]);
-                if (inside_frustum(a, c1v, c2v) && (ds || cross_n_z(sub3(c1v, a), sub3(c2v, a)) > 0.0f)) {
-                    sy[ia] = kYesDrawn | (below_near(a.z) ? kYesBehind : 0);
-                    sy[ib] = kYesDrawn | (below_near(c1v.z) ? kYesBehind : 0);
-                    sy[ic] = kYesDrawn | (below_near(c2v.z) ? kYesBehind : 0);
-                }
-            }
-            __syncwarp();
-            // the compaction's decisions, as k_compact
-            uint32_t nx = 0;
-            for (uint32_t t = lane; t < gq.w; t += 32) {
-                const uint4 tri = t < 32 ? tr[0] : (t < 64 ? tr[1] : tris[gq.z + t]);
-                const uint32_t ia = tri.x - gq.x, ib = tri.y - gq.x, ic = tri.z - gq.x;
-                const uint32_t ya = sy[ia], yb = sy[ib], yc = sy[ic];
-                uint8_t d = 0;
-                if (ya & yb & yc & kYesDrawn) {
-                    if ((ya | yb | yc) & kYesBehind) {
-                        d = 2;
-                    } else {
-                        d = 1;
-                        const float y0 = vm11 * pos[3 * ia + 1] + vm13;
-                        const float y1 = vm11 * pos[3 * ib + 1] + vm13;
-                        const float y2 = vm11 * pos[3 * ic + 1] + vm13;
-                        const float lo_y = fminf(y0, fminf(y1, y2)), hi_y = fmaxf(y0, fmaxf(y1, y2));
-                        if (y0 == y0 && y1 == y1 && y2 == y2) {
-                            if (f2i(ceilf(lo_y)) == f2i(ceilf(hi_y))) {
-                                d = 0; // no row
-                            } else {
-                                const float x0 = vm00 * pos[3 * ia] + vm03;
-                                const float x1 = vm00 * pos[3 * ib] + vm03;
-                                const float x2 = vm00 * pos[3 * ic] + vm03;
-                                const float mx = fmaxf(fabsf(x0), fmaxf(fabsf(x1), fabsf(x2)));
-                                const float rows = ceilf(hi_y) - ceilf(lo_y);
-                                const float eps = (rows + 32.0f) * 0x1p-23f * (mx + 1.0f);
-                                const float lo_x = fminf(x0, fminf(x1, x2)) - eps;
-                                const float hi_x = fmaxf(x0, fmaxf(x1, x2)) + eps;
-                                if (ceilf(lo_x) == ceilf(hi_x)) {
-                                    d = 3; // no pixel column
-                                    if (b->slot_flags)
-                                        b->slot_flags[2 * (gq.z + t)] = 1;
+                    // visibility flags (renderer.cpp:86-185), as k_flags; every
+                    // store to a vertex writes the same value
+                    for (uint32_t t = lane; t < gq.w; t += 32) {
+                        const uint32_t tp = stri[t];
+                        const uint32_t ia = tp & 0xFFu, ib = (tp >> 8) & 0xFFu, ic = tp >> 16;
+                        const V3 a = mk3(pos[3 * ia], pos[3 * ia + 1], pos[3 * ia + 2]);
+                        const V3 c1v = mk3(pos[3 * ib], pos[3 * ib + 1], pos[3 * ib + 2]);
+                        const V3 c2v = mk3(pos[3 * ic], pos[3 * ic + 1], pos[3 * ic + 2]);
+                        if (inside_frustum(a, c1v, c2v) && (ds || cross_n_z(sub3(c1v, a), sub3(c2v, a)) > 0.0f)) {
+                            sy[ia] = kYesDrawn | (below_near(a.z) ? kYesBehind : 0);
+                            sy[ib] = kYesDrawn | (below_near(c1v.z) ? kYesBehind : 0);
+                            sy[ic] = kYesDrawn | (below_near(c2v.z) ? kYesBehind : 0);
+                        }
+                    }
+                    __syncwarp();
+                    // the compaction's decisions, as k_compact
+                    const float vm00 = S.vm[vi][0], vm03 = S.vm[vi][1], vm11 = S.vm[vi][2], vm13 = S.vm[vi][3];
+                    for (uint32_t t0 = 0; t0 < gq.w; t0 += 32) {
+                        const uint32_t t = t0 + lane;
+                        int d = 0; // 0 none, 1 walk list, 2 clip list, 3 no pixel column
+                        if (t < gq.w) {
+                            const uint32_t tp = stri[t];
+                            const uint32_t ia = tp & 0xFFu, ib = (tp >> 8) & 0xFFu, ic = tp >> 16;
+                            const uint32_t ya = sy[ia], yb = sy[ib], yc = sy[ic];
+                            if (ya & yb & yc & kYesDrawn) {
+                                if ((ya | yb | yc) & kYesBehind) {
+                                    d = 2;
+                                } else {
+                                    d = 1;
+                                    const float y0 = vm11 * pos[3 * ia + 1] + vm13;
+                                    const float y1 = vm11 * pos[3 * ib + 1] + vm13;
+                                    const float y2 = vm11 * pos[3 * ic + 1] + vm13;
+                                    const float lo_y = fminf(y0, fminf(y1, y2)), hi_y = fmaxf(y0, fmaxf(y1, y2));
+                                    if (y0 == y0 && y1 == y1 && y2 == y2) {
+                                        if (f2i(ceilf(lo_y)) == f2i(ceilf(hi_y))) {
+                                            d = 0; // no row
+                                        } else {
+                                            const float x0 = vm00 * pos[3 * ia] + vm03;
+                                            const float x1 = vm00 * pos[3 * ib] + vm03;
+                                            const float x2 = vm00 * pos[3 * ic] + vm03;
+                                            const float mx = fmaxf(fabsf(x0), fmaxf(fabsf(x1), fabsf(x2)));
+                                            const float rows = ceilf(hi_y) - ceilf(lo_y);
+                                            const float eps = (rows + 32.0f) * 0x1p-23f * (mx + 1.0f);
+                                            const float lo_x = fminf(x0, fminf(x1, x2)) - eps;
+                                            const float hi_x = fmaxf(x0, fmaxf(x1, x2)) + eps;
+                                            if (ceilf(lo_x) == ceilf(hi_x)) {
+                                                d = 3; // no pixel column
+                                                if (b->slot_flags)
+                                                    b->slot_flags[2 * (gq.z + t)] = 1;
+                                            }
+                                        }
+                                    }
                                 }
                             }
                         }
+                        const unsigned m1 = __ballot_sync(0xFFFFFFFFu, d == 1);
+                        const unsigned m2 = __ballot_sync(0xFFFFFFFFu, d == 2);
+                        const unsigned m3 = __ballot_sync(0xFFFFFFFFu, d == 3);
+                        if (lane == 0) {
+                            S.walk[vi][warp][t0 >> 5] = m1;
+                            S.clip[vi][warp][t0 >> 5] = m2;
+                        }
+                        c0 += __popc(m1);
+                        c1 += __popc(m2);
+                        nx += __popc(m3);
                     }
                 }
-                dec[t] = d;
-                c0 += d == 1;
-                c1 += d == 2;
-                nx += d == 3;
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                nx += __shfl_xor_sync(0xFFFFFFFFu, nx, o);
-            if (nx) {
-                if (cur != acc_item) {
-                    if (acc_item >= 0 && lane == 0)
-                        atomicAdd(b->item_counters + 2 * (size_t)acc_item, acc_n);
-                    acc_item = cur;
-                    acc_n = 0;
+                if (lane == 0) {
+                    S.cnt[vi][warp][0] = c0;
+                    S.cnt[vi][warp][1] = c1;
+                    S.nx[vi][warp] = nx;
                 }
-                acc_n += nx;
             }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            c0 += __shfl_xor_sync(0xFFFFFFFFu, c0, o);
-            c1 += __shfl_xor_sync(0xFFFFFFFFu, c1, o);
-        }
-        if (lane == 0) {
-            s_cnt[warp][0] = c0;
-            s_cnt[warp][1] = c1;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t n0 = 0, n1 = 0;
-            for (int w = 0; w < kGeomWarps; w++) {
-                const uint32_t a0 = s_cnt[w][0], a1 = s_cnt[w][1];
-                s_cnt[w][0] = n0;
-                s_cnt[w][1] = n1;
-                n0 += a0;
-                n1 += a1;
-            }
-            const unsigned long long old = reserve_lists(b, n0, n1);
-            const uint32_t g0 = (uint32_t)old, g1 = (uint32_t)(old >> 32);
-            for (int w = 0; w < kGeomWarps; w++) {
-                s_cnt[w][0] += g0;
-                s_cnt[w][1] += g1;
-            }
-        }
-        __syncthreads();
-        uint32_t o0 = s_cnt[warp][0], o1 = s_cnt[warp][1];
-        const unsigned below = (1u << lane) - 1u;
-#pragma unroll
-        for (int u = 0; u < kGeomPrims; u++) {
-            if (items[u] < 0)
-                continue;
-            const uint8_t *dec = s_dec[warp][u];
-            for (uint32_t t0 = 0; t0 < count[u]; t0 += 32) {
-                const uint32_t t = t0 + lane;
-                const uint8_t d = t < count[u] ? dec[t] : 0;
-                const unsigned m1 = __ballot_sync(0xFFFFFFFFu, d == 1), m2 = __ballot_sync(0xFFFFFFFFu, d == 2);
-                if (d == 1) {
-                    const uint32_t j = o0 + __popc(m1 & below);
-                    if (j < b->list_cap)
-                        b->list[j] = make_uint2(first[u] + t, (uint32_t)items[u]);
-                } else if (d == 2) {
-                    const uint32_t j = o1 + __popc(m2 & below);
-                    if (j < b->clip_cap)
-                        b->clip[b->clip_cap - 1 - j] = make_uint2(first[u] + t, (uint32_t)items[u]); // from the end
-                    b->recmap[tlo[u] + first[u] + t] = kRecClip;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                // first positions per item and warp, one reservation for the pass
+                uint32_t n0 = 0, n1 = 0;
+                for (int vi = 0; vi < nv; vi++) {
+                    uint32_t x = 0;
+                    for (int w = 0; w < kGeomWarps; w++) {
+                        const uint32_t a0 = S.cnt[vi][w][0], a1 = S.cnt[vi][w][1];
+                        S.cnt[vi][w][0] = n0;
+                        S.cnt[vi][w][1] = n1;
+                        n0 += a0;
+                        n1 += a1;
+                        x += S.nx[vi][w];
+                    }
+                    // triangles counted as drawn here: they reached fill_triangle_2's set-up
+                    if (x)
+                        atomicAdd(b->item_counters + 2 * (size_t)S.item[vi], (unsigned long long)x);
                 }
-                o0 += __popc(m1);
-                o1 += __popc(m2);
+                const unsigned long long old = reserve_lists(b, n0, n1);
+                const uint32_t g0 = (uint32_t)old, g1 = (uint32_t)(old >> 32);
+                for (int vi = 0; vi < nv; vi++)
+                    for (int w = 0; w < kGeomWarps; w++) {
+                        S.cnt[vi][w][0] += g0;
+                        S.cnt[vi][w][1] += g1;
+                    }
+            }
+            __syncthreads();
+            if (has) {
+                for (int vi = 0; vi < nv; vi++) {
+                    uint32_t o0 = S.cnt[vi][warp][0], o1 = S.cnt[vi][warp][1];
+                    const uint32_t item = S.item[vi], tlo = S.tri_lo[vi];
+                    for (uint32_t t0 = 0; t0 < gq.w; t0 += 32) {
+                        const unsigned m1 = S.walk[vi][warp][t0 >> 5], m2 = S.clip[vi][warp][t0 >> 5];
+                        const uint32_t t = t0 + lane;
+                        if ((m1 >> lane) & 1u) {
+                            const uint32_t j = o0 + __popc(m1 & below);
+                            if (j < b->list_cap)
+                                b->list[j] = make_uint2(tlo + gq.z + t, item);
+                        } else if ((m2 >> lane) & 1u) {
+                            const uint32_t j = o1 + __popc(m2 & below);
+                            if (j < b->clip_cap)
+                                b->clip[b->clip_cap - 1 - j] = make_uint2(gq.z + t, item); // from the end
+                            mark_clip(b, tlo + gq.z + t);
+                        }
+                        o0 += __popc(m1);
+                        o1 += __popc(m2);
+                    }
+                }
             }
         }
-        __syncthreads(); // s_cnt is rewritten by the next iteration
     }
-    if (acc_item >= 0 && lane == 0)
-        atomicAdd(b->item_counters + 2 * (size_t)acc_item, acc_n);
 }
 
 // ------------------------------------------------------------ triangle walk --
@@ -845,11 +887,6 @@ __device__ __forceinline__ void span_pixels(int x1, int x2, const Side &Ls, cons
 __device__ __forceinline__ unsigned long long make_key(float z, uint32_t slot)
 {
     return ((unsigned long long)__float_as_uint(z) << 32) | slot;
-}
-
-__device__ __forceinline__ uint32_t *counter32(const BatchDev *b, int w)
-{
-    return reinterpret_cast<uint32_t *>(b->counters) + w;
 }
 
 // Bin a long span: the qpixel state after its displacement to x1.
@@ -1186,12 +1223,13 @@ __device__ __forceinline__ void smem_row_in(RowIn &r, const WalkRow *S, int o, i
 
 // Set-up of triangle t of `item` (list entry i): fill_triangle's z sort
 // (renderer.cpp:264-279), fill_triangle_2's y sort, edges and halves
-// (:375-460), into the TriRec of the entry.  Returns whether the triangle
-// reached scanline set-up (y0 != y2); the record of one that did not has no
-// rows.
-__device__ __forceinline__ bool tri_setup(const BatchDev *b, uint32_t i, uint32_t t, uint32_t item, bool &tall)
+// (:375-460), into the TriRec of batch triangle r (t = r - tri_base[item]).
+// Returns whether the triangle reached scanline set-up (y0 != y2); the record
+// of one that did not has no rows.
+__device__ __forceinline__ bool tri_setup(const BatchDev *b, uint32_t r, uint32_t item, bool &tall)
 {
     tall = false;
+    const uint32_t t = r - __ldg(b->tri_base + item);
     const ItemDev &it = b->items[item];
     const ViewDev &v = it.v;
     const uint4 tri = it.s.tris[t];
@@ -1202,7 +1240,7 @@ __device__ __forceinline__ bool tri_setup(const BatchDev *b, uint32_t i, uint32_
     sort_y_asc(a, c1, c2, pa, pb, pc);
     const V3 v0 = a, v1 = c1, v2 = c2;
     const int y0 = f2i(ceilf(v0.y)), y1 = f2i(ceilf(v1.y)), y2 = f2i(ceilf(v2.y));
-    float4 *dst = reinterpret_cast<float4 *>(b->recs + i);
+    float4 *dst = reinterpret_cast<float4 *>(b->recs + r);
     if (y0 == y2) {
         // no rows: n_u = n_d = 0
         dst[5] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0));
@@ -1259,7 +1297,6 @@ __device__ __forceinline__ bool tri_setup(const BatchDev *b, uint32_t i, uint32_
     dst[5] = make_float4(v2.z, __int_as_float(ys), __int_as_float(y_l), __int_as_float(n_u));
     dst[6] = make_float4(__int_as_float(n_d), __uint_as_float(flags), __uint_as_float(slot), __uint_as_float(item));
     dst[7] = make_float4(__uint_as_float(g0), __uint_as_float(g1), __uint_as_float(g2), __uint_as_float(tri.w));
-    b->recmap[__ldg(b->tri_base + item) + t] = i;
     return true;
 }
 
@@ -1274,11 +1311,12 @@ __global__ void __launch_bounds__(256) k_setup(const BatchDev *b)
     for (uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; i0 < n; i0 += stride) {
         const uint32_t i = i0 + (threadIdx.x & 31);
         bool drawn = false, tall = false;
-        uint32_t item = 0;
+        uint32_t item = 0, r = 0;
         if (i < n) {
             const uint2 e = b->list[i];
+            r = e.x;
             item = e.y;
-            drawn = tri_setup(b, i, e.x, item, tall);
+            drawn = tri_setup(b, r, item, tall);
         }
         // tall triangles are walked by a whole warp each, in k_walk_rare
         const unsigned tm = __ballot_sync(0xFFFFFFFFu, tall);
@@ -1289,7 +1327,7 @@ __global__ void __launch_bounds__(256) k_setup(const BatchDev *b)
                 tb = atomicAdd(counter32(b, C_TALL), (uint32_t)__popc(tm));
             tb = __shfl_sync(0xFFFFFFFFu, tb, leader);
             if (tall)
-                b->tall[tb + __popc(tm & ((1u << lane) - 1u))] = i;
+                b->tall[tb + __popc(tm & ((1u << lane) - 1u))] = r;
         }
         acc.add(b, item, drawn ? 1ull : 0ull, 0ull, i < n);
     }
@@ -1416,9 +1454,9 @@ __device__ __noinline__ void walk_tall_all(const BatchDev *b, ItemAcc &acc);
 
 // Depth walk of the drawable triangles wholly in front of the near plane
 // (fill_triangle's normal case, renderer.cpp:281-285: one sub-triangle, slot
-// 2t).  Each warp takes groups of 32 list entries (warp-strided), loads their
-// set-ups into shared memory (one 128-byte record per load) and deals their
-// rows across its lanes.  FRAGS: the fragment capture of a layered view (the
+// 2t).  Each warp takes groups of 32 list entries (from work queues), loads
+// their set-ups into shared memory (one 128-byte record per load) and deals
+// their rows across its lanes.  FRAGS: the fragment capture of a layered view (the
 // near-clipped triangles are captured by k_frags).
 template <bool FRAGS>
 __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(const BatchDev *b)
@@ -1428,14 +1466,21 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
     const uint32_t n_raw = *counter32(b, C_LIST);
     const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
     const uint32_t n_groups = (n + 31) / 32;
+    // the record (batch triangle) of entry `lane` of group g; loaded one
+    // group ahead of its fetch, so that the copies do not wait for it
+    auto rec_of = [&](uint32_t g) -> uint32_t {
+        const uint32_t i = 32 * g + (uint32_t)lane;
+        return g < n_groups && i < n ? b->list[i].x : 0u;
+    };
     // record j of group g -> word `lane` of field row `lane`, column j
-    auto fetch = [&](uint32_t g, WalkRow *D) {
+    auto fetch = [&](uint32_t g, uint32_t rec, WalkRow *D) {
         if (g < n_groups) {
             const uint32_t base = 32 * g, cnt = n - base < 32u ? n - base : 32u;
-            const uint32_t *src = reinterpret_cast<const uint32_t *>(b->recs + base) + lane;
 #pragma unroll 8
-            for (uint32_t j = 0; j < cnt; j++)
-                cp_async4(&D[lane][j], src + 32 * j);
+            for (uint32_t j = 0; j < cnt; j++) {
+                const uint32_t rj = __shfl_sync(0xFFFFFFFFu, rec, j);
+                cp_async4(&D[lane][j], reinterpret_cast<const uint32_t *>(b->recs + rj) + lane);
+            }
         }
         cp_async_commit();
     };
@@ -1443,16 +1488,26 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
     WalkView view;
     view.item = 0xFFFFFFFFu;
     view.inline_span = b->inline_span;
-    // Warps take groups g, g + W, g + 2W, ... (W warps in the grid; a shared
-    // counter costs more in contention than it saves in balance).  While
-    // group g is walked, the records of the next one are copied in.
-    const uint32_t W = (gridDim.x * blockDim.x) >> 5;
-    uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t g_next = g + W;
+    // Groups come from kQueues queues (queue q holds groups q, q + kQueues,
+    // ...; warp w draws from queue w % kQueues).  While group g is walked, the
+    // records of the next one are copied in, the list entries of the one
+    // after are loaded, and the index of the one after that is drawn, so that
+    // neither the draw's round trip nor the entries' load holds up a copy.
+    const uint32_t wq = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % kQueues;
+    uint32_t *qc = counter32(b, C_WALK_Q + 32 * (int)wq);
+    auto draw = [&]() -> uint32_t { return lane == 0 ? atomicAdd(qc, 1u) : 0u; }; // lane 0 holds the draw
+    auto group_of = [&](uint32_t d) -> uint32_t { return wq + kQueues * __shfl_sync(0xFFFFFFFFu, d, 0); };
+    const uint32_t d0 = draw(), d1 = draw();
+    uint32_t g = group_of(d0), g_next = group_of(d1);
+    uint32_t d_after = draw();
     int buf = 0;
-    fetch(g, sm[threadIdx.x >> 5][0]);
+    fetch(g, rec_of(g), sm[threadIdx.x >> 5][0]);
+    uint32_t rec_next = rec_of(g_next);
     while (g < n_groups) {
-        fetch(g_next, sm[threadIdx.x >> 5][buf ^ 1]);
+        fetch(g_next, rec_next, sm[threadIdx.x >> 5][buf ^ 1]);
+        const uint32_t g_after = group_of(d_after);
+        rec_next = rec_of(g_after);
+        d_after = g_after < n_groups ? draw() : 0xFFFFFFFFu / kQueues; // (past the end: no more draws)
         cp_async_wait<1>(); // this group's copies are done
         WalkRow *S = sm[threadIdx.x >> 5][buf];
         const uint32_t base = 32 * g;
@@ -1495,7 +1550,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
         acc.add(b, valid ? S[F_ITEM][lane] : 0u, 0ull, valid ? (unsigned long long)S[F_FRAGS][lane] : 0ull, valid);
         __syncwarp();
         g = g_next;
-        g_next = g + W;
+        g_next = g_after;
         buf ^= 1;
     }
     cp_async_wait<0>();
@@ -1677,8 +1732,9 @@ __device__ __noinline__ void winner_overflow(const BatchDev *b)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint2 e = b->list[i];
         const ItemDev &it = b->items[e.y];
-        WinnerVisitor vis{&it, 2 * e.x, b->inline_span, true};
-        const uint4 tri = it.s.tris[e.x];
+        const uint32_t t = e.x - __ldg(b->tri_base + e.y);
+        WinnerVisitor vis{&it, 2 * t, b->inline_span, true};
+        const uint4 tri = it.s.tris[t];
         V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
         int pa = 0, pb = 1, pc = 2;
         sort_z_desc(a, c1, c2, pa, pb, pc);
@@ -1750,19 +1806,13 @@ __global__ void __launch_bounds__(256) k_spans(const BatchDev *b) { spans_pass(b
 
 __device__ __forceinline__ void bind_material(const SceneDev &s, uint32_t prim, Shader &sh)
 {
-    const PrimDesc pd = s.prims[prim];
-    const MatDesc m = (pd.material >= 0 && pd.material < s.n_mats) ? s.mats[pd.material] : s.default_mat;
-    sh.shininess = m.shininess;
-    sh.color = m.color;
-    if (m.texture < 0 || m.texture >= s.n_texs) {
-        sh.tex = nullptr;
-        sh.tw = sh.th = 1;
-    } else {
-        const TexDesc td = s.texs[m.texture];
-        sh.tex = td.texels;
-        sh.tw = td.w;
-        sh.th = td.h;
-    }
+    const uint4 *p = reinterpret_cast<const uint4 *>(s.pshade + prim); // PrimShade: one 32-byte load
+    const uint4 a = p[0], c = p[1];
+    sh.tex = reinterpret_cast<const uint32_t *>((unsigned long long)a.x | ((unsigned long long)a.y << 32));
+    sh.tw = (int)a.z;
+    sh.th = (int)a.w;
+    sh.color = c.x;
+    sh.shininess = (int)c.y;
 }
 
 // prepare_for_upper/lower_triangle, prepare_for_scanline and shade for the
@@ -1860,13 +1910,12 @@ __device__ __forceinline__ uint32_t shade_winner_impl(const BatchDev *b, uint32_
 {
     const ItemDev &it = b->items[item];
     const ViewDev &v = it.v;
-    const uint32_t ri = b->recmap[__ldg(b->tri_base + item) + (slot >> 1)];
-    if (ri == kRecClip)
-        return shade_clip_px(it, i, slot);
-    const TriRec *rp = b->recs + ri;
+    const TriRec *rp = b->recs + __ldg(b->tri_base + item) + (slot >> 1);
     const uint4 q6 = reinterpret_cast<const uint4 *>(rp)[6];
     const uint4 q7 = reinterpret_cast<const uint4 *>(rp)[7];
     const uint32_t flags = q6.y;
+    if (flags == kRecClip)
+        return shade_clip_px(it, i, slot);
     const int y = (int)(i / (uint32_t)v.w), x = (int)(i - (uint32_t)y * (uint32_t)v.w);
     float4 rec;
     if (overflow || (flags & kRecTall) || !rec_replay(rp, v, b->inline_span, x + v.x, y + v.y, rec))
@@ -2060,20 +2109,43 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
             c0 = c0 < 0 ? 0 : (c0 >= w ? w - 1 : c0);
             c1 = c1 < 0 ? 0 : (c1 >= w ? w - 1 : c1);
             c2 = c2 < 0 ? 0 : (c2 >= w ? w - 1 : c2);
+            // the staged pixels' common value, if they all have one
+            const uint32_t ref = __ldg(it.pixels + (size_t)y0 * it.pitch_px + x0);
+            bool same = true;
 #pragma unroll 4
             for (int yy = warp; yy < S; yy += 8) {
                 int sy = y0 - R + yy;
                 sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
                 const uint32_t *row = it.pixels + (size_t)sy * it.pitch_px;
                 uint32_t *dst = halo + yy * S;
-                if (lane < S)
-                    dst[lane] = __ldg(row + c0);
-                if (lane + 32 < S)
-                    dst[lane + 32] = __ldg(row + c1);
-                if (lane + 64 < S)
-                    dst[lane + 64] = __ldg(row + c2);
+                if (lane < S) {
+                    const uint32_t v = __ldg(row + c0);
+                    dst[lane] = v;
+                    same &= v == ref;
+                }
+                if (lane + 32 < S) {
+                    const uint32_t v = __ldg(row + c1);
+                    dst[lane + 32] = v;
+                    same &= v == ref;
+                }
+                if (lane + 64 < S) {
+                    const uint32_t v = __ldg(row + c2);
+                    dst[lane + 64] = v;
+                    same &= v == ref;
+                }
             }
-            __syncthreads();
+            if (__syncthreads_and(same)) {
+                // Every tap of every pixel of the tile reads the value ref:
+                // 32 equal channels c sum to 32 c, and (32 c + 16) / 32 = c,
+                // alpha is the centre's: the gather leaves ref unchanged.
+                for (int p = threadIdx.x; p < kDofTile * kDofTile; p += blockDim.x) {
+                    const int x = x0 + (p & (kDofTile - 1)), y = y0 + p / kDofTile;
+                    if (x < w && y < h)
+                        it.dof_out[(size_t)y * it.dof_pitch + x] = ref;
+                }
+                __syncthreads(); // the halo is reused by the next tile
+                continue;
+            }
         }
         for (int p = threadIdx.x; p < kDofTile * kDofTile; p += blockDim.x) {
             // a warp takes one row of 32 pixels of the tile
@@ -2365,11 +2437,11 @@ template <bool ALL_MODES>
 __device__ __forceinline__ uint32_t shade_frag(const BatchDev *b, const ItemDev &it, uint32_t item, uint32_t slot,
                                                float4 rec)
 {
-    const uint32_t ri = b->recmap[__ldg(b->tri_base + item) + (slot >> 1)];
-    if (ri == kRecClip)
+    const uint4 *q = reinterpret_cast<const uint4 *>(b->recs + __ldg(b->tri_base + item) + (slot >> 1));
+    const uint4 q6 = q[6];
+    if (q6.y == kRecClip)
         return shade_clip_rec(it, slot, rec);
-    const uint4 *q = reinterpret_cast<const uint4 *>(b->recs + ri);
-    return shade_rec<ALL_MODES>(it, q[7], q[6].y, rec);
+    return shade_rec<ALL_MODES>(it, q[7], q6.y, rec);
 }
 
 // One pixel with fragments: the opaque winner to the screen and the depth
@@ -2621,7 +2693,10 @@ cudaError_t init_device_constants()
     float2 taps[SGL_DOF_TAPS];
     for (int k = 0; k < SGL_DOF_TAPS; k++)
         taps[k] = make_float2(sgl_dof_taps[k][0], sgl_dof_taps[k][1]);
-    return cudaMemcpyToSymbol(c_dof_taps, taps, sizeof taps);
+    cudaError_t e = cudaMemcpyToSymbol(c_dof_taps, taps, sizeof taps);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_geom, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGeomSmem);
+    return e;
 }
 
 cudaError_t launch_dof(const BatchDev *b, cudaStream_t st)
@@ -2653,7 +2728,7 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
     int n = 0;
     mark(PK_GEOM);
     if (flags & kSeqFused) {
-        k_geom<<<sms * 8, kGeomWarps * 32, 0, st>>>(b);
+        k_geom<<<sms * 3, kGeomWarps * 32, kGeomSmem, st>>>(b);
         ran(PK_GEOM);
         n++;
     }

@@ -30,10 +30,29 @@ struct PrimDesc {
     int node;
 };
 
+// What the pixel shader binds for a primitive, resolved at upload
+// (pixel_shader_t::prepare_for_primitive, src/render/pixel_shaders.cpp:14-31,
+// 284-302): its material's colour, shininess and texture — or the scene's
+// default material when its index is out of range — and, for the visibility
+// flags, whether its material is double sided (renderer.cpp:135-150: false
+// for an out-of-range index).
+struct __align__(16) PrimShade {
+    const uint32_t *tex; // mip 0 texels, nullptr when untextured
+    int tw, th;          // 1 x 1 when untextured
+    uint32_t color;
+    int shininess;
+    int double_sided;
+    int pad;
+};
+static_assert(sizeof(PrimShade) == 32, "PrimShade layout");
+
 // Scenes whose every primitive has at most kFuseVerts vertices and
 // kFuseTris triangles take the fused geometry pass (one warp per primitive:
 // vertex transform, visibility flags and compaction in shared memory).
 constexpr uint32_t kFuseVerts = 256, kFuseTris = 512;
+// The fused geometry pass: a block takes kGeomWarps primitives of a group (one
+// warp each) and runs them for every item of the group.
+constexpr int kGeomWarps = 8;
 
 struct LightsDev {
     float ambient;
@@ -59,6 +78,7 @@ struct SceneDev {
     float4 *wnrm;            // normal_world
     float2 *uv;              // tex_coords
     const uint4 *pgeo;       // draw-order primitives: first vertex, vertex count, first triangle, triangle count
+    const PrimShade *pshade; // draw-order primitives: material and texture as the pixel shader binds them
     uint32_t n_vertices;
     uint32_t n_triangles;
     uint32_t n_prims;
@@ -183,16 +203,22 @@ constexpr uint32_t kRecLLRUpper = 1u; // long_line_on_right in the upper half
 constexpr uint32_t kRecLLRLower = 2u; // ... in the lower half
 constexpr uint32_t kRecFFV = 4u;      // front_face_visible
 constexpr uint32_t kRecTall = 8u;     // every span was binned (winners recorded in prec)
-constexpr uint32_t kRecClip = 0xFFFFFFFFu; // recmap entry of a near-clipped triangle
+// The flags word of the record slot of a near-clipped triangle (written by the
+// geometry passes; such a triangle gets no set-up record).
+constexpr uint32_t kRecClip = 0xFFFFFFFFu;
+constexpr int kRecFlagsWord = 25; // 32-bit word of TriRec::flags
+static_assert(offsetof(TriRec, flags) == 4 * kRecFlagsWord, "TriRec::flags word");
 
 // Batch counters (32-bit words); the drawn-triangle and fragment counts are
 // kept per item (item_counters) and summed by the host.
-enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_FRAGS = 8, C_TALL = 10 };
+enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_FRAGS = 8, C_TALL = 10, C_GEOM_Q = 11 };
 // Work queues of the shade kernel's tiles: kQueues counters, one per 128-byte
 // line so that blocks of different queues do not contend.
 constexpr int kQueues = 16;
 constexpr int C_SHADE_Q = 32;                       // 32-bit index of queue q: C_SHADE_Q + 32 q
-constexpr int kCounterWords = (C_SHADE_Q + 32 * kQueues) / 2; // 64-bit words
+// ... and of the walk kernel's groups of 32 walk-list entries
+constexpr int C_WALK_Q = C_SHADE_Q + 32 * kQueues;   // 32-bit index of queue q: C_WALK_Q + 32 q
+constexpr int kCounterWords = (C_WALK_Q + 32 * kQueues) / 2; // 64-bit words
 
 // A batch of views rendered by one launch sequence (lives in device memory).
 struct BatchDev {
@@ -201,21 +227,26 @@ struct BatchDev {
     const uint32_t *px_base;   // n_items + 1 prefix of pixel counts
     const uint32_t *tile_base; // n_items + 1 prefix of shade-tile counts
     const uint32_t *dof_base;  // n_items + 1 prefix of depth-of-field tile counts (0 for items without)
-    // the geometry passes: items of fused scenes by primitive (prim_base),
-    // the others by vertex and triangle (g_vtx_base, g_tri_base); each item
-    // counts in one of the two
-    const uint32_t *g_vtx_base, *g_tri_base, *prim_base;
-    uint32_t total_gvtx, total_gtri, total_prims;
+    // the geometry passes: items of fused scenes in groups that read the same
+    // vertex data (one scene, or one posed request's own world positions) —
+    // group g holds the items grp_items[grp_item_base[g] .. grp_item_base[g+1])
+    // and the chunks grp_chunk_base[g] .. grp_chunk_base[g+1] of kGeomWarps
+    // primitives each; the other items by vertex and triangle (g_vtx_base,
+    // g_tri_base).  Each item counts in one of the two.
+    const uint32_t *g_vtx_base, *g_tri_base;
+    const uint32_t *grp_chunk_base, *grp_item_base, *grp_items;
+    uint32_t total_gvtx, total_gtri, total_chunks;
+    int n_groups;
     int n_items;
     int inline_span;           // spans wider than this go to the long-span bins
     uint32_t total_px, total_tiles, total_dof_tiles;
-    uint2 *list;               // drawable triangles {t, item}
+    uint2 *list;               // drawable triangles {batch triangle (tri_base[item] + t), item}
     uint32_t list_cap;
     uint2 *clip;               // drawable triangles crossing the near plane {t, item}: entry j at clip[clip_cap - 1 - j]
     uint32_t clip_cap;
-    TriRec *recs;              // scanline set-up of list entry i (list_cap entries)
-    uint32_t *recmap;          // per batch triangle (tri_base[item] + t): its list entry, or kRecClip
-    uint32_t *tall;            // list entries of the tall triangles (list_cap entries)
+    TriRec *recs;              // per batch triangle (tri_base[item] + t): the scanline set-up of a walk-list
+                               // triangle, or flags kRecClip for a near-clipped one (others: stale)
+    uint32_t *tall;            // batch triangles of the tall set-ups (list_cap entries)
     int keep_keys;             // leave the depth keys for the caller (debug); else the shade resets them
     SpanRec *spans;            // long-span bins
     uint32_t span_cap;
@@ -267,7 +298,8 @@ constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqLayers = 4, kSeqFused = 8, kSeqS
 cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st, int *launches, Profiler *prof);
 // The depth-of-field gather alone (items prepared by the caller).
 cudaError_t launch_dof(const BatchDev *b, cudaStream_t st);
-// Upload the constant tables (depth-of-field taps) to the current device.
+// Upload the constant tables (depth-of-field taps) to the current device and
+// set the kernels' shared-memory limits there; before any launch or capture.
 cudaError_t init_device_constants();
 
 } // namespace sgl

@@ -106,8 +106,13 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     // prefixes and pool offsets
     uint32_t *hb = (uint32_t *)sl.h_bases.ptr;
     uint32_t *vb = hb, *tb = hb + (n + 1), *pb = hb + 2 * (n + 1), *gb = hb + 3 * (n + 1), *fb = hb + 4 * (n + 1);
-    uint32_t *gvb = hb + 5 * (n + 1), *gtb = hb + 6 * (n + 1), *qb = hb + 7 * (n + 1);
-    uint64_t tv = 0, tt = 0, tp = 0, tg = 0, tf = 0, dof_px = 0, dofz_px = 0, tgv = 0, tgt = 0, tq = 0;
+    uint32_t *gvb = hb + 5 * (n + 1), *gtb = hb + 6 * (n + 1);
+    uint32_t *gcb = hb + 7 * (n + 1), *gib = hb + 8 * (n + 1), *gi = hb + 9 * (n + 1);
+    uint64_t tv = 0, tt = 0, tp = 0, tg = 0, tf = 0, dof_px = 0, dofz_px = 0, tgv = 0, tgt = 0;
+    // items of fused scenes, grouped by the vertex data they read (the scene's
+    // world positions, or a posed request's own), groups in order of first use
+    std::vector<const void *> grp_key;
+    std::vector<std::vector<uint32_t>> grp_members;
     int geom_flags = 0;
     size_t ndc_off = 0, yes_off = 0;
     std::vector<size_t> ndc_at(n), yes_at(n), dof_at(n), dofz_at(n);
@@ -121,9 +126,16 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         fb[i] = (uint32_t)tf;
         gvb[i] = (uint32_t)tgv;
         gtb[i] = (uint32_t)tgt;
-        qb[i] = (uint32_t)tq;
         if (s.dev.fused) {
-            tq += s.dev.n_prims;
+            const void *key = e[i].wpos ? (const void *)e[i].wpos : (const void *)s.dev.wpos;
+            size_t gk = 0;
+            while (gk < grp_key.size() && grp_key[gk] != key)
+                gk++;
+            if (gk == grp_key.size()) {
+                grp_key.push_back(key);
+                grp_members.emplace_back();
+            }
+            grp_members[gk].push_back((uint32_t)i);
             geom_flags |= kSeqFused;
         } else {
             tgv += s.n_vertices;
@@ -148,8 +160,22 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
                 dofz_px += align_up((size_t)v.w * v.h, 64);
         }
     }
+    // the fused pass's groups: chunks of kGeomWarps primitives, items
+    uint64_t tc = 0;
+    uint32_t n_grouped = 0;
+    const int n_groups = (int)grp_key.size();
+    for (int k = 0; k < n_groups; k++) {
+        gcb[k] = (uint32_t)tc;
+        gib[k] = n_grouped;
+        const Scene &s = *e[grp_members[k][0]].scene;
+        tc += (s.dev.n_prims + kGeomWarps - 1) / kGeomWarps;
+        for (uint32_t it : grp_members[k])
+            gi[n_grouped++] = it;
+    }
+    gcb[n_groups] = (uint32_t)tc;
+    gib[n_groups] = n_grouped;
     if (tv >= (1ull << 32) || tt >= (1ull << 31) || tp >= (1ull << 32) || tg >= (1ull << 32) || tf >= (1ull << 32) ||
-        tq >= (1ull << 32)) {
+        tc >= (1ull << 31)) {
         ctx->fail("batch too large (%llu vertices, %llu triangles, %llu pixels)", (unsigned long long)tv,
                   (unsigned long long)tt, (unsigned long long)tp);
         return SGL_ERR_UNSUPPORTED;
@@ -161,7 +187,6 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     fb[n] = (uint32_t)tf;
     gvb[n] = (uint32_t)tgv;
     gtb[n] = (uint32_t)tgt;
-    qb[n] = (uint32_t)tq;
     const size_t span_cap = std::max<size_t>(65536, tp / 8);
     CUDA_TRY(ndc.ensure(sizeof(float4) * std::max<size_t>(ndc_off, 1)));
     CUDA_TRY(yes.ensure(std::max<size_t>(yes_off, 1)));
@@ -175,7 +200,6 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     CUDA_TRY(prec.ensure(sizeof(float4) * std::max<uint64_t>(tp, 1)));
     CUDA_TRY(list.ensure(sizeof(uint2) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(recs.ensure(sizeof(TriRec) * std::max<uint64_t>(tt, 1)));
-    CUDA_TRY(recmap.ensure(sizeof(uint32_t) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(tall.ensure(sizeof(uint32_t) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(spans.ensure(sizeof(SpanRec) * span_cap));
     if (dof_px) {
@@ -264,10 +288,13 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.dof_base = db + 4 * (n + 1);
     bd.g_vtx_base = db + 5 * (n + 1);
     bd.g_tri_base = db + 6 * (n + 1);
-    bd.prim_base = db + 7 * (n + 1);
+    bd.grp_chunk_base = db + 7 * (n + 1);
+    bd.grp_item_base = db + 8 * (n + 1);
+    bd.grp_items = db + 9 * (n + 1);
+    bd.n_groups = n_groups;
     bd.total_gvtx = (uint32_t)tgv;
     bd.total_gtri = (uint32_t)tgt;
-    bd.total_prims = (uint32_t)tq;
+    bd.total_chunks = (uint32_t)tc;
     bd.n_items = n;
     bd.inline_span = inline_span;
     bd.total_px = (uint32_t)tp;
@@ -278,7 +305,6 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.clip = (uint2 *)list.ptr; // shares the list buffer, filled from its end
     bd.clip_cap = bd.list_cap;
     bd.recs = (TriRec *)recs.ptr;
-    bd.recmap = (uint32_t *)recmap.ptr;
     bd.tall = (uint32_t *)tall.ptr;
     bd.keep_keys = slot_flags != nullptr; // debug renders read the keys back
     sl.keep_keys = bd.keep_keys != 0;

@@ -53,7 +53,7 @@ struct Ctx;
 // A scene resident in device memory.
 struct Scene {
     DevBuf d_pos_u, d_nrm_v, d_vnode, d_tris, d_prims, d_mats, d_texs, d_texels, d_wpos, d_wnrm, d_uv,
-        d_node_world, d_node_rs, d_lights, d_pgeo;
+        d_node_world, d_node_rs, d_lights, d_pgeo, d_pshade;
     SceneDev dev{};
     LightsDev lights{};
     std::vector<sgl_node_desc> nodes;
@@ -114,10 +114,11 @@ struct Lane {
         bool keep_keys = false;
     } slots[kSlots];
     int next = 0;
-    DevBuf list, recs, recmap, tall, spans, ndc, yes, key, prec, doftmp, dofz;
+    DevBuf list, recs, tall, spans, ndc, yes, key, prec, doftmp, dofz;
     DevBuf frags, frag_head, layer0; // views with transparency layers
-    static constexpr int kBaseArrays = 8; // prefixes: vertices, triangles, pixels, tiles, dof tiles, and the
-                                          // geometry passes' vertices, triangles and primitives
+    static constexpr int kBaseArrays = 10; // prefixes: vertices, triangles, pixels, tiles, dof tiles, the
+                                           // general geometry pass's vertices and triangles; the fused
+                                           // pass's group chunks, group items and the grouped items
     size_t frag_want = 0;            // fragments the pool must hold (grown after an overflow)
     bool keys_dirty = false; // the key pool may hold other than kEmptyKey (debug, failed launch)
     ~Lane();

@@ -362,6 +362,30 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     CUDA_TRY(upload(d_pgeo, pgeo.data(), pgeo.size()));
     CUDA_TRY(upload(d_mats, mats.data(), mats.size()));
     CUDA_TRY(upload(d_texs, texs.data(), texs.size()));
+    // per draw-order primitive: the material and texture the pixel shader binds
+    const MatDesc def_mat{d->default_material.color,
+                          d->default_material.texture < d->n_textures ? d->default_material.texture : -1,
+                          d->default_material.double_sided, d->default_material.shininess};
+    std::vector<PrimShade> pshade(std::max<size_t>(prims.size(), 1));
+    for (size_t q = 0; q < prims.size(); q++) {
+        const int mi = prims[q].material;
+        const bool in_range = mi >= 0 && mi < d->n_materials;
+        const MatDesc &m = in_range ? mats[mi] : def_mat;
+        PrimShade ps{};
+        ps.color = m.color;
+        ps.shininess = m.shininess;
+        ps.double_sided = in_range && mats[mi].double_sided ? 1 : 0;
+        if (m.texture < 0 || m.texture >= d->n_textures) {
+            ps.tex = nullptr;
+            ps.tw = ps.th = 1;
+        } else {
+            ps.tex = texs[m.texture].texels;
+            ps.tw = texs[m.texture].w;
+            ps.th = texs[m.texture].h;
+        }
+        pshade[q] = ps;
+    }
+    CUDA_TRY(upload(d_pshade, pshade.data(), pshade.size()));
     CUDA_TRY(d_wpos.ensure(sizeof(float4) * std::max<size_t>(n_vertices, 1)));
     CUDA_TRY(d_wnrm.ensure(sizeof(float4) * std::max<size_t>(n_vertices, 1)));
     CUDA_TRY(d_uv.ensure(sizeof(float2) * std::max<size_t>(n_vertices, 1)));
@@ -377,6 +401,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     dev.wnrm = (float4 *)d_wnrm.ptr;
     dev.uv = (float2 *)d_uv.ptr;
     dev.pgeo = (const uint4 *)d_pgeo.ptr;
+    dev.pshade = (const PrimShade *)d_pshade.ptr;
     dev.n_prims = (uint32_t)pgeo.size();
     dev.fused = fused ? 1 : 0;
     dev.n_vertices = n_vertices;
@@ -394,7 +419,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     if (st != SGL_OK)
         return st;
     device_bytes = d_pos_u.bytes + d_nrm_v.bytes + d_vnode.bytes + d_tris.bytes + d_prims.bytes + d_mats.bytes +
-                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_uv.bytes + d_node_world.bytes + d_node_rs.bytes + d_lights.bytes + d_pgeo.bytes;
+                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_uv.bytes + d_node_world.bytes + d_node_rs.bytes + d_lights.bytes + d_pgeo.bytes + d_pshade.bytes;
     return SGL_OK;
 }
 

@@ -295,6 +295,79 @@ def test_animate_matches_the_reference(tmp_path):
             assert np.array_equal(bits(nd.translation[:]), bits(s.node_translation[i])), (t, i)
 
 
+def _flatten_reference(r):
+    """The reference loader's scene_t in the library's flat scene layout: nodes
+    in order (parents from their children lists); each node's primitives as
+    the renderer draws them (triangle lists, strips and fans; the other modes
+    draw nothing, renderer.cpp:195-230), without the two spare vertices the
+    loader appends to each primitive (gltf.cpp:174-175)."""
+    from swegl_gb300 import scenes as S
+
+    s = S.Scene()
+    parent = [-1] * len(r.nodes)
+    for k, n in enumerate(r.nodes):
+        for c in n["children"]:
+            parent[c] = k
+    nv = ni = 0
+    pos, nrm, uv, idx = [], [], [], []
+    for k, n in enumerate(r.nodes):
+        s.node_scale.append(n["scale"])
+        s.node_rotation.append(n["rotation"])
+        s.node_translation.append(n["translation"])
+        s.node_parent.append(parent[k])
+        for p in n["primitives"]:
+            if p["mode"] not in (4, 5, 6):
+                continue
+            v = p["vertices"][:-2]
+            s.primitives.append((k, p["mode"], p["material"], nv, len(v), ni, len(p["indices"])))
+            pos.append(v[:, 0:3])
+            nrm.append(v[:, 3:6])
+            uv.append(v[:, 6:8])
+            idx.append(p["indices"])
+            nv += len(v)
+            ni += len(p["indices"])
+    s.positions, s.normals, s.uvs = np.concatenate(pos), np.concatenate(nrm), np.concatenate(uv)
+    s.indices = np.concatenate(idx).astype(np.uint32)
+    # materials as the library keeps them: colour, texture, double sided, shininess
+    s.materials = [(c, t, ds, 32) for (c, _m, _r, t, ds) in r.materials]
+    return s
+
+
+@needs_ref
+@pytest.mark.parametrize("glb,seed", [(True, 3), (False, 5)])
+def test_loader_matches_the_reference_loader(lib, tmp_path, glb, seed):
+    """The library's loader against the reference's own (src/data/gltf.cpp,
+    compiled by oracle/ref with a stand-in for its un-vendored nlohmann/json
+    include): node transforms and hierarchy, every primitive's vertices,
+    texture coordinates, normals and indices (bit-exact), materials, image
+    count, root nodes and animation channels.  A GLB with a PNG in a buffer
+    view, and a .gltf with an external buffer (the reference reads buffers
+    only from files)."""
+    from swegl_gb300.gltf import GltfScene
+
+    path = GF.build_test_scene(str(tmp_path), glb, seed=seed)
+    ref = oracle.reference_gltf(path)
+    g = GltfScene(path)
+    ours = g.scene()
+    A, B = scene_arrays(ours), scene_arrays(_flatten_reference(ref))
+    for k in A:
+        if k == "textures":
+            assert len(A[k]) == ref.images
+        else:
+            assert A[k].shape == B[k].shape and np.array_equal(A[k], B[k]), f"{k} differs from the reference loader"
+    assert ref.roots == [k for k, p in enumerate(ours.node_parent) if p < 0]
+    # animation channels: the restatement's, which the library's animate()
+    # follows (test_animation_matches_the_restatement), against the reference's
+    res = GO.load_scene(path, GO.decode_image)
+    assert g.animation_count == len(ref.animations) == len(res.animations)
+    for (e0, c0), (e1, c1) in zip(ref.animations, res.animations):
+        assert bits(e0) == bits(e1)
+        assert [(n, p) for n, p, _ in c0] == [(n, p) for n, p, _ in c1]
+        for (_, _, s0), (_, _, s1) in zip(c0, c1):
+            assert np.array_equal(bits(np.array([[t, *v] for t, v in s0])), bits(np.array([[t, *v] for t, v in s1])))
+    g.close()
+
+
 @needs_ref
 def test_loaded_scene_renders_as_the_reference_renders_it(tmp_path):
     """The restated loader's scene, lit and animated, rendered by the oracle
