@@ -348,6 +348,16 @@ SGL_API sgl_status sgl_server_drain(sgl_server *srv, double timeout_s);
 SGL_API sgl_status sgl_server_stats(sgl_server *srv, uint64_t *batches, uint64_t *kernels, uint64_t *completed);
 SGL_API void       sgl_server_destroy(sgl_server *srv);
 
+/* Device-side bounds checks.  The library built with them (libsgl_check.so,
+ * compiled with -DSGL_BOUNDS_CHECK beside libsgl.so) tests the index of each
+ * guarded device access — projected vertices, set-up records, depth keys,
+ * winner records, output pixels, texels — against its buffer; an index outside
+ * is recorded (the first failure's check code and index, and a count) and the
+ * access skipped, so nothing traps.  Reads the record (and clears it when
+ * `reset`); SGL_ERR_UNSUPPORTED from the library without the checks.  No
+ * reference counterpart (a stand-in for a memory checker). */
+SGL_API sgl_status sgl_check_status(sgl_ctx *ctx, uint32_t *code, uint64_t *index, uint32_t *count, int reset);
+
 /* Per-kernel device timing (CUDA events on the launching stream around each
  * kernel of every frame rendered while enabled).  Enabling resets the totals.
  * Kernels are numbered 0..n-1; reading past the last returns SGL_ERR_NOT_FOUND.

@@ -163,6 +163,8 @@ __global__ void __launch_bounds__(256) k_vertex(const BatchDev *b)
             p.x = p.x / fabsf(p.z);
             p.y = p.y / fabsf(p.z);
         }
+        if (!in_bounds(l < hi - lo, CHK_NDC, l))
+            return;
         ndc[l] = make_float4(p.x, p.y, p.z, 0.0f);
         yes[l] = below_near(p.z) ? kYesBehind : 0; // kYesDrawn is set by k_flags
     };
@@ -355,7 +357,8 @@ struct ItemAcc {
 // The record slot of a near-clipped batch triangle: flags = kRecClip.
 __device__ __forceinline__ void mark_clip(const BatchDev *b, uint32_t r)
 {
-    reinterpret_cast<uint32_t *>(b->recs + r)[kRecFlagsWord] = kRecClip;
+    if (in_bounds(r < b->list_cap, CHK_REC, r))
+        reinterpret_cast<uint32_t *>(b->recs + r)[kRecFlagsWord] = kRecClip;
 }
 
 // 32-bit batch counter w (C_*)
@@ -506,33 +509,37 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
 // scene in the batch; the reference likewise transforms a scene to world
 // space once for all the viewports of a render call, renderer.hpp:27-34).
 // A block takes a chunk of kGeomWarps consecutive primitives of a group and
-// loads each warp's primitive once — world positions into registers, its
-// triangles as local vertex indices into shared memory — then runs it for
-// every item of the group.  The items go in passes of kGeomPass: per item the
-// warp records its walk-list and clip-list decisions as ballot masks, and
-// after the pass one global atomic reserves both lists for all the pass's
-// items and warps (reserve_lists).
-constexpr int kGeomPass = 8;                // items per list reservation
-constexpr int kGeomVPL = kFuseVerts / 32;   // vertices per lane
-constexpr int kGeomTG = kFuseTris / 32;     // groups of 32 triangles
+// runs each warp's primitive for every item of the group: the primitive's
+// first 64 triangles stay in registers as local vertex indices and its world
+// positions are read again per item (from L1 after the first).  The items go
+// in passes of kGeomPass: per item the warp records its walk-list and
+// clip-list decisions as ballot masks, and after the pass one global atomic
+// reserves both lists for all the pass's items and warps (reserve_lists).
+constexpr int kGeomPass = 8;            // items per list reservation
+constexpr int kGeomTG = kFuseTris / 32; // groups of 32 triangles
+constexpr int kGeomBlocks = 4;          // resident blocks per SM the pass is compiled for
 struct GeomShared {
-    float pos[kGeomWarps][3 * kFuseVerts];  // x, y, z' of each vertex (for the item in hand)
-    uint32_t tri[kGeomWarps][kFuseTris];    // local vertex indices a | b << 8 | c << 16
+    float pos[kGeomWarps][3 * kFuseVerts];         // x, y, z' of each vertex (for the item in hand)
     uint8_t yes[kGeomWarps][kFuseVerts];
     uint32_t walk[kGeomPass][kGeomWarps][kGeomTG]; // per 32 triangles: ballot of the walk list
     uint32_t clip[kGeomPass][kGeomWarps][kGeomTG]; // ... of the clip list
     uint32_t cnt[kGeomPass][kGeomWarps][2];        // entries of each list, then their first positions
     uint32_t nx[kGeomPass][kGeomWarps];            // drawable triangles without a pixel column
-    float m[kGeomPass][24];                        // view and projection rows 0-2 of each item of the pass
-    float vm[kGeomPass][4];                        // vm00, vm03, vm11, vm13
-    float4 *ndc[kGeomPass];
-    uint32_t item[kGeomPass], tri_lo[kGeomPass];
-    uint32_t next;                                 // the block's next chunk
+    float view[kGeomWarps][28];                    // the warp's copy of the item in hand: view and
+                                                   // projection rows 0-2, vm00, vm03, vm11, vm13
 };
 static_assert(kFuseVerts <= 256, "local vertex indices are bytes");
 constexpr size_t kGeomSmem = sizeof(GeomShared);
 
-__global__ void __launch_bounds__(kGeomWarps * 32, 3) k_geom(const BatchDev *b)
+// The local vertex indices of triangle t of a fused primitive (a | b << 8 | c << 16).
+__device__ __forceinline__ uint32_t geom_tri(const uint4 *tris, uint4 gq, uint32_t t)
+{
+    const uint4 tri = tris[gq.z + t];
+    in_bounds(tri.x - gq.x < gq.y && tri.y - gq.x < gq.y && tri.z - gq.x < gq.y, CHK_LOCAL, gq.z + t);
+    return (tri.x - gq.x) | ((tri.y - gq.x) << 8) | ((tri.z - gq.x) << 16);
+}
+
+__global__ void __launch_bounds__(kGeomWarps * 32, kGeomBlocks) k_geom(const BatchDev *b)
 {
     extern __shared__ __align__(16) unsigned char geom_smem[];
     GeomShared &S = *reinterpret_cast<GeomShared *>(geom_smem);
@@ -541,22 +548,12 @@ __global__ void __launch_bounds__(kGeomWarps * 32, 3) k_geom(const BatchDev *b)
     const unsigned below = (1u << lane) - 1u;
     float *pos = S.pos[warp];
     uint8_t *sy = S.yes[warp];
-    uint32_t *stri = S.tri[warp];
+    float *vw = S.view[warp];
     int g = -1;
     uint32_t c_lo = 0, c_hi = 0;
     const uint32_t total = b->total_chunks;
-    // chunks: the block's index first, then from a shared counter; every
-    // thread of the block runs the same iterations (barriers inside)
-    if (threadIdx.x == 0)
-        S.next = blockIdx.x;
-    for (;;) {
-        __syncthreads();
-        const uint32_t c = S.next;
-        if (c >= total)
-            break;
-        __syncthreads(); // every thread has read S.next
-        if (threadIdx.x == 0)
-            S.next = gridDim.x + atomicAdd(counter32(b, C_GEOM_Q), 1u);
+    // every thread of the block runs the same iterations (barriers inside)
+    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
         if (c < c_lo || c >= c_hi) {
             g = find_item(b->grp_chunk_base, b->n_groups, c);
             c_lo = __ldg(b->grp_chunk_base + g);
@@ -568,79 +565,70 @@ __global__ void __launch_bounds__(kGeomWarps * 32, 3) k_geom(const BatchDev *b)
         const bool has = q < sc.n_prims;
         uint4 gq = make_uint4(0u, 0u, 0u, 0u); // first vertex, vertex count, first triangle, triangle count
         bool ds = false;
-        float wx[kGeomVPL], wy[kGeomVPL], wz[kGeomVPL];
-        __syncwarp(); // the previous chunk's reads of stri are done
+        uint32_t tr0 = 0, tr1 = 0; // the first 64 triangles, local vertex indices
+        const float4 *wpos = sc.wpos;
+        const uint4 *tris = sc.tris;
         if (has) {
             gq = sc.pgeo[q];
             gq.y = min(gq.y, kFuseVerts); // (a fused scene's primitives are within both limits)
             gq.w = min(gq.w, kFuseTris);
-            const float4 *wpos = sc.wpos + gq.x;
-#pragma unroll
-            for (int k = 0; k < kGeomVPL; k++) {
-                wx[k] = wy[k] = wz[k] = 0.0f;
-                if (lane + 32 * k < gq.y) {
-                    const float4 w = wpos[lane + 32 * k];
-                    wx[k] = w.x;
-                    wy[k] = w.y;
-                    wz[k] = w.z;
-                }
-            }
-            for (uint32_t t = lane; t < gq.w; t += 32) {
-                const uint4 tri = sc.tris[gq.z + t];
-                stri[t] = (tri.x - gq.x) | ((tri.y - gq.x) << 8) | ((tri.z - gq.x) << 16);
-            }
+            if (lane < gq.w)
+                tr0 = geom_tri(tris, gq, lane);
+            if (lane + 32 < gq.w)
+                tr1 = geom_tri(tris, gq, lane + 32);
             ds = sc.pshade[q].double_sided != 0;
         }
         for (uint32_t v0 = i_lo; v0 < i_hi; v0 += kGeomPass) {
             const int nv = (int)min((uint32_t)kGeomPass, i_hi - v0);
-            __syncthreads(); // the previous pass is done with the view data and the counts
-            if (warp < nv) { // warp vi loads item vi's view
-                const uint32_t item = __ldg(b->grp_items + v0 + warp);
-                const ItemDev &it = b->items[item];
-                if (lane < 12) {
-                    S.m[warp][lane] = it.v.view[lane];
-                    S.m[warp][12 + lane] = it.v.proj[lane];
-                } else if (lane == 12) {
-                    S.vm[warp][0] = it.v.vm00;
-                    S.vm[warp][1] = it.v.vm03;
-                    S.vm[warp][2] = it.v.vm11;
-                    S.vm[warp][3] = it.v.vm13;
-                } else if (lane == 13) {
-                    S.ndc[warp] = it.ndc;
-                    S.item[warp] = item;
-                    S.tri_lo[warp] = __ldg(b->tri_base + item);
-                }
-            }
-            __syncthreads();
             for (int vi = 0; vi < nv; vi++) {
                 uint32_t c0 = 0, c1 = 0, nx = 0;
                 if (has) {
-                    const float *m = S.m[vi];
-                    float4 *ndc = S.ndc[vi] + gq.x;
-                    __syncwarp(); // the previous item's reads of pos and sy are done
-                    // world_to_camera_or_frustum (vertex_shaders.hpp:35-52), as k_vertex
+                    const uint32_t item = __ldg(b->grp_items + v0 + vi);
+                    const ItemDev &it = b->items[item];
+                    __syncwarp(); // the previous item's reads of pos, sy and vw are done
+                    if (lane < 12) {
+                        vw[lane] = it.v.view[lane];
+                        vw[12 + lane] = it.v.proj[lane];
+                    } else if (lane == 12) {
+                        vw[24] = it.v.vm00;
+                        vw[25] = it.v.vm03;
+                        vw[26] = it.v.vm11;
+                        vw[27] = it.v.vm13;
+                    }
+                    float4 *ndc = it.ndc + gq.x;
+                    __syncwarp();
+                    // world_to_camera_or_frustum (vertex_shaders.hpp:35-52), as
+                    // k_vertex; 128 vertices per round, their loads issued first
+                    for (uint32_t i0 = 0; i0 < gq.y; i0 += 128) {
+                        float4 w[4];
 #pragma unroll
-                    for (int k = 0; k < kGeomVPL; k++) {
-                        const uint32_t i = lane + 32 * k;
-                        if (i < gq.y) {
-                            V3 v = transform3(mk3(wx[k], wy[k], wz[k]), m);
-                            v = transform3(v, m + 12);
-                            if (v.z != 0.0f) {
-                                v.x = v.x / fabsf(v.z);
-                                v.y = v.y / fabsf(v.z);
+                        for (int k = 0; k < 4; k++)
+                            if (i0 + lane + 32 * k < gq.y)
+                                w[k] = wpos[gq.x + i0 + lane + 32 * k];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const uint32_t i = i0 + lane + 32 * k;
+                            if (i < gq.y) {
+                                V3 v = transform3(mk3(w[k].x, w[k].y, w[k].z), vw);
+                                v = transform3(v, vw + 12);
+                                if (v.z != 0.0f) {
+                                    v.x = v.x / fabsf(v.z);
+                                    v.y = v.y / fabsf(v.z);
+                                }
+                                if (in_bounds(gq.x + i < sc.n_vertices, CHK_NDC, gq.x + i))
+                                    ndc[i] = make_float4(v.x, v.y, v.z, 0.0f);
+                                pos[3 * i] = v.x;
+                                pos[3 * i + 1] = v.y;
+                                pos[3 * i + 2] = v.z;
+                                sy[i] = below_near(v.z) ? kYesBehind : 0;
                             }
-                            ndc[i] = make_float4(v.x, v.y, v.z, 0.0f);
-                            pos[3 * i] = v.x;
-                            pos[3 * i + 1] = v.y;
-                            pos[3 * i + 2] = v.z;
-                            sy[i] = below_near(v.z) ? kYesBehind : 0;
                         }
                     }
                     __syncwarp();
                     // visibility flags (renderer.cpp:86-185), as k_flags; every
                     // store to a vertex writes the same value
                     for (uint32_t t = lane; t < gq.w; t += 32) {
-                        const uint32_t tp = stri[t];
+                        const uint32_t tp = t < 32 ? tr0 : (t < 64 ? tr1 : geom_tri(tris, gq, t));
                         const uint32_t ia = tp & 0xFFu, ib = (tp >> 8) & 0xFFu, ic = tp >> 16;
                         const V3 a = mk3(pos[3 * ia], pos[3 * ia + 1], pos[3 * ia + 2]);
                         const V3 c1v = mk3(pos[3 * ib], pos[3 * ib + 1], pos[3 * ib + 2]);
@@ -653,12 +641,12 @@ __global__ void __launch_bounds__(kGeomWarps * 32, 3) k_geom(const BatchDev *b)
                     }
                     __syncwarp();
                     // the compaction's decisions, as k_compact
-                    const float vm00 = S.vm[vi][0], vm03 = S.vm[vi][1], vm11 = S.vm[vi][2], vm13 = S.vm[vi][3];
+                    const float vm00 = vw[24], vm03 = vw[25], vm11 = vw[26], vm13 = vw[27];
                     for (uint32_t t0 = 0; t0 < gq.w; t0 += 32) {
                         const uint32_t t = t0 + lane;
                         int d = 0; // 0 none, 1 walk list, 2 clip list, 3 no pixel column
                         if (t < gq.w) {
-                            const uint32_t tp = stri[t];
+                            const uint32_t tp = t < 32 ? tr0 : (t < 64 ? tr1 : geom_tri(tris, gq, t));
                             const uint32_t ia = tp & 0xFFu, ib = (tp >> 8) & 0xFFu, ic = tp >> 16;
                             const uint32_t ya = sy[ia], yb = sy[ib], yc = sy[ic];
                             if (ya & yb & yc & kYesDrawn) {
@@ -726,7 +714,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32, 3) k_geom(const BatchDev *b)
                     }
                     // triangles counted as drawn here: they reached fill_triangle_2's set-up
                     if (x)
-                        atomicAdd(b->item_counters + 2 * (size_t)S.item[vi], (unsigned long long)x);
+                        atomicAdd(b->item_counters + 2 * (size_t)__ldg(b->grp_items + v0 + vi), (unsigned long long)x);
                 }
                 const unsigned long long old = reserve_lists(b, n0, n1);
                 const uint32_t g0 = (uint32_t)old, g1 = (uint32_t)(old >> 32);
@@ -740,7 +728,8 @@ __global__ void __launch_bounds__(kGeomWarps * 32, 3) k_geom(const BatchDev *b)
             if (has) {
                 for (int vi = 0; vi < nv; vi++) {
                     uint32_t o0 = S.cnt[vi][warp][0], o1 = S.cnt[vi][warp][1];
-                    const uint32_t item = S.item[vi], tlo = S.tri_lo[vi];
+                    const uint32_t item = __ldg(b->grp_items + v0 + vi);
+                    const uint32_t tlo = __ldg(b->tri_base + item);
                     for (uint32_t t0 = 0; t0 < gq.w; t0 += 32) {
                         const unsigned m1 = S.walk[vi][warp][t0 >> 5], m2 = S.clip[vi][warp][t0 >> 5];
                         const uint32_t t = t0 + lane;
@@ -759,6 +748,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32, 3) k_geom(const BatchDev *b)
                     }
                 }
             }
+            __syncthreads(); // the counts and masks are rewritten by the next pass
         }
     }
 }
@@ -944,7 +934,9 @@ struct DepthVisitor {
         unsigned long long *row = it->key + ((long long)(y - v.y) * v.w - v.x);
         const uint32_t sl = slot;
         auto op = [&](int x, float z, float) {
-            key_min(row + x, make_key(z, sl));
+            if (in_bounds(x >= v.x && x < v.x + v.w && y >= v.y && y < v.y + v.h, CHK_KEY,
+                          (unsigned long long)(uint32_t)y << 32 | (uint32_t)x))
+                key_min(row + x, make_key(z, sl));
         };
         span_pixels(x1, x2, Ls, Rs, op);
     }
@@ -1153,7 +1145,7 @@ __device__ __forceinline__ bool bin_span_warp(const BatchDev *b, bool want, uint
 // The view fields the walk needs, kept in registers while the item stays.
 struct WalkView {
     uint32_t item;
-    int x, y, w;
+    int x, y, w, h;
     unsigned long long *key;
     int inline_span;
     __device__ __forceinline__ void load(const BatchDev *b, uint32_t i)
@@ -1163,6 +1155,7 @@ struct WalkView {
         x = it.v.x;
         y = it.v.y;
         w = it.v.w;
+        h = it.v.h;
         key = it.key;
     }
 };
@@ -1174,7 +1167,9 @@ __device__ __forceinline__ void span_depth(const WalkView &v, int y, uint32_t sl
         const float z = q.value();
         if (below_near(z) || __float_as_uint(z) >= kMaxZBits)
             continue;
-        key_min(row + x, make_key(z, slot));
+        if (in_bounds(x >= v.x && x < v.x + v.w && y >= v.y && y < v.y + v.h, CHK_KEY,
+                      (unsigned long long)(uint32_t)y << 32 | (uint32_t)x))
+            key_min(row + x, make_key(z, slot));
     }
 }
 
@@ -1240,6 +1235,8 @@ __device__ __forceinline__ bool tri_setup(const BatchDev *b, uint32_t r, uint32_
     sort_y_asc(a, c1, c2, pa, pb, pc);
     const V3 v0 = a, v1 = c1, v2 = c2;
     const int y0 = f2i(ceilf(v0.y)), y1 = f2i(ceilf(v1.y)), y2 = f2i(ceilf(v2.y));
+    if (!in_bounds(r < b->list_cap, CHK_REC, r))
+        return false;
     float4 *dst = reinterpret_cast<float4 *>(b->recs + r);
     if (y0 == y2) {
         // no rows: n_u = n_d = 0
@@ -1454,9 +1451,9 @@ __device__ __noinline__ void walk_tall_all(const BatchDev *b, ItemAcc &acc);
 
 // Depth walk of the drawable triangles wholly in front of the near plane
 // (fill_triangle's normal case, renderer.cpp:281-285: one sub-triangle, slot
-// 2t).  Each warp takes groups of 32 list entries (from work queues), loads
-// their set-ups into shared memory (one 128-byte record per load) and deals
-// their rows across its lanes.  FRAGS: the fragment capture of a layered view (the
+// 2t).  Each warp takes groups of 32 list entries (warp-strided), loads their
+// set-ups into shared memory (one 128-byte record per load) and deals their
+// rows across its lanes.  FRAGS: the fragment capture of a layered view (the
 // near-clipped triangles are captured by k_frags).
 template <bool FRAGS>
 __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(const BatchDev *b)
@@ -1479,7 +1476,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
 #pragma unroll 8
             for (uint32_t j = 0; j < cnt; j++) {
                 const uint32_t rj = __shfl_sync(0xFFFFFFFFu, rec, j);
-                cp_async4(&D[lane][j], reinterpret_cast<const uint32_t *>(b->recs + rj) + lane);
+                if (in_bounds(rj < b->list_cap, CHK_REC, rj))
+                    cp_async4(&D[lane][j], reinterpret_cast<const uint32_t *>(b->recs + rj) + lane);
             }
         }
         cp_async_commit();
@@ -1488,26 +1486,20 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
     WalkView view;
     view.item = 0xFFFFFFFFu;
     view.inline_span = b->inline_span;
-    // Groups come from kQueues queues (queue q holds groups q, q + kQueues,
-    // ...; warp w draws from queue w % kQueues).  While group g is walked, the
-    // records of the next one are copied in, the list entries of the one
-    // after are loaded, and the index of the one after that is drawn, so that
-    // neither the draw's round trip nor the entries' load holds up a copy.
-    const uint32_t wq = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % kQueues;
-    uint32_t *qc = counter32(b, C_WALK_Q + 32 * (int)wq);
-    auto draw = [&]() -> uint32_t { return lane == 0 ? atomicAdd(qc, 1u) : 0u; }; // lane 0 holds the draw
-    auto group_of = [&](uint32_t d) -> uint32_t { return wq + kQueues * __shfl_sync(0xFFFFFFFFu, d, 0); };
-    const uint32_t d0 = draw(), d1 = draw();
-    uint32_t g = group_of(d0), g_next = group_of(d1);
-    uint32_t d_after = draw();
+    // Warps take groups g, g + W, g + 2W, ... (W warps in the grid; work
+    // queues were measured slower: 41 -> 48 us on the 1080p frame).  While
+    // group g is walked, the records of the next one are copied in and the
+    // list entries of the one after are loaded.
+    const uint32_t W = (gridDim.x * blockDim.x) >> 5;
+    uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t g_next = g + W;
     int buf = 0;
     fetch(g, rec_of(g), sm[threadIdx.x >> 5][0]);
     uint32_t rec_next = rec_of(g_next);
     while (g < n_groups) {
         fetch(g_next, rec_next, sm[threadIdx.x >> 5][buf ^ 1]);
-        const uint32_t g_after = group_of(d_after);
+        const uint32_t g_after = g_next + W;
         rec_next = rec_of(g_after);
-        d_after = g_after < n_groups ? draw() : 0xFFFFFFFFu / kQueues; // (past the end: no more draws)
         cp_async_wait<1>(); // this group's copies are done
         WalkRow *S = sm[threadIdx.x >> 5][buf];
         const uint32_t base = 32 * g;
@@ -1792,6 +1784,9 @@ __device__ __forceinline__ void spans_pass(const BatchDev *b, bool winner)
                 continue;
             const unsigned long long key = make_key(z, r.slot);
             unsigned long long *kp = it.key + base + x;
+            if (!in_bounds(x >= it.v.x && x < it.v.x + it.v.w && y >= it.v.y && y < it.v.y + it.v.h,
+                           winner ? CHK_PREC : CHK_KEY, (unsigned long long)(uint32_t)y << 32 | (uint32_t)x))
+                continue;
             if (!winner)
                 key_min(kp, key);
             else if (*kp == key)
@@ -1910,7 +1905,10 @@ __device__ __forceinline__ uint32_t shade_winner_impl(const BatchDev *b, uint32_
 {
     const ItemDev &it = b->items[item];
     const ViewDev &v = it.v;
-    const TriRec *rp = b->recs + __ldg(b->tri_base + item) + (slot >> 1);
+    const uint32_t r = __ldg(b->tri_base + item) + (slot >> 1);
+    if (!in_bounds(r < b->list_cap, CHK_REC, r))
+        return 0u;
+    const TriRec *rp = b->recs + r;
     const uint4 q6 = reinterpret_cast<const uint4 *>(rp)[6];
     const uint4 q7 = reinterpret_cast<const uint4 *>(rp)[7];
     const uint32_t flags = q6.y;
@@ -2028,7 +2026,8 @@ __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(c
                 const ViewDev &ve = ie.v;
                 const uint32_t c = shade_winner_impl<ALL_MODES>(b, e.y, e.x, e.z, overflow);
                 const int yy = (int)(e.x / (uint32_t)ve.w), xx = (int)(e.x - (uint32_t)yy * (uint32_t)ve.w);
-                ie.pixels[(long long)yy * ie.pitch_px + xx] = c;
+                if (in_bounds(yy < ve.h, CHK_PIXEL, e.x))
+                    ie.pixels[(long long)yy * ie.pitch_px + xx] = c;
                 __syncthreads();
                 if ((int)threadIdx.x < have - kShadeThreads)
                     queue[threadIdx.x] = queue[kShadeThreads + threadIdx.x];
@@ -2044,7 +2043,8 @@ __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(c
         const ItemDev &ie = b->items[e.y];
         const uint32_t c = shade_winner_impl<ALL_MODES>(b, e.y, e.x, e.z, overflow);
         const int yy = (int)(e.x / (uint32_t)ie.v.w), xx = (int)(e.x - (uint32_t)yy * (uint32_t)ie.v.w);
-        ie.pixels[(long long)yy * ie.pitch_px + xx] = c;
+        if (in_bounds(yy < ie.v.h, CHK_PIXEL, e.x))
+            ie.pixels[(long long)yy * ie.pitch_px + xx] = c;
     }
 }
 
@@ -2699,6 +2699,36 @@ cudaError_t init_device_constants()
     return e;
 }
 
+cudaError_t check_status(unsigned *code, unsigned long long *index, unsigned *count, bool reset, bool *compiled)
+{
+#ifdef SGL_BOUNDS_CHECK
+    *compiled = true;
+    unsigned long long first = 0;
+    unsigned n = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&first, g_check_first, sizeof first);
+    if (e == cudaSuccess)
+        e = cudaMemcpyFromSymbol(&n, g_check_count, sizeof n);
+    if (e == cudaSuccess && reset) {
+        const unsigned long long z0 = 0;
+        const unsigned z1 = 0;
+        e = cudaMemcpyToSymbol(g_check_first, &z0, sizeof z0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyToSymbol(g_check_count, &z1, sizeof z1);
+    }
+    *code = (unsigned)(first >> 48);
+    *index = first & 0xFFFFFFFFFFFFull;
+    *count = n;
+    return e;
+#else
+    *compiled = false;
+    *code = 0;
+    *index = 0;
+    *count = 0;
+    (void)reset;
+    return cudaSuccess;
+#endif
+}
+
 cudaError_t launch_dof(const BatchDev *b, cudaStream_t st)
 {
     k_dof<<<sm_count() * 8, 256, 0, st>>>(b);
@@ -2728,7 +2758,7 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
     int n = 0;
     mark(PK_GEOM);
     if (flags & kSeqFused) {
-        k_geom<<<sms * 3, kGeomWarps * 32, kGeomSmem, st>>>(b);
+        k_geom<<<sms * kGeomBlocks * 2, kGeomWarps * 32, kGeomSmem, st>>>(b);
         ran(PK_GEOM);
         n++;
     }

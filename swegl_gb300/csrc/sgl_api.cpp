@@ -362,8 +362,11 @@ SGL_API sgl_status sgl_render(sgl_ctx *c, int scene_id, const sgl_view *views, c
         }
         int slot = 0;
         sgl_status r = lane->prepare(ctx, &e, 1, ctx->tile, ctx->inline_span, nullptr, &slot);
-        if (r == SGL_OK)
-            r = lane->launch(ctx, slot, ctx->tile, false, &launches, &ctx->prof);
+        if (r == SGL_OK) {
+            // one CUDA graph launch per view (captured once per lane slot and
+            // sequence variant); direct launches while per-kernel timing is on
+            r = lane->launch(ctx, slot, ctx->tile, !ctx->prof.enabled, &launches, &ctx->prof);
+        }
         if (r != SGL_OK)
             return r;
         if (!device_buffers) {
@@ -672,6 +675,26 @@ SGL_API sgl_status sgl_dof(sgl_ctx *c, const sgl_view *view, const sgl_target *i
                                    dst, 4 * (size_t)v.w, 4 * (size_t)v.w, v.h, cudaMemcpyDeviceToHost, st));
     }
     CUDA_TRY(cudaStreamSynchronize(st)); // the descriptors above live on this call's stack
+    return SGL_OK;
+}
+
+SGL_API sgl_status sgl_check_status(sgl_ctx *c, uint32_t *code, uint64_t *index, uint32_t *count, int reset)
+{
+    Ctx *ctx = reinterpret_cast<Ctx *>(c);
+    if (!ctx || !code || !index || !count)
+        return SGL_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    bool compiled = false;
+    unsigned cd = 0, n = 0;
+    unsigned long long ix = 0;
+    CUDA_TRY(check_status(&cd, &ix, &n, reset != 0, &compiled));
+    if (!compiled) {
+        ctx->fail("this build has no device-side bounds checks (load libsgl_check.so)");
+        return SGL_ERR_UNSUPPORTED;
+    }
+    *code = cd;
+    *index = ix;
+    *count = n;
     return SGL_OK;
 }
 

@@ -13,6 +13,37 @@
 
 namespace sgl {
 
+// Device-side bounds checks.  The checked build (-DSGL_BOUNDS_CHECK, the
+// library libsgl_check.so) tests the index of each guarded access against its
+// buffer; an index outside records its check code and the index in a status
+// word (the first failure, and a count) and the access is skipped: nothing
+// traps and no kernel waits.  The host reads the status with
+// sgl_check_status().  In the normal build the checks compile away.
+enum CheckCode : unsigned {
+    CHK_NDC = 1,      // projected vertex: index against the scene's vertices
+    CHK_REC = 2,      // set-up record slot: batch triangle against the record pool
+    CHK_KEY = 3,      // depth key: pixel against the view rectangle
+    CHK_PREC = 4,     // winner record: pixel against the view
+    CHK_PIXEL = 5,    // output colour / depth: pixel against the view
+    CHK_TEXEL = 6,    // texel against its texture
+    CHK_LOCAL = 7,    // local vertex index of a fused primitive against its vertex count
+    CHK_DOF = 8,      // depth-of-field output: pixel against the view
+};
+#ifdef SGL_BOUNDS_CHECK
+static __device__ unsigned long long g_check_first; // code << 48 | index (low 48 bits); 0: no failure
+static __device__ unsigned int g_check_count;
+__device__ __forceinline__ bool in_bounds(bool ok, unsigned code, unsigned long long index)
+{
+    if (!ok) {
+        atomicCAS(&g_check_first, 0ull, ((unsigned long long)code << 48) | (index & 0xFFFFFFFFFFFFull));
+        atomicAdd(&g_check_count, 1u);
+    }
+    return ok;
+}
+#else
+__device__ __forceinline__ constexpr bool in_bounds(bool, unsigned, unsigned long long) { return true; }
+#endif
+
 struct V3 {
     float x, y, z;
 };

@@ -211,14 +211,12 @@ static_assert(offsetof(TriRec, flags) == 4 * kRecFlagsWord, "TriRec::flags word"
 
 // Batch counters (32-bit words); the drawn-triangle and fragment counts are
 // kept per item (item_counters) and summed by the host.
-enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_FRAGS = 8, C_TALL = 10, C_GEOM_Q = 11 };
+enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_FRAGS = 8, C_TALL = 10 };
 // Work queues of the shade kernel's tiles: kQueues counters, one per 128-byte
 // line so that blocks of different queues do not contend.
 constexpr int kQueues = 16;
 constexpr int C_SHADE_Q = 32;                       // 32-bit index of queue q: C_SHADE_Q + 32 q
-// ... and of the walk kernel's groups of 32 walk-list entries
-constexpr int C_WALK_Q = C_SHADE_Q + 32 * kQueues;   // 32-bit index of queue q: C_WALK_Q + 32 q
-constexpr int kCounterWords = (C_WALK_Q + 32 * kQueues) / 2; // 64-bit words
+constexpr int kCounterWords = (C_SHADE_Q + 32 * kQueues) / 2; // 64-bit words
 
 // A batch of views rendered by one launch sequence (lives in device memory).
 struct BatchDev {
@@ -296,6 +294,10 @@ cudaError_t launch_pose(const SceneDev &s, const float *node_world, const float 
 // k_flags, k_compact).
 constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqLayers = 4, kSeqFused = 8, kSeqSplit = 16, kSeqVariants = 32;
 cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st, int *launches, Profiler *prof);
+// The device-side bounds checks of the checked build (-DSGL_BOUNDS_CHECK):
+// the first failure's check code and index and the failure count, cleared
+// when `reset`; `compiled` says whether this build has the checks.
+cudaError_t check_status(unsigned *code, unsigned long long *index, unsigned *count, bool reset, bool *compiled);
 // The depth-of-field gather alone (items prepared by the caller).
 cudaError_t launch_dof(const BatchDev *b, cudaStream_t st);
 // Upload the constant tables (depth-of-field taps) to the current device and

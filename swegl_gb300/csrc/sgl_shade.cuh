@@ -181,6 +181,8 @@ __device__ __forceinline__ uint32_t sh_nearest(const Shader &sh, float progress)
     const uint32_t tw = (uint32_t)sh.tw, th = (uint32_t)sh.th;
     const uint32_t u = (uint32_t)f2i(t.x) % tw;
     const uint32_t vv = (uint32_t)f2i(t.y) % th;
+    if (sh.tex && !in_bounds(u < tw && vv < th, CHK_TEXEL, (unsigned long long)vv * tw + u))
+        return 0u;
     return sh.tex ? __ldg(sh.tex + vv * tw + u) : sh.color; // untextured: 1x1 of the colour
 }
 

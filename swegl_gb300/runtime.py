@@ -19,8 +19,10 @@ from . import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsgl.so")
+# the same library with device-side bounds checks (sgl_check_status)
+LIB_CHECK_PATH = os.path.join(HERE, "_build", "libsgl_check.so")
 
-_lib = None
+_libs = {}
 
 
 class SglError(RuntimeError):
@@ -29,13 +31,14 @@ class SglError(RuntimeError):
         self.status = status
 
 
-def library() -> C.CDLL:
-    """The in-tree CUDA library (raises if it was not built)."""
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
-        lib = C.CDLL(LIB_PATH)
+def library(checked: bool = False) -> C.CDLL:
+    """The in-tree CUDA library (raises if it was not built); `checked`: the
+    build with device-side bounds checks."""
+    path = LIB_CHECK_PATH if checked else LIB_PATH
+    if path not in _libs:
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        lib = C.CDLL(path)
         P = C.POINTER
         sigs = {
             "sgl_version": ([], C.c_int),
@@ -54,6 +57,7 @@ def library() -> C.CDLL:
             "sgl_render_debug": ([C.c_void_p, C.c_int, P(abi.ViewDesc), P(abi.Target), P(C.c_uint32), P(C.c_uint8),
                                   P(abi.FrameStats)], C.c_int),
             "sgl_profile": ([C.c_void_p, C.c_int], C.c_int),
+            "sgl_check_status": ([C.c_void_p, P(C.c_uint32), P(C.c_uint64), P(C.c_uint32), C.c_int], C.c_int),
             "sgl_render_batch": ([C.c_void_p, P(abi.BatchItem), C.c_int, P(abi.BatchOpts), C.c_void_p,
                                   P(abi.FrameStats)], C.c_int),
             "sgl_autotune": ([C.c_void_p, P(abi.BatchItem), C.c_int, P(abi.BatchOpts)], C.c_int),
@@ -80,15 +84,15 @@ def library() -> C.CDLL:
             fn = getattr(lib, name)
             fn.argtypes = args
             fn.restype = res
-        _lib = lib
-    return _lib
+        _libs[path] = lib
+    return _libs[path]
 
 
 class Renderer:
     """One sgl context on one CUDA device."""
 
-    def __init__(self, device: int = 0):
-        self.lib = library()
+    def __init__(self, device: int = 0, checked: bool = False):
+        self.lib = library(checked)
         h = C.c_void_p()
         st = self.lib.sgl_create(C.byref(h), device)
         if st != 0:
@@ -106,6 +110,14 @@ class Renderer:
             self.close()
         except Exception:
             pass
+
+    def check_status(self, reset: bool = False) -> dict:
+        """The device-side bounds checks' record (a Renderer on the checked
+        library): the first failure's check code and index, and the count."""
+        code, index, count = C.c_uint32(), C.c_uint64(), C.c_uint32()
+        self._check(self.lib.sgl_check_status(self.ctx, C.byref(code), C.byref(index), C.byref(count),
+                                              1 if reset else 0))
+        return {"code": code.value, "index": index.value, "count": count.value}
 
     def _check(self, st: int):
         if st != 0:
