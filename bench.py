@@ -682,6 +682,7 @@ def run_serve(args, rank, world, local_rank):
     # e2e: closed loop with every frame copied to pinned host memory
     e2e = e2e_run(r, torch, sids, timed, args)
 
+    kshares = serve_kernel_shares(r, torch, sids, timed[:args.profile_requests], args.max_batch)
     fm = frame_measure(r, torch, 10, 3, False)
     gpu_launches = int(b1["kernels"] - b0["kernels"])
     out = {
@@ -694,6 +695,7 @@ def run_serve(args, rank, world, local_rank):
         "batched_frames_per_s_same_requests": round(batched_same_fps, 2),
         "sequential_requests": n_seq,
         "latency_ms": lat,
+        "kernels": kshares,
         "batches": int(b1["batches"] - b0["batches"]),
         "frame_1080p": {"frames_per_s": round(1e3 / fm["frame_ms"], 1), "kernels": kernels_of(fm)},
         "roofline": roofline_of(fm),
@@ -710,6 +712,45 @@ def run_serve(args, rank, world, local_rank):
     if dist:
         dist.destroy_process_group()
     return out if rank == 0 else None
+
+
+def serve_kernel_shares(r, torch, sids, sample, batch: int) -> dict:
+    """Device time per kernel of the serving stream's work: the sample's
+    requests in batches of `batch` (in arrival order, as the serving loop forms
+    them at saturation), launched directly with CUDA events around each kernel
+    (sgl_profile), in microseconds per request and as shares."""
+    from swegl_gb300 import abi
+
+    if not sample:
+        return {}
+    per = max(2 * v.w * v.h for (_, _, v) in sample)
+    pool = torch.zeros(batch * per + 16, dtype=torch.int32, device="cuda")
+    base = pool.data_ptr()
+    batches = []
+    for i in range(0, len(sample), batch):
+        items, off = [], 0
+        for (_, k, v) in sample[i:i + batch]:
+            t = abi.Target()
+            t.pixels = base + 4 * off
+            t.pitch = 4 * v.w
+            t.width, t.height = v.w, v.h
+            t.zbuffer = C.cast(C.c_void_p(base + 4 * (off + v.w * v.h)), C.POINTER(C.c_float))
+            off += 2 * v.w * v.h
+            items.append((sids[k], v, t))
+        batches.append(items)
+    r.render_batch(batches[0], use_graph=False)
+    torch.cuda.synchronize()
+    r.profile(True)
+    for items in batches:
+        r.render_batch(items, use_graph=False)
+    torch.cuda.synchronize()
+    prof = r.profile_read()
+    r.profile(False)
+    total = sum(d["total_ms"] for d in prof.values()) or 1.0
+    return {"requests": len(sample), "batch": batch,
+            "per_kernel": {k: {"us_per_request": round(1e3 * d["total_ms"] / len(sample), 2),
+                               "share": round(d["total_ms"] / total, 3)}
+                           for k, d in prof.items() if d["launches"]}}
 
 
 def _retarget(tgt, v):
@@ -1013,6 +1054,7 @@ def main():
     ap.add_argument("--workload", choices=["serve", "frame", "dof", "layers", "batch64"], default="serve")
     ap.add_argument("--requests-per-step", type=int, default=4096)
     ap.add_argument("--seq-requests", type=int, default=512)
+    ap.add_argument("--profile-requests", type=int, default=512, help="serving: requests of the per-kernel profile")
     ap.add_argument("--duration", type=float, default=60.0, help="open-loop latency run, seconds")
     ap.add_argument("--ring-bytes", type=int, default=4 << 30, help="latency run: pinned host frames in flight")
     ap.add_argument("--e2e-chunk", type=int, default=256, help="e2e: requests submitted together")

@@ -219,10 +219,26 @@ __device__ __forceinline__ uint32_t sh_bilinear(const Shader &sh, float progress
                 w22 = (u2 - u) * (v2 - v);
     uint32_t c11 = sh.color, c21 = sh.color, c12 = sh.color, c22 = sh.color; // untextured: 1x1 of the colour
     if (sh.tex) {
-        c11 = __ldg(sh.tex + i11);
-        c21 = __ldg(sh.tex + i21);
-        c12 = __ldg(sh.tex + i12);
-        c22 = __ldg(sh.tex + i22);
+        // the two texels of a row are neighbours unless the column wraps: one
+        // 8-byte load when the pair starts on an even texel (textures start
+        // 256-byte aligned), else two 4-byte loads
+        const bool pair = u2m == u1m + 1;
+        if (pair && (i11 & 1) == 0) {
+            const uint2 t = __ldg(reinterpret_cast<const uint2 *>(sh.tex + i11));
+            c11 = t.x;
+            c12 = t.y;
+        } else {
+            c11 = __ldg(sh.tex + i11);
+            c12 = __ldg(sh.tex + i12);
+        }
+        if (pair && (i21 & 1) == 0) {
+            const uint2 t = __ldg(reinterpret_cast<const uint2 *>(sh.tex + i21));
+            c21 = t.x;
+            c22 = t.y;
+        } else {
+            c21 = __ldg(sh.tex + i21);
+            c22 = __ldg(sh.tex + i22);
+        }
     }
     uint32_t out = 0;
 #pragma unroll
