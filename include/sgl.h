@@ -339,9 +339,22 @@ typedef struct sgl_request_result {
 SGL_API sgl_status sgl_server_create(sgl_ctx *ctx, const sgl_serve_opts *opts, sgl_server **out);
 /* Queue a request; SGL_ERR_BUDGET when it alone exceeds the budget. */
 SGL_API sgl_status sgl_server_submit(sgl_server *srv, const sgl_request *req, uint64_t *ticket);
+/* Queue n requests in one call (each as sgl_server_submit would; a host
+ * binding through a foreign-function interface pays its call overhead once
+ * instead of per request).  tickets[i] receives request i's ticket; stops
+ * at the first request that is refused and returns its status, with
+ * *n_queued (may be NULL) the number queued before it.  No reference
+ * counterpart (the reference has no serving loop). */
+SGL_API sgl_status sgl_server_submit_batch(sgl_server *srv, const sgl_request *reqs, int n, uint64_t *tickets,
+                                           int *n_queued);
 /* SGL_OK with the result (once per ticket), SGL_ERR_BUSY while in flight. */
 SGL_API sgl_status sgl_server_poll(sgl_server *srv, uint64_t ticket, sgl_request_result *result);
 SGL_API sgl_status sgl_server_wait(sgl_server *srv, uint64_t ticket, double timeout_s, sgl_request_result *result);
+/* Wait for n tickets; results[i] (may be NULL) receives ticket i's result.
+ * SGL_ERR_TIMEOUT when they are not all done within timeout_s (the results
+ * of the tickets before the one waited for are filled and consumed). */
+SGL_API sgl_status sgl_server_wait_batch(sgl_server *srv, const uint64_t *tickets, int n, double timeout_s,
+                                         sgl_request_result *results);
 /* Wait until every submitted request is done (SGL_ERR_TIMEOUT otherwise). */
 SGL_API sgl_status sgl_server_drain(sgl_server *srv, double timeout_s);
 /* Batches and kernels launched, requests completed so far. */

@@ -381,11 +381,9 @@ SGL_API sgl_status sgl_server_create(sgl_ctx *c, const sgl_serve_opts *opts, sgl
     return SGL_OK;
 }
 
-SGL_API sgl_status sgl_server_submit(sgl_server *s, const sgl_request *req, uint64_t *ticket)
+// A request checked and turned into a job (nothing queued yet).
+static sgl_status make_job(Server *srv, const sgl_request *req, Job &j)
 {
-    Server *srv = reinterpret_cast<Server *>(s);
-    if (!srv || !req || !ticket)
-        return SGL_ERR_INVALID;
     Scene *scene = srv->ctx->find(req->scene_id);
     if (!scene)
         return SGL_ERR_NOT_FOUND;
@@ -396,7 +394,7 @@ SGL_API sgl_status sgl_server_submit(sgl_server *s, const sgl_request *req, uint
         return SGL_ERR_INVALID;
     if (v.layers > 0 && v.dof.enabled)
         return SGL_ERR_UNSUPPORTED; // depth of field on a layered view is not implemented
-    Job j{};
+    j = Job{};
     j.req = *req;
     j.scene = scene;
     j.bytes = request_bytes(scene, v);
@@ -416,17 +414,66 @@ SGL_API sgl_status sgl_server_submit(sgl_server *s, const sgl_request *req, uint
         return SGL_ERR_BUDGET;
     j.res.submit_s = now_s();
     j.res.status = SGL_ERR_BUSY;
+    return SGL_OK;
+}
+
+SGL_API sgl_status sgl_server_submit(sgl_server *s, const sgl_request *req, uint64_t *ticket)
+{
+    Server *srv = reinterpret_cast<Server *>(s);
+    if (!srv || !req || !ticket)
+        return SGL_ERR_INVALID;
+    Job j;
+    const sgl_status st = make_job(srv, req, j);
+    if (st != SGL_OK)
+        return st;
     {
         std::lock_guard<std::mutex> g(srv->mu);
         if (srv->stop)
             return SGL_ERR_INVALID;
         j.ticket = srv->next_ticket++;
-        srv->pending.push_back(j);
+        srv->pending.push_back(std::move(j));
         srv->submitted++;
+        *ticket = srv->pending.back().ticket;
     }
     srv->cv_submit.notify_one();
-    *ticket = j.ticket;
     return SGL_OK;
+}
+
+SGL_API sgl_status sgl_server_submit_batch(sgl_server *s, const sgl_request *reqs, int n, uint64_t *tickets,
+                                           int *n_queued)
+{
+    Server *srv = reinterpret_cast<Server *>(s);
+    if (n_queued)
+        *n_queued = 0;
+    if (!srv || n < 0 || (n > 0 && (!reqs || !tickets)))
+        return SGL_ERR_INVALID;
+    sgl_status st = SGL_OK;
+    int k = 0;
+    std::vector<Job> jobs;
+    jobs.reserve((size_t)n);
+    for (; k < n; k++) {
+        Job j;
+        st = make_job(srv, reqs + k, j);
+        if (st != SGL_OK)
+            break;
+        jobs.push_back(std::move(j));
+    }
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        if (srv->stop)
+            return SGL_ERR_INVALID;
+        for (size_t i = 0; i < jobs.size(); i++) {
+            jobs[i].ticket = srv->next_ticket++;
+            tickets[i] = jobs[i].ticket;
+            srv->pending.push_back(std::move(jobs[i]));
+            srv->submitted++;
+        }
+    }
+    if (k > 0)
+        srv->cv_submit.notify_one();
+    if (n_queued)
+        *n_queued = k;
+    return st;
 }
 
 SGL_API sgl_status sgl_server_poll(sgl_server *s, uint64_t ticket, sgl_request_result *result)
@@ -464,6 +511,33 @@ SGL_API sgl_status sgl_server_wait(sgl_server *s, uint64_t ticket, double timeou
         if (srv->cv_done.wait_until(lk, deadline) == std::cv_status::timeout)
             return SGL_ERR_TIMEOUT;
     }
+}
+
+SGL_API sgl_status sgl_server_wait_batch(sgl_server *s, const uint64_t *tickets, int n, double timeout_s,
+                                         sgl_request_result *results)
+{
+    Server *srv = reinterpret_cast<Server *>(s);
+    if (!srv || n < 0 || (n > 0 && !tickets))
+        return SGL_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+    for (int i = 0; i < n; i++) {
+        const uint64_t ticket = tickets[i];
+        for (;;) {
+            auto it = srv->done.find(ticket);
+            if (it != srv->done.end()) {
+                if (results)
+                    results[i] = it->second;
+                srv->done.erase(it);
+                break;
+            }
+            if (ticket == 0 || ticket >= srv->next_ticket)
+                return SGL_ERR_NOT_FOUND;
+            if (srv->cv_done.wait_until(lk, deadline) == std::cv_status::timeout)
+                return SGL_ERR_TIMEOUT;
+        }
+    }
+    return SGL_OK;
 }
 
 SGL_API sgl_status sgl_server_drain(sgl_server *s, double timeout_s)

@@ -68,6 +68,9 @@ def library(checked: bool = False) -> C.CDLL:
             "sgl_server_poll": ([C.c_void_p, C.c_uint64, P(abi.RequestResult)], C.c_int),
             "sgl_server_wait": ([C.c_void_p, C.c_uint64, C.c_double, P(abi.RequestResult)], C.c_int),
             "sgl_server_drain": ([C.c_void_p, C.c_double], C.c_int),
+            "sgl_server_submit_batch": ([C.c_void_p, P(abi.Request), C.c_int, P(C.c_uint64), P(C.c_int)], C.c_int),
+            "sgl_server_wait_batch": ([C.c_void_p, P(C.c_uint64), C.c_int, C.c_double, P(abi.RequestResult)],
+                                      C.c_int),
             "sgl_server_destroy": ([C.c_void_p], None),
             "sgl_server_stats": ([C.c_void_p, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)], C.c_int),
             "sgl_profile_read": ([C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_uint64)], C.c_int),
@@ -281,6 +284,42 @@ class Server:
             raise SglError(st, "sgl_server_submit")
         self._keep[t.value] = (host_pixels, host_zbuffer)
         return t.value
+
+    @staticmethod
+    def requests(items) -> "C.Array":
+        """An abi.Request array for submit_many: items of (scene_id, view) or
+        (scene_id, view, host_pixels, host_zbuffer), host buffers as numpy
+        arrays (the caller keeps them alive until the results)."""
+        arr = (abi.Request * len(items))()
+        for r, it in zip(arr, items):
+            r.scene_id = it[0]
+            r.view = abi.view_desc(it[1])
+            if len(it) > 2 and it[2] is not None:
+                r.host_pixels = it[2].ctypes.data_as(C.POINTER(C.c_uint32))
+            if len(it) > 3 and it[3] is not None:
+                r.host_zbuffer = it[3].ctypes.data_as(C.POINTER(C.c_float))
+        return arr
+
+    def submit_many(self, reqs) -> np.ndarray:
+        """Queue an abi.Request array (Server.requests) in one call; returns
+        the tickets."""
+        tickets = np.zeros(len(reqs), np.uint64)
+        queued = C.c_int()
+        st = self.lib.sgl_server_submit_batch(self.h, reqs, len(reqs), tickets.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                              C.byref(queued))
+        if st != 0:
+            raise SglError(st, f"sgl_server_submit_batch (queued {queued.value} of {len(reqs)})")
+        return tickets
+
+    def wait_many(self, tickets: np.ndarray, timeout_s: float = 60.0) -> "C.Array":
+        """Wait for every ticket; returns their abi.RequestResult array."""
+        tickets = np.ascontiguousarray(tickets, np.uint64)
+        res = (abi.RequestResult * len(tickets))()
+        st = self.lib.sgl_server_wait_batch(self.h, tickets.ctypes.data_as(C.POINTER(C.c_uint64)), len(tickets),
+                                            timeout_s, res)
+        if st != 0:
+            raise SglError(st, "sgl_server_wait_batch")
+        return res
 
     def _result(self, res: abi.RequestResult) -> dict:
         return {"status": res.status, "submit_s": res.submit_s, "start_s": res.start_s, "done_s": res.done_s,

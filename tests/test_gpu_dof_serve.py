@@ -169,6 +169,46 @@ def test_serving_full_size_scenes_alone_and_in_the_mix(renderer):
         renderer.release(sid)
 
 
+def test_serving_batch_submit_and_wait(renderer):
+    """sgl_server_submit_batch / sgl_server_wait_batch: one call queues a
+    list of requests (into host buffers) and one call collects them; each
+    frame equals the one-frame-per-launch render; a request the budget can
+    never hold stops the batch there, with the ones before it queued."""
+    from swegl_gb300.runtime import Server, SglError
+
+    sc = S.spheres_scene(n_spheres=9, seed=71, tex_size=128)
+    sid = renderer.upload(sc)
+    rng = S.Rng(93)
+    items, views = [], []
+    for i in range(20):
+        m, c = S.camera_on_sphere(rng, 35.0)
+        v = S.view_for(S.log_uniform_int(rng, 64, 500), S.log_uniform_int(rng, 64, 400), m, c)
+        v.dof = i % 3 == 0
+        pix = np.zeros((v.h, v.w), np.uint32)
+        z = np.zeros((v.h, v.w), np.float32)
+        items.append((sid, v, pix, z))
+        views.append(v)
+    srv = renderer.server(budget_bytes=256 << 20, max_batch=8, streams=2, copy_out=True)
+    tickets = srv.submit_many(Server.requests(items))
+    assert len(set(tickets.tolist())) == len(items)
+    res = srv.wait_many(tickets, 60.0)
+    assert all(x.status == 0 for x in res)
+    for (_, v, pix, z), x in zip(items, res):
+        alone, st = renderer.render(sid, [v], stats=True)
+        assert np.array_equal(pix, alone[0].pixels)
+        assert np.array_equal(z.view(np.uint32), alone[0].zbuffer.view(np.uint32))
+        assert x.fragments == st["fragments"] and x.submit_s <= x.start_s <= x.rendered_s <= x.done_s
+    # the third request cannot fit the budget: the first two are queued
+    big = S.cube_view(3840, 2160)
+    reqs = Server.requests([(sid, views[0]), (sid, views[1]), (sid, big), (sid, views[2])])
+    with pytest.raises(SglError) as e:
+        srv.submit_many(reqs)
+    assert e.value.status == -5 and "queued 2 of 4" in str(e.value)
+    srv.drain(60.0)
+    srv.close()
+    renderer.release(sid)
+
+
 def test_serving_budget_and_poll(renderer):
     from swegl_gb300.runtime import SglError
 
