@@ -269,6 +269,12 @@ typedef struct sgl_batch_item {
     int        scene_id;
     sgl_view   view;
     sgl_target target; /* device buffers */
+    /* Optional pose of this item alone: the scene's n_nodes node transforms
+     * to render it with (e.g. from sgl_gltf_animate at the item's time); NULL
+     * renders the scene's current nodes.  Many poses of one resident scene
+     * render in one batch; the scene's own nodes are untouched. */
+    const sgl_node_desc *nodes;
+    int        n_nodes;
 } sgl_batch_item;
 
 /* Asynchronous on `stream` unless `stats` is requested (then it waits).

@@ -85,7 +85,8 @@ class BatchOpts(C.Structure):
 
 
 class BatchItem(C.Structure):
-    _fields_ = [("scene_id", C.c_int), ("view", ViewDesc), ("target", Target)]
+    _fields_ = [("scene_id", C.c_int), ("view", ViewDesc), ("target", Target), ("nodes", C.POINTER(NodeDesc)),
+                ("n_nodes", C.c_int)]
 
 
 class ServeOpts(C.Structure):

@@ -479,6 +479,61 @@ static sgl_status batch_entries(Ctx *ctx, const sgl_batch_item *items, int n, st
     return SGL_OK;
 }
 
+// Batch items with their own pose: the node matrices composed on the host (as
+// sgl_scene_set_nodes does), then k_pose writes the item's world positions and
+// normals into the lane's pose scratch on the lane's stream, and the item's
+// entry points at them (the scene's own arrays and nodes are untouched).
+static sgl_status pose_items(Ctx *ctx, Lane *lane, const sgl_batch_item *items, int n, std::vector<BatchEntry> &e)
+{
+    std::vector<std::vector<float>> mats((size_t)n);
+    size_t total = 0;
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    for (int i = 0; i < n; i++) {
+        if (!items[i].nodes)
+            continue;
+        const Scene *s = e[i].scene;
+        if (items[i].n_nodes != (int)s->nodes.size()) {
+            ctx->fail("batch item %d: a pose gives all %zu nodes of the scene, not %d", i, s->nodes.size(),
+                      items[i].n_nodes);
+            return SGL_ERR_INVALID;
+        }
+        std::vector<sgl_node_desc> nd(items[i].nodes, items[i].nodes + items[i].n_nodes);
+        std::vector<float> world, rs;
+        if (!node_matrices(nd, world, rs)) {
+            ctx->fail("batch item %d: the pose's node hierarchy has a cycle or a bad parent index", i);
+            return SGL_ERR_INVALID;
+        }
+        mats[i] = std::move(world);
+        mats[i].insert(mats[i].end(), rs.begin(), rs.end());
+        total += up(sizeof(float) * mats[i].size()) + up(2 * sizeof(float4) * std::max<size_t>(s->n_vertices, 1));
+    }
+    if (!total)
+        return SGL_OK;
+    CUDA_TRY(lane->poses.ensure(total));
+    uint8_t *base = (uint8_t *)lane->poses.ptr;
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+        if (!items[i].nodes)
+            continue;
+        const Scene *s = e[i].scene;
+        float *m = (float *)(base + off);
+        off += up(sizeof(float) * mats[i].size());
+        float4 *wpos = (float4 *)(base + off);
+        float4 *wnrm = wpos + s->n_vertices;
+        off += up(2 * sizeof(float4) * std::max<size_t>(s->n_vertices, 1));
+        const size_t nm = mats[i].size() / 2;
+        // (from pageable memory: staged before the call returns)
+        CUDA_TRY(cudaMemcpyAsync(m, mats[i].data(), sizeof(float) * mats[i].size(), cudaMemcpyHostToDevice,
+                                 lane->stream));
+        CUDA_TRY(launch_pose(s->dev, m, m + nm, wpos, wnrm, lane->stream));
+        e[i].wpos = wpos;
+        e[i].wnrm = wnrm;
+        e[i].node_world = m;
+        e[i].node_rs = m + nm;
+    }
+    return SGL_OK;
+}
+
 SGL_API sgl_status sgl_render_batch(sgl_ctx *c, const sgl_batch_item *items, int n_items,
                                     const sgl_batch_opts *opts, void *stream, sgl_frame_stats *stats)
 {
@@ -493,6 +548,13 @@ SGL_API sgl_status sgl_render_batch(sgl_ctx *c, const sgl_batch_item *items, int
     sgl_status r = batch_entries(ctx, items, n_items, all);
     if (r != SGL_OK)
         return r;
+    Lane *lane = nullptr;
+    r = ext_lane(ctx, (cudaStream_t)stream, &lane);
+    if (r != SGL_OK)
+        return r;
+    r = pose_items(ctx, lane, items, n_items, all);
+    if (r != SGL_OK)
+        return r;
     // items with transparency layers run after the others, each as its own
     // launch sequence, in item order (the call then waits for them)
     std::vector<BatchEntry> e;
@@ -503,10 +565,6 @@ SGL_API sgl_status sgl_render_batch(sgl_ctx *c, const sgl_batch_item *items, int
         else
             e.push_back(all[i]);
     }
-    Lane *lane = nullptr;
-    r = ext_lane(ctx, (cudaStream_t)stream, &lane);
-    if (r != SGL_OK)
-        return r;
     int slot = 0, launches = 0;
     sgl_frame_stats acc{};
     if (!e.empty()) {
@@ -556,6 +614,8 @@ SGL_API sgl_status sgl_autotune(sgl_ctx *c, const sgl_batch_item *items, int n_i
         return r;
     Lane *lane = nullptr;
     r = ext_lane(ctx, ctx->stream, &lane);
+    if (r == SGL_OK)
+        r = pose_items(ctx, lane, items, n_items, e);
     if (r != SGL_OK)
         return r;
     cudaEvent_t a = nullptr, b = nullptr;

@@ -116,6 +116,7 @@ struct Lane {
     int next = 0;
     DevBuf list, recs, tall, spans, ndc, yes, key, prec, doftmp, dofz;
     DevBuf frags, frag_head, layer0; // views with transparency layers
+    DevBuf poses;                    // batch items with their own pose: node matrices, world positions, normals
     static constexpr int kBaseArrays = 10; // prefixes: vertices, triangles, pixels, tiles, dof tiles, the
                                            // general geometry pass's vertices and triangles; the fused
                                            // pass's group chunks, group items and the grouped items

@@ -190,12 +190,18 @@ class Renderer:
     # batches --------------------------------------------------------------
     def render_batch(self, items, tile: int = 0, span_bin: int = 0, use_graph: bool = True, stream: int = 0,
                      stats: bool = False):
-        """items: list of (scene_id, view, abi.Target with device pointers)."""
+        """items: list of (scene_id, view, abi.Target with device pointers)
+        or (scene_id, view, target, nodes): `nodes` an abi.NodeDesc array of
+        every node of the scene, the item's own pose."""
         arr = (abi.BatchItem * len(items))()
-        for i, (sid, v, t) in enumerate(items):
+        for i, it in enumerate(items):
+            sid, v, t = it[0], it[1], it[2]
             arr[i].scene_id = sid
             arr[i].view = abi.view_desc(v)
             arr[i].target = t
+            if len(it) > 3 and it[3] is not None:
+                arr[i].nodes = C.cast(it[3], C.POINTER(abi.NodeDesc))
+                arr[i].n_nodes = len(it[3])
         opts = abi.BatchOpts(tile, span_bin, 1 if use_graph else 0)
         fs = abi.FrameStats()
         self._check(self.lib.sgl_render_batch(self.ctx, arr, len(items), C.byref(opts), C.c_void_p(stream),

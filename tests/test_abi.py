@@ -50,7 +50,8 @@ STRUCTS = {
     "sgl_node_desc": abi.NodeDesc, "sgl_primitive_desc": abi.PrimitiveDesc, "sgl_material_desc": abi.MaterialDesc,
     "sgl_texture_desc": abi.TextureDesc, "sgl_point_light": abi.PointLight, "sgl_scene_desc": abi.SceneDesc,
     "sgl_dof_desc": abi.DofDesc, "sgl_view": abi.ViewDesc, "sgl_target": abi.Target,
-    "sgl_frame_stats": abi.FrameStats,
+    "sgl_frame_stats": abi.FrameStats, "sgl_batch_opts": abi.BatchOpts, "sgl_batch_item": abi.BatchItem,
+    "sgl_serve_opts": abi.ServeOpts, "sgl_request": abi.Request, "sgl_request_result": abi.RequestResult,
 }
 
 
@@ -59,7 +60,8 @@ def test_ctypes_layout_matches_header():
     for name in STRUCTS:
         src += f'printf("{name} %zu\\n", sizeof({name}));\n'
     src += 'printf("view.dof %zu\\n", offsetof(sgl_view, dof));\n'
-    src += 'printf("scene.default_material %zu\\n", offsetof(sgl_scene_desc, default_material));\nreturn 0;}\n'
+    src += 'printf("scene.default_material %zu\\n", offsetof(sgl_scene_desc, default_material));\n'
+    src += 'printf("batch_item.nodes %zu\\n", offsetof(sgl_batch_item, nodes));\nreturn 0;}\n'
     with tempfile.TemporaryDirectory() as d:
         c = os.path.join(d, "t.c")
         exe = os.path.join(d, "t")
@@ -71,3 +73,4 @@ def test_ctypes_layout_matches_header():
         assert int(sizes[name]) == C.sizeof(cls), name
     assert int(sizes["view.dof"]) == abi.ViewDesc.dof.offset
     assert int(sizes["scene.default_material"]) == abi.SceneDesc.default_material.offset
+    assert int(sizes["batch_item.nodes"]) == abi.BatchItem.nodes.offset

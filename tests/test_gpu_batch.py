@@ -1,6 +1,7 @@
 """The batched renderer (one launch sequence / one CUDA graph for many views of
 uneven size, over several resident scenes) produces exactly the frames of the
 plain one-frame-per-launch renderer, for every tile and span-bin choice."""
+import copy
 import ctypes as C
 
 import numpy as np
@@ -242,3 +243,56 @@ def test_batch_of_every_pixel_shader(rig, use_graph):
             d = np.abs(pix.view(np.uint8).astype(np.int16) - ref.pixels.view(np.uint8).astype(np.int16))
             assert int(d.max()) <= 2, (abi.SHADERS[mode], int(d.max()))
     r.release(sid)
+
+
+@pytest.mark.parametrize("make", ["spheres", "grid"])
+def test_posed_items_equal_the_scene_set_to_each_pose(rig, make):
+    """sgl_batch_item.nodes: several poses of one resident scene in one batch
+    (each item's own node transforms), mixed with items that render the
+    scene's current nodes.  Every item equals sgl_render of a second copy of
+    the scene set to that item's pose (sgl_scene_set_nodes), bit for bit;
+    the batched scene's own nodes are unchanged.  The spheres scene (200
+    nodes) takes the fused geometry pass, where items are grouped by the
+    vertex data they read; the floor takes the general one."""
+    r, torch = rig
+    rng = np.random.default_rng(23)
+    if make == "spheres":
+        base = S.spheres_scene(n_spheres=60, tex_size=128)
+        views = [S.spheres_view(480, 270) for _ in range(6)]
+    else:
+        base = S.grid_scene()
+        m, c = S.look_at((0.3, 3.0, 7.0), (0.0, -0.5, 0.0))
+        views = [S.view_for(400, 300, m, c) for _ in range(6)]
+    n = len(base.node_parent)
+    sid, check = r.upload(base), r.upload(base)
+    rest = abi.SceneDescHolder(base).nodes
+    poses = []
+    for k in range(4):
+        sc = copy.deepcopy(base)
+        for i in range(n):
+            sc.node_translation[i] = (np.asarray(sc.node_translation[i], np.float32)
+                                      + rng.uniform(-0.6, 0.6, 3).astype(np.float32))
+        poses.append(abi.SceneDescHolder(sc).nodes)
+    plan = [poses[0], None, poses[1], poses[2], None, poses[3]]
+    bufs, tgts = device_targets(torch, views)
+    r.render_batch([(sid, v, t, p) for v, t, p in zip(views, tgts, plan)])
+    torch.cuda.synchronize()
+    got = frames_of(bufs)
+    for i, (v, p) in enumerate(zip(views, plan)):
+        assert r.lib.sgl_scene_set_nodes(r.ctx, check, p if p is not None else rest, n) == 0
+        exp, _ = r.render(check, [v])
+        assert np.array_equal(got[i][0], exp[0].pixels), f"item {i}: colour"
+        assert np.array_equal(got[i][1].view(np.uint32), exp[0].zbuffer.view(np.uint32)), f"item {i}: depth"
+        if p is not None:
+            assert not np.array_equal(got[i][1], got[1][1]), f"item {i}: the pose changed nothing"
+    # the batched scene still renders its own nodes
+    a, _ = r.render(sid, [views[1]])
+    assert np.array_equal(a[0].pixels, got[1][0])
+    # a pose must give every node of the scene
+    short = (abi.NodeDesc * max(1, n - 1))()
+    from swegl_gb300.runtime import SglError
+    with pytest.raises(SglError) as e:
+        r.render_batch([(sid, views[0], tgts[0], short)])
+    assert e.value.status == -1
+    r.release(sid)
+    r.release(check)
