@@ -1092,13 +1092,24 @@ __device__ __forceinline__ void row_span(RowIn &r, int vx, int vw, RowSpan &o)
 }
 
 // The qpixel interpolator of a span after its displacement to x1, and the
-// progress of both edges (renderer.cpp:474-480, prepare_for_scanline).
-__device__ __forceinline__ void span_interp(const RowSpan &o, Interp &q, float &pl, float &pr)
+// progress of both edges (renderer.cpp:474-480, prepare_for_scanline).  With
+// `steps` > 0 the interpolator is also stepped that many pixels: top and
+// bottom take every addition of the reference's per-pixel steps, and alpha,
+// which each step recomputes from them alone, is divided out once at the end
+// (the same value as the last step's).
+__device__ __forceinline__ void span_interp(const RowSpan &o, Interp &q, float &pl, float &pr, int steps = 0)
 {
     pl = o.Lt / o.Lb;
     pr = o.Rt / o.Rb;
     q.init_self(o.Rx - o.Lx, o.Lz + o.Ldv * pl, o.Rz + o.Rdv * pr);
-    q.displace((float)o.x1 - o.Lx);
+    const float move = (float)o.x1 - o.Lx;
+    q.top = q.top + q.tstep * move; // Interp::displace without its division
+    q.bottom = q.bottom + q.bstep * move;
+    for (int k = 0; k < steps; k++) {
+        q.top = q.top + q.tstep;
+        q.bottom = q.bottom + q.bstep;
+    }
+    q.alpha = q.top / q.bottom;
 }
 
 // Bins the spans of the lanes that ask for it (one atomic per warp).  Every
@@ -1888,9 +1899,7 @@ __device__ __forceinline__ bool rec_replay(const TriRec *rp, const ViewDev &v, i
         return false;
     Interp it;
     float pl, pr;
-    span_interp(sp, it, pl, pr);
-    for (int x = sp.x1; x < X; x++)
-        it.step();
+    span_interp(sp, it, pl, pr, X - sp.x1);
     out = make_float4(it.alpha, pl, pr, __uint_as_float(r.bits));
     return true;
 }
@@ -2080,13 +2089,12 @@ __device__ __forceinline__ uint32_t dof_average(uint32_t centre, uint32_t sb, ui
 // A block takes kDofTile x kDofTile tiles of the items that ask for the
 // gather and stages the tile with its halo (the taps reach at most
 // ceil(max_radius) pixels: every tap component is below 1), clamped to the
-// view as the taps are, in shared memory; the 32 taps of each pixel then read
-// shared memory without further clamping.  Views whose reach exceeds
+// view as the taps are, in shared memory (rows kDofPitch apart); the 32 taps
+// of each pixel then read shared memory without further clamping.  Views whose reach exceeds
 // kDofMaxHalo gather from the colour buffer.
 __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
 {
-    constexpr int S_MAX = kDofTile + 2 * kDofMaxHalo;
-    __shared__ uint32_t halo[S_MAX * S_MAX];
+    __shared__ uint32_t halo[kDofPitch * kDofPitch];
     int item = -1;
     uint32_t lo = 0, hi = 0;
     for (uint32_t tg = blockIdx.x; tg < b->total_dof_tiles; tg += gridDim.x) {
@@ -2117,7 +2125,7 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                 int sy = y0 - R + yy;
                 sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
                 const uint32_t *row = it.pixels + (size_t)sy * it.pitch_px;
-                uint32_t *dst = halo + yy * S;
+                uint32_t *dst = halo + yy * kDofPitch;
                 if (lane < S) {
                     const uint32_t v = __ldg(row + c0);
                     dst[lane] = v;
@@ -2147,45 +2155,92 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                 continue;
             }
         }
-        for (int p = threadIdx.x; p < kDofTile * kDofTile; p += blockDim.x) {
-            // a warp takes one row of 32 pixels of the tile
-            const int x = x0 + (p & (kDofTile - 1)), y = y0 + p / kDofTile;
-            if (y >= h)
-                continue; // the whole warp
+        if (R >= 0) {
+            // Warp w takes rows w, w + 8, w + 16 and w + 24 of the tile, a lane
+            // one column.  The sums are exact integers, so the taps may be
+            // taken in any order: rb holds red and blue in two 16-bit lanes,
+            // g the green byte in place (32 x 255 x 256 fits), alpha is the
+            // centre's.
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            const int x = x0 + lane;
             const bool valid = x < w;
             const int xs = valid ? x : x0; // lanes past the view's right edge work on a pixel inside
-            const uint32_t i = (uint32_t)y * (uint32_t)w + (uint32_t)xs;
-            const float r = dof_radius(it, i);
-            uint32_t out;
-            if (R >= 0) {
-                // the halo holds the view-clamped pixels, so a tap needs no clamp:
-                // |offset| <= ceil(r) <= R keeps it inside
-                const uint32_t *c = halo + (y - y0 + R) * S + (xs - x0 + R);
-                uint32_t br = 0, ga = 0; // two 16-bit lanes each: 32 taps x 255 fit
-                const float r0 = __shfl_sync(0xFFFFFFFFu, r, 0);
-                if (__all_sync(0xFFFFFFFFu, !valid || r == r0)) {
-                    // one radius for the warp (the clamped radius, or the empty
-                    // background's): lane k makes tap k's offset once
+            if (y0 + warp < h) {
+                float r[4];
+                bool uniform = true;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int y = y0 + warp + 8 * j;
+                    r[j] = y < h ? dof_radius(it, (uint32_t)y * (uint32_t)w + (uint32_t)xs) : 0.0f;
+                }
+                const float r0 = __shfl_sync(0xFFFFFFFFu, r[0], 0);
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    uniform &= !valid || y0 + warp + 8 * j >= h || r[j] == r0;
+                // the halo holds the view-clamped pixels, so a tap needs no
+                // clamp: |offset| <= ceil(r) <= R keeps it inside
+                const uint32_t *c = halo + (warp + R) * kDofPitch + (xs - x0 + R);
+                uint32_t rb[4] = {0u, 0u, 0u, 0u}, g[4] = {0u, 0u, 0u, 0u};
+                if (__all_sync(0xFFFFFFFFu, uniform)) {
+                    // one radius for the warp's 128 pixels (the clamped radius,
+                    // or the empty background's): lane k makes tap k's offset
+                    // once, and each offset serves the four rows
                     static_assert(SGL_DOF_TAPS == 32, "one tap per lane");
-                    const float2 t = c_dof_taps[threadIdx.x & 31];
-                    const int off = __float2int_rn(r0 * t.y) * S + __float2int_rn(r0 * t.x);
-#pragma unroll 8
+                    const float2 t = c_dof_taps[lane];
+                    const int off = __float2int_rn(r0 * t.y) * kDofPitch + __float2int_rn(r0 * t.x);
+#pragma unroll 4
                     for (int k = 0; k < SGL_DOF_TAPS; k++) {
-                        const uint32_t v = c[__shfl_sync(0xFFFFFFFFu, off, k)];
-                        br += v & 0x00FF00FFu;
-                        ga += (v >> 8) & 0x00FF00FFu;
+                        const uint32_t *q = c + __shfl_sync(0xFFFFFFFFu, off, k);
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const uint32_t v = q[8 * j * kDofPitch];
+                            rb[j] += v & 0x00FF00FFu;
+                            g[j] += v & 0x0000FF00u;
+                        }
                     }
                 } else {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        if (y0 + warp + 8 * j >= h)
+                            break; // the whole warp
+                        const uint32_t *cj = c + 8 * j * kDofPitch;
+                        const float rj0 = __shfl_sync(0xFFFFFFFFu, r[j], 0);
+                        if (__all_sync(0xFFFFFFFFu, !valid || r[j] == rj0)) {
+                            const float2 t = c_dof_taps[lane];
+                            const int off = __float2int_rn(rj0 * t.y) * kDofPitch + __float2int_rn(rj0 * t.x);
 #pragma unroll 8
-                    for (int k = 0; k < SGL_DOF_TAPS; k++) {
-                        const float2 t = c_dof_taps[k];
-                        const uint32_t v = c[__float2int_rn(r * t.y) * S + __float2int_rn(r * t.x)];
-                        br += v & 0x00FF00FFu;
-                        ga += (v >> 8) & 0x00FF00FFu;
+                            for (int k = 0; k < SGL_DOF_TAPS; k++) {
+                                const uint32_t v = cj[__shfl_sync(0xFFFFFFFFu, off, k)];
+                                rb[j] += v & 0x00FF00FFu;
+                                g[j] += v & 0x0000FF00u;
+                            }
+                        } else {
+#pragma unroll 8
+                            for (int k = 0; k < SGL_DOF_TAPS; k++) {
+                                const float2 t = c_dof_taps[k];
+                                const uint32_t v = cj[__float2int_rn(r[j] * t.y) * kDofPitch + __float2int_rn(r[j] * t.x)];
+                                rb[j] += v & 0x00FF00FFu;
+                                g[j] += v & 0x0000FF00u;
+                            }
+                        }
                     }
                 }
-                out = dof_average(c[0], br & 0xFFFFu, ga & 0xFFFFu, br >> 16);
-            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int y = y0 + warp + 8 * j;
+                    if (valid && y < h)
+                        it.dof_out[(size_t)y * it.dof_pitch + x] =
+                            dof_average(c[8 * j * kDofPitch], rb[j] & 0xFFFFu, g[j] >> 8, rb[j] >> 16);
+                }
+            }
+        } else {
+            for (int p = threadIdx.x; p < kDofTile * kDofTile; p += blockDim.x) {
+                const int x = x0 + (p & (kDofTile - 1)), y = y0 + p / kDofTile;
+                if (y >= h)
+                    continue; // the whole warp
+                const bool valid = x < w;
+                const int xs = valid ? x : x0;
+                const float r = dof_radius(it, (uint32_t)y * (uint32_t)w + (uint32_t)xs);
                 uint32_t sb = 0, sg = 0, sr = 0;
 #pragma unroll 8
                 for (int k = 0; k < SGL_DOF_TAPS; k++) {
@@ -2198,10 +2253,10 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                     sg += (v >> 8) & 0xFFu;
                     sr += (v >> 16) & 0xFFu;
                 }
-                out = dof_average(it.pixels[(size_t)y * it.pitch_px + xs], sb, sg, sr);
+                if (valid)
+                    it.dof_out[(size_t)y * it.dof_pitch + x] =
+                        dof_average(it.pixels[(size_t)y * it.pitch_px + xs], sb, sg, sr);
             }
-            if (valid)
-                it.dof_out[(size_t)y * it.dof_pitch + x] = out;
         }
         if (R >= 0)
             __syncthreads(); // the halo is reused by the next tile

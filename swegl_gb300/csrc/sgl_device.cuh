@@ -51,20 +51,20 @@ struct V2 {
     float x, y;
 };
 
-__device__ __forceinline__ V3 mk3(float x, float y, float z) { return V3{x, y, z}; }
-__device__ __forceinline__ V3 add3(V3 a, V3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ V3 sub3(V3 a, V3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ V3 mul3(V3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ V3 neg3(V3 a) { return mk3(-a.x, -a.y, -a.z); }
+__host__ __device__ __forceinline__ V3 mk3(float x, float y, float z) { return V3{x, y, z}; }
+__host__ __device__ __forceinline__ V3 add3(V3 a, V3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ V3 sub3(V3 a, V3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ V3 mul3(V3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ V3 neg3(V3 a) { return mk3(-a.x, -a.y, -a.z); }
 // vector_t::dot (swegl/projection/points.hpp:91-94)
-__device__ __forceinline__ float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ V2 mk2(float x, float y) { return V2{x, y}; }
 __device__ __forceinline__ V2 add2(V2 a, V2 b) { return mk2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ V2 sub2(V2 a, V2 b) { return mk2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ V2 mul2(V2 a, float s) { return mk2(a.x * s, a.y * s); }
 
 // vector_t::normalize (swegl/projection/points.hpp:71-90)
-__device__ __forceinline__ V3 normalize3(V3 v)
+__host__ __device__ __forceinline__ V3 normalize3(V3 v)
 {
     float l = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
     if (l != 0.0f) {
@@ -160,48 +160,46 @@ struct Side {
     float x;
 };
 
-// Float-float helpers for the specular power.  The reference evaluates
-// pow((double)s, p) and rounds to float (src/render/pixel_shaders.cpp:193);
-// s^p is formed here by binary exponentiation on (hi, lo) float pairs with
-// exact products (error-free transformations built on fmaf), ~44 bits of
-// precision, then rounded to float.
-struct FF {
-    float hi, lo;
-};
-__device__ __forceinline__ FF ff_two_prod(float a, float b)
+// s^p for the specular term.  The reference evaluates pow((double)s, p) and
+// rounds it to float (src/render/pixel_shaders.cpp:193).  Here s^p is formed
+// by left-to-right binary exponentiation on a pair of floats hi + lo holding
+// about 46 bits: a square takes hi * hi, its exact rounding error from one
+// fused multiply-add (Dekker's exact product, "A floating-point technique for
+// extending the available precision", 1971), and the cross term 2 * hi * lo
+// added to that error by one more fused multiply-add (lo * lo, below 2^-46 of
+// the value, is dropped); the pair is then renormalised (Dekker's fast two-
+// sum).  A multiply by s takes hi * s, its exact error, and lo * s added to
+// the error by a fused multiply-add, unnormalised (|lo| stays within a few
+// units in the last place of hi).  The pair is rounded to float once at the
+// end: the float nearest s^p unless s^p lies within about p * 2^-45 of its
+// value from a rounding boundary.  Shininess is 0..1024 (checked at upload).
+__host__ __device__ __forceinline__ int top_bit(int p)
 {
-    float p = a * b;
-    float e = fmaf(a, b, -p);
-    return FF{p, e};
+#ifdef __CUDA_ARCH__
+    return 31 - __clz(p);
+#else
+    return 31 - __builtin_clz((unsigned)p);
+#endif
 }
-__device__ __forceinline__ FF ff_fast_two_sum(float a, float b)
+__host__ __device__ __forceinline__ float spec_pow(float s, int p)
 {
-    float s = a + b;
-    float e = b - (s - a);
-    return FF{s, e};
-}
-__device__ __forceinline__ FF ff_mul(FF a, FF b)
-{
-    FF p = ff_two_prod(a.hi, b.hi);
-    float cross = fmaf(a.hi, b.lo, a.lo * b.hi);
-    return ff_fast_two_sum(p.hi, p.lo + cross);
-}
-__device__ __forceinline__ float spec_pow(float s, int p)
-{
-    FF base{s, 0.0f};
-    FF acc{1.0f, 0.0f};
-    bool first = true;
-    while (p > 0) {
-        if (p & 1) {
-            acc = first ? base : ff_mul(acc, base);
-            first = false;
+    if (p <= 0)
+        return 1.0f;
+    float hi = s, lo = 0.0f;
+    for (int bit = top_bit(p) - 1; bit >= 0; bit--) {
+        const float sq = hi * hi;
+        const float err = fmaf(hi, hi, -sq);
+        const float low = fmaf(hi + hi, lo, err);
+        hi = sq + low;
+        lo = low - (hi - sq);
+        if ((p >> bit) & 1) {
+            const float m = hi * s;
+            const float em = fmaf(hi, s, -m);
+            lo = fmaf(lo, s, em);
+            hi = m;
         }
-        p >>= 1;
-        if (p)
-            base = ff_mul(base, base);
     }
-    // round the pair to the nearest float
-    return acc.hi + acc.lo;
+    return hi + lo;
 }
 
 } // namespace sgl

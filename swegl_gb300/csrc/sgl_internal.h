@@ -146,6 +146,9 @@ constexpr uint8_t kYesBehind = 2; // its z' is below the near plane (fill_triang
 // kDofMaxHalo pixels staged in shared memory.
 constexpr int kDofTile = 32;
 constexpr int kDofMaxHalo = 32;
+// Row pitch of the staged tile in shared memory, the same for every halo so
+// that the rows of a tap are constant offsets apart.
+constexpr int kDofPitch = kDofTile + 2 * kDofMaxHalo;
 
 // The tap reach of a depth-of-field view: ceil(max_radius) when it fits the
 // staged halo, else -1 (the gather then reads the colour buffer directly).

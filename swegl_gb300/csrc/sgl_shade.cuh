@@ -111,7 +111,22 @@ __device__ __forceinline__ void sh_prepare_scanline(Shader &sh, float pl, float 
 // The sun and point-light sum of the Phong and the flat light shaders
 // (src/render/pixel_shaders.cpp:159-205 per pixel, :33-84 per triangle): the
 // same expressions at a point with a normal.
-__device__ __forceinline__ float light_sum(const LightsDev &L, V3 center, V3 normal, V3 camvec, int shininess)
+//
+// A point light whose direction the reference would find behind the surface
+// (alignment < 0, the light skipped) is skipped here before its division and
+// normalisation when the unnormalised dot product already shows it with a
+// margin that rounding cannot cross: with a_i = n_i * d_i (d = center minus
+// the light), the float sum of the a_i is within 3 * 2^-24 * sum |a_i| of the
+// exact dot product, and the reference's dot product of n with the
+// normalised d (three IEEE divisions by the same length, three products, two
+// sums) is within 2^-22 * sum |a_i| / length of the exact one divided by
+// that length.  A float sum above 2^-20 * sum |a_i| therefore makes both
+// positive, and the reference skips the light too (its test on the
+// intensity / distance^2 ratio only skips more).  Sums below 2^-100 (where
+// products could be subnormal), squared distances from 2^100 up (where the
+// length could overflow) and NaNs take the full path.
+__host__ __device__ __forceinline__ float light_sum(const LightsDev &L, V3 center, V3 normal, V3 camvec,
+                                                    int shininess)
 {
     float face_sun = -dot3(normal, mk3(L.sun[0], L.sun[1], L.sun[2]));
     if (face_sun < 0.0f)
@@ -123,6 +138,10 @@ __device__ __forceinline__ float light_sum(const LightsDev &L, V3 center, V3 nor
         const float4 pl = L.pl[l];
         V3 ld = sub3(center, mk3(pl.x, pl.y, pl.z));
         const float d2 = ld.x * ld.x + ld.y * ld.y + ld.z * ld.z;
+        const float ax = normal.x * ld.x, ay = normal.y * ld.y, az = normal.z * ld.z;
+        const float mag = fabsf(ax) + fabsf(ay) + fabsf(az);
+        if (ax + ay + az > 0x1p-20f * mag && mag > 0x1p-100f && d2 < 0x1p100f)
+            continue; // behind the surface
         float diffuse = pl.w / d2;
         if (diffuse < 0.05f) // (double)diffuse < 0.05, see sgl_device.cuh
             continue;
