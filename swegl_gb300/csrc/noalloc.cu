@@ -189,6 +189,9 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     off += up256(8 * px);
     const size_t o_prec = off;
     off += up256(16 * px);
+    const bool win_list = px >= kWinListMinPixels; // the shade goes through a winner list
+    const size_t o_wins = off;
+    off += win_list ? up256(8 * px) : 0;
     const size_t o_list = off;
     off += up256(8 * (nt ? nt : 1));
     const size_t o_recs = off;
@@ -283,6 +286,8 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     b.recs = (TriRec *)(base + o_recs);
     b.tall = (uint32_t *)(base + o_tall);
     b.keep_keys = 0;
+    b.key_pool = (unsigned long long *)(base + o_key);
+    b.wins = win_list ? (uint2 *)(base + o_wins) : nullptr;
     b.spans = (SpanRec *)(base + o_spans);
     b.span_cap = span_cap;
     b.counters = (unsigned long long *)(base + o_counters);
@@ -297,7 +302,7 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     CUDA_TRY(cudaMemsetAsync(base + o_key, 0xFF, 8 * px, st)); // kEmptyKey
 
     const int seq = (dof ? kSeqDof : 0) | (v.shader != SGL_SHADER_PHONG_BILINEAR ? kSeqShaders : 0) |
-                    (fused ? kSeqFused : kSeqSplit);
+                    (fused ? kSeqFused : kSeqSplit) | (win_list ? kSeqWinList : 0);
     CUDA_TRY(launch_batch((const BatchDev *)(base + o_batch), tile, seq, st, nullptr, nullptr));
     return SGL_OK;
 }

@@ -2057,6 +2057,115 @@ __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade(c
     }
 }
 
+// The same per-pixel work for a batch of one large view (kSeqWinList), in
+// two passes.  k_classify streams the batch's depth keys (one contiguous pool
+// in batch pixel order, kClassifyPx keys per thread in flight): empty pixels
+// get the background colour and depth at once; a winner gets its depth, its
+// key is reset to empty (unless kept for debug), and it is appended to the
+// winner list in pixel order, with one atomic per block pass.  k_shade_wins
+// then shades one winner per thread, without tiles or barriers.
+constexpr int kClassifyPx = 8; // pixels per thread and block pass
+
+__global__ void __launch_bounds__(256) k_classify(const BatchDev *b)
+{
+    __shared__ uint32_t at[kClassifyPx * 8]; // per (pass row j, warp): winners, then their first list index
+    __shared__ uint32_t base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool keep = b->keep_keys != 0;
+    const uint32_t total = b->total_px;
+    int item = -1;
+    uint32_t lo = 0, hi = 0;
+    for (uint32_t c0 = blockIdx.x * (256u * kClassifyPx); c0 < total; c0 += gridDim.x * (256u * kClassifyPx)) {
+        unsigned long long k[kClassifyPx];
+#pragma unroll
+        for (int j = 0; j < kClassifyPx; j++) {
+            const uint32_t g = c0 + j * 256u + threadIdx.x;
+            k[j] = g < total ? b->key_pool[g] : kEmptyKey;
+        }
+        unsigned m[kClassifyPx];
+#pragma unroll
+        for (int j = 0; j < kClassifyPx; j++) {
+            const uint32_t g = c0 + j * 256u + threadIdx.x;
+            bool win = false;
+            if (g < total) {
+                if (g < lo || g >= hi) {
+                    item = find_item(b->px_base, b->n_items, g);
+                    lo = __ldg(b->px_base + item);
+                    hi = __ldg(b->px_base + item + 1);
+                }
+                const ItemDev &it = b->items[item];
+                const uint32_t i = g - lo, w = (uint32_t)it.v.w;
+                const uint32_t y = i / w, x = i - y * w;
+                if (k[j] == kEmptyKey) {
+                    it.pixels[(long long)y * it.pitch_px + x] = 0u;
+                    if (it.zbuf)
+                        it.zbuf[i] = __uint_as_float(kMaxZBits);
+                } else {
+                    win = true;
+                    if (it.zbuf)
+                        it.zbuf[i] = __uint_as_float((uint32_t)(k[j] >> 32));
+                    if (!keep)
+                        b->key_pool[g] = kEmptyKey;
+                }
+            }
+            m[j] = __ballot_sync(0xFFFFFFFFu, win);
+            if (lane == 0)
+                at[j * 8 + warp] = __popc(m[j]);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            // exclusive prefix of the 64 counts in (j, warp) order, which is pixel order
+            const uint32_t a0 = at[2 * lane], a1 = at[2 * lane + 1];
+            uint32_t incl = a0 + a1;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+                if (lane >= d)
+                    incl += t;
+            }
+            const uint32_t excl = incl - (a0 + a1);
+            at[2 * lane] = excl;
+            at[2 * lane + 1] = excl + a0;
+            if (lane == 31)
+                base = incl ? atomicAdd(counter32(b, C_WINS), incl) : 0u;
+        }
+        __syncthreads();
+        const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+        for (int j = 0; j < kClassifyPx; j++)
+            if (m[j] & (1u << lane)) {
+                const uint32_t g = c0 + j * 256u + threadIdx.x;
+                const uint32_t e = base + at[j * 8 + warp] + __popc(m[j] & below);
+                if (in_bounds(e < total, CHK_PIXEL, e))
+                    b->wins[e] = make_uint2(g, (uint32_t)k[j]);
+            }
+        __syncthreads(); // `at` and `base` are reused by the next pass
+    }
+}
+
+template <bool ALL_MODES>
+__global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade_wins(const BatchDev *b)
+{
+    const uint32_t n = *counter32(b, C_WINS);
+    const bool overflow = *counter32(b, C_OVERFLOW) != 0u;
+    int item = -1;
+    uint32_t lo = 0, hi = 0;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const uint2 wn = b->wins[e];
+        if (wn.x < lo || wn.x >= hi) {
+            item = find_item(b->px_base, b->n_items, wn.x);
+            lo = __ldg(b->px_base + item);
+            hi = __ldg(b->px_base + item + 1);
+        }
+        const ItemDev &it = b->items[item];
+        const uint32_t i = wn.x - lo;
+        const uint32_t c = shade_winner_impl<ALL_MODES>(b, (uint32_t)item, i, wn.y, overflow);
+        const uint32_t y = i / (uint32_t)it.v.w, x = i - y * (uint32_t)it.v.w;
+        if (in_bounds(y < (uint32_t)it.v.h, CHK_PIXEL, i))
+            it.pixels[(long long)y * it.pitch_px + x] = c;
+    }
+}
+
 // ------------------------------------------------------------ depth of field --
 
 __constant__ float2 c_dof_taps[SGL_DOF_TAPS];
@@ -2158,8 +2267,10 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
         if (R >= 0) {
             // Warp w takes rows w, w + 8, w + 16 and w + 24 of the tile, a lane
             // one column.  The sums are exact integers, so the taps may be
-            // taken in any order: rb holds red and blue in two 16-bit lanes,
-            // g the green byte in place (32 x 255 x 256 fits), alpha is the
+            // taken in any order: rb sums bytes 0 and 2 in two 16-bit lanes
+            // (32 x 255 fits), g sums whole pixels modulo 2^32, so that bits
+            // 8..23 of g - rb are the sum of byte 1 (below 2^24 after the
+            // shift: byte 3's sum lands at bit 24 and up); alpha is the
             // centre's.
             const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
             const int x = x0 + lane;
@@ -2195,7 +2306,7 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                         for (int j = 0; j < 4; j++) {
                             const uint32_t v = q[8 * j * kDofPitch];
                             rb[j] += v & 0x00FF00FFu;
-                            g[j] += v & 0x0000FF00u;
+                            g[j] += v;
                         }
                     }
                 } else {
@@ -2212,7 +2323,7 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                             for (int k = 0; k < SGL_DOF_TAPS; k++) {
                                 const uint32_t v = cj[__shfl_sync(0xFFFFFFFFu, off, k)];
                                 rb[j] += v & 0x00FF00FFu;
-                                g[j] += v & 0x0000FF00u;
+                                g[j] += v;
                             }
                         } else {
 #pragma unroll 8
@@ -2220,7 +2331,7 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                                 const float2 t = c_dof_taps[k];
                                 const uint32_t v = cj[__float2int_rn(r[j] * t.y) * kDofPitch + __float2int_rn(r[j] * t.x)];
                                 rb[j] += v & 0x00FF00FFu;
-                                g[j] += v & 0x0000FF00u;
+                                g[j] += v;
                             }
                         }
                     }
@@ -2230,7 +2341,8 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                     const int y = y0 + warp + 8 * j;
                     if (valid && y < h)
                         it.dof_out[(size_t)y * it.dof_pitch + x] =
-                            dof_average(c[8 * j * kDofPitch], rb[j] & 0xFFFFu, g[j] >> 8, rb[j] >> 16);
+                            dof_average(c[8 * j * kDofPitch], rb[j] & 0xFFFFu, ((g[j] - rb[j]) >> 8) & 0xFFFFu,
+                                        rb[j] >> 16);
                 }
             }
         } else {
@@ -2882,7 +2994,14 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
     // the kernel with every pixel shader only when a view asks for another
     // than the default, which then keeps all the registers
     const unsigned sg = sms * SGL_SHADE_MIN_BLOCKS;
-    if (flags & kSeqShaders) {
+    if (flags & kSeqWinList) {
+        k_classify<<<sms * 8, 256, 0, st>>>(b);
+        if (flags & kSeqShaders)
+            k_shade_wins<true><<<sg, kShadeThreads, 0, st>>>(b);
+        else
+            k_shade_wins<false><<<sg, kShadeThreads, 0, st>>>(b);
+        n++;
+    } else if (flags & kSeqShaders) {
         if (tile == 8)
             k_shade<8, true><<<sg, kShadeThreads, 0, st>>>(b);
         else if (tile == 32)

@@ -214,7 +214,7 @@ static_assert(offsetof(TriRec, flags) == 4 * kRecFlagsWord, "TriRec::flags word"
 
 // Batch counters (32-bit words); the drawn-triangle and fragment counts are
 // kept per item (item_counters) and summed by the host.
-enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_FRAGS = 8, C_TALL = 10 };
+enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_FRAGS = 8, C_TALL = 10, C_WINS = 12 };
 // Work queues of the shade kernel's tiles: kQueues counters, one per 128-byte
 // line so that blocks of different queues do not contend.
 constexpr int kQueues = 16;
@@ -249,6 +249,8 @@ struct BatchDev {
                                // triangle, or flags kRecClip for a near-clipped one (others: stale)
     uint32_t *tall;            // batch triangles of the tall set-ups (list_cap entries)
     int keep_keys;             // leave the depth keys for the caller (debug); else the shade resets them
+    unsigned long long *key_pool; // the items' depth keys: batch pixel px_base[item] + i at key_pool[...]
+    uint2 *wins;               // kSeqWinList: pixels with a winner {batch pixel, draw slot}, in pixel order
     SpanRec *spans;            // long-span bins
     uint32_t span_cap;
     unsigned long long *counters;      // kCounterWords words
@@ -294,8 +296,15 @@ cudaError_t launch_pose(const SceneDev &s, const float *node_world, const float 
 // (C_FRAGS <= frag_cap) for the outputs to be written, else they are left
 // untouched and the host renders again with a bigger pool.
 // kSeqFused: items of fused scenes (k_geom); kSeqSplit: other items (k_vertex,
-// k_flags, k_compact).
-constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqLayers = 4, kSeqFused = 8, kSeqSplit = 16, kSeqVariants = 32;
+// k_flags, k_compact).  kSeqWinList shades through a winner list (k_classify
+// then k_shade_wins, for a batch of one large view) instead of the tiled
+// k_shade; BatchDev::wins must then hold total_px entries.
+constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqLayers = 4, kSeqFused = 8, kSeqSplit = 16, kSeqWinList = 32,
+              kSeqVariants = 64;
+// A batch of one view of at least this many pixels shades through the winner
+// list: the tiled shade's per-tile key reads and barriers then cost more than
+// the list's second kernel and its round trip through L2.
+constexpr uint64_t kWinListMinPixels = 1u << 20;
 cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st, int *launches, Profiler *prof);
 // The device-side bounds checks of the checked build (-DSGL_BOUNDS_CHECK):
 // the first failure's check code and index and the failure count, cleared

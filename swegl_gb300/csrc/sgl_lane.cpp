@@ -42,6 +42,7 @@ size_t view_scratch_bytes(uint32_t n_vertices, uint32_t n_triangles, int w, int 
 {
     const size_t px = (size_t)w * h;
     return align_up(16 * (size_t)n_vertices, 256) + align_up(n_vertices, 256) + 8 * px + 16 * px  // ndc yes key prec
+           + (px >= kWinListMinPixels ? 8 * px : 0)                                               // winner list
            + (8 + sizeof(TriRec) + 8) * (size_t)n_triangles + sizeof(SpanRec) * (px / 8 + 64)      // lists, set-ups, bins
            + 8 * px;                                                                               // dof colour, depth
 }
@@ -198,6 +199,10 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         keys_dirty = false;
     }
     CUDA_TRY(prec.ensure(sizeof(float4) * std::max<uint64_t>(tp, 1)));
+    // one large view: the shade goes through a winner list
+    const bool win_list = n == 1 && tp >= kWinListMinPixels && e[0].view.layers == 0;
+    if (win_list)
+        CUDA_TRY(wins.ensure(sizeof(uint2) * tp));
     CUDA_TRY(list.ensure(sizeof(uint2) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(recs.ensure(sizeof(TriRec) * std::max<uint64_t>(tt, 1)));
     CUDA_TRY(tall.ensure(sizeof(uint32_t) * std::max<uint64_t>(tt, 1)));
@@ -207,7 +212,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         if (dofz_px)
             CUDA_TRY(dofz.ensure(4 * dofz_px));
     }
-    int seq_flags = geom_flags;
+    int seq_flags = geom_flags | (win_list ? kSeqWinList : 0);
     int layers = 0;
     for (int i = 0; i < n; i++)
         layers = std::max(layers, e[i].view.layers);
@@ -307,6 +312,8 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     bd.recs = (TriRec *)recs.ptr;
     bd.tall = (uint32_t *)tall.ptr;
     bd.keep_keys = slot_flags != nullptr; // debug renders read the keys back
+    bd.key_pool = (unsigned long long *)key.ptr;
+    bd.wins = win_list ? (uint2 *)wins.ptr : nullptr;
     sl.keep_keys = bd.keep_keys != 0;
     bd.spans = (SpanRec *)spans.ptr;
     bd.span_cap = (uint32_t)std::min<size_t>(spans.bytes / sizeof(SpanRec), 0xFFFFFFFFu);

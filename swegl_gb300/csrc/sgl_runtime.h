@@ -114,7 +114,7 @@ struct Lane {
         bool keep_keys = false;
     } slots[kSlots];
     int next = 0;
-    DevBuf list, recs, tall, spans, ndc, yes, key, prec, doftmp, dofz;
+    DevBuf list, recs, tall, spans, ndc, yes, key, prec, wins, doftmp, dofz;
     DevBuf frags, frag_head, layer0; // views with transparency layers
     DevBuf poses;                    // batch items with their own pose: node matrices, world positions, normals
     static constexpr int kBaseArrays = 10; // prefixes: vertices, triangles, pixels, tiles, dof tiles, the

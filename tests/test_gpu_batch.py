@@ -296,3 +296,29 @@ def test_posed_items_equal_the_scene_set_to_each_pose(rig, make):
     assert e.value.status == -1
     r.release(sid)
     r.release(check)
+
+
+def test_winner_list_shade_equals_tiled_shade(rig):
+    """A batch of one view of a million pixels or more shades through a winner
+    list (k_classify, then k_shade_wins); other batches shade in tiles
+    (k_shade).  The same 1920x1080 view, with and without depth of field, as
+    a batch of one (winner list) and as two items of one batch (tiled): the
+    frames are equal bit for bit, and equal to the plain renderer's."""
+    r, torch = rig
+    sc = S.spheres_scene()
+    sid = r.upload(sc)
+    for dof in (False, True):
+        v = S.spheres_view(1920, 1080)
+        v.dof = dof
+        one_bufs, one_tgts = device_targets(torch, [v])
+        r.render_batch([(sid, v, one_tgts[0])])
+        two_bufs, two_tgts = device_targets(torch, [v, v])
+        r.render_batch([(sid, v, t) for t in two_tgts])
+        torch.cuda.synchronize()
+        one, two = frames_of(one_bufs), frames_of(two_bufs)
+        plain, _ = r.render(sid, [v])
+        for got in (one[0], two[0], two[1]):
+            assert np.array_equal(got[0], plain[0].pixels), dof
+            assert np.array_equal(got[1].view(np.uint32), plain[0].zbuffer.view(np.uint32)), dof
+        assert int((one[0][1] < 1e30).sum()) > 100000  # the view shows the scene
+    r.release(sid)

@@ -100,7 +100,8 @@ def test_noalloc_general_geometry_near_clip_and_span_overflow():
     # wide, so most rows are long spans.  Find the tallest 1920-wide view the
     # static array accepts (refusals happen on the host, before any device
     # work): its span capacity is then within one row's scratch (24 B per
-    # pixel) of the minimum of 4,096 records.
+    # pixel, 32 B for views of a million pixels or more, which shade through
+    # a winner list) of the minimum of 4,096 records.
     m, c = S.look_at((0.3, 3.0, 7.0), (0.0, -0.5, 0.0))
     w = 1920
     _, _, t_probe = _target(torch, w, 4096)
