@@ -2068,6 +2068,7 @@ constexpr int kClassifyPx = 8; // pixels per thread and block pass
 
 __global__ void __launch_bounds__(256) k_classify(const BatchDev *b)
 {
+    static_assert(kClassifyPx % 4 == 0, "the counts divide among the scan warp's lanes");
     __shared__ uint32_t at[kClassifyPx * 8]; // per (pass row j, warp): winners, then their first list index
     __shared__ uint32_t base;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -2114,18 +2115,28 @@ __global__ void __launch_bounds__(256) k_classify(const BatchDev *b)
         }
         __syncthreads();
         if (warp == 0) {
-            // exclusive prefix of the 64 counts in (j, warp) order, which is pixel order
-            const uint32_t a0 = at[2 * lane], a1 = at[2 * lane + 1];
-            uint32_t incl = a0 + a1;
+            // exclusive prefix of the counts in (j, warp) order, which is pixel
+            // order: each lane takes kPerLane consecutive counts
+            constexpr int kPerLane = kClassifyPx * 8 / 32;
+            uint32_t a[kPerLane], sum = 0;
+#pragma unroll
+            for (int q = 0; q < kPerLane; q++) {
+                a[q] = at[kPerLane * lane + q];
+                sum += a[q];
+            }
+            uint32_t incl = sum;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
                 const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
                 if (lane >= d)
                     incl += t;
             }
-            const uint32_t excl = incl - (a0 + a1);
-            at[2 * lane] = excl;
-            at[2 * lane + 1] = excl + a0;
+            uint32_t run = incl - sum;
+#pragma unroll
+            for (int q = 0; q < kPerLane; q++) {
+                at[kPerLane * lane + q] = run;
+                run += a[q];
+            }
             if (lane == 31)
                 base = incl ? atomicAdd(counter32(b, C_WINS), incl) : 0u;
         }
@@ -2201,12 +2212,23 @@ __device__ __forceinline__ uint32_t dof_average(uint32_t centre, uint32_t sb, ui
 // view as the taps are, in shared memory (rows kDofPitch apart); the 32 taps
 // of each pixel then read shared memory without further clamping.  Views whose reach exceeds
 // kDofMaxHalo gather from the colour buffer.
-__global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
+constexpr int kDofBlocks = 5; // resident blocks per SM (shared memory: 37 KB each)
+
+__global__ void __launch_bounds__(256, kDofBlocks) k_dof(const BatchDev *b)
 {
     __shared__ uint32_t halo[kDofPitch * kDofPitch];
+    __shared__ uint32_t claim[2]; // this tile and the next (tiles cost from a copy to a full gather)
     int item = -1;
     uint32_t lo = 0, hi = 0;
-    for (uint32_t tg = blockIdx.x; tg < b->total_dof_tiles; tg += gridDim.x) {
+    if (threadIdx.x == 0)
+        claim[0] = atomicAdd(counter32(b, C_DOF_NEXT), 1u);
+    __syncthreads();
+    for (int cb = 0;; cb ^= 1) {
+        const uint32_t tg = claim[cb];
+        if (tg >= b->total_dof_tiles)
+            break;
+        if (threadIdx.x == 0)
+            claim[cb ^ 1] = atomicAdd(counter32(b, C_DOF_NEXT), 1u);
         if (tg < lo || tg >= hi) {
             item = find_item(b->dof_base, b->n_items, tg);
             lo = __ldg(b->dof_base + item);
@@ -2260,7 +2282,7 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                     if (x < w && y < h)
                         it.dof_out[(size_t)y * it.dof_pitch + x] = ref;
                 }
-                __syncthreads(); // the halo is reused by the next tile
+                __syncthreads(); // the halo is reused by the next tile, claim[cb ^ 1] is written
                 continue;
             }
         }
@@ -2370,8 +2392,7 @@ __global__ void __launch_bounds__(256) k_dof(const BatchDev *b)
                         dof_average(it.pixels[(size_t)y * it.pitch_px + xs], sb, sg, sr);
             }
         }
-        if (R >= 0)
-            __syncthreads(); // the halo is reused by the next tile
+        __syncthreads(); // the halo is reused by the next tile, claim[cb ^ 1] is written
     }
 }
 
@@ -2898,7 +2919,7 @@ cudaError_t check_status(unsigned *code, unsigned long long *index, unsigned *co
 
 cudaError_t launch_dof(const BatchDev *b, cudaStream_t st)
 {
-    k_dof<<<sm_count() * 8, 256, 0, st>>>(b);
+    k_dof<<<sm_count() * kDofBlocks, 256, 0, st>>>(b);
     return cudaGetLastError();
 }
 
@@ -3020,7 +3041,7 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
     n++;
     mark(PK_DOF);
     if (flags & kSeqDof) {
-        k_dof<<<sms * 8, 256, 0, st>>>(b);
+        k_dof<<<sms * kDofBlocks, 256, 0, st>>>(b);
         ran(PK_DOF);
         n++;
     }

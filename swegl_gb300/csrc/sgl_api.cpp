@@ -713,13 +713,15 @@ SGL_API sgl_status sgl_dof(sgl_ctx *c, const sgl_view *view, const sgl_target *i
     it.dof_halo = dof_halo_of(v.dof.max_radius);
     it.dof_tiles_x = (v.w + kDofTile - 1) / kDofTile;
     const uint32_t dof_tiles = (uint32_t)it.dof_tiles_x * (uint32_t)((v.h + kDofTile - 1) / kDofTile);
-    CUDA_TRY(ctx->dof_desc.ensure(sizeof(ItemDev) + sizeof(BatchDev) + 4 * sizeof(uint32_t)));
+    const size_t counters_at = (sizeof(ItemDev) + sizeof(BatchDev) + 4 * sizeof(uint32_t) + 15) & ~(size_t)15;
+    CUDA_TRY(ctx->dof_desc.ensure(counters_at + sizeof(unsigned long long) * kCounterWords));
     uint8_t *dd = (uint8_t *)ctx->dof_desc.ptr;
     ItemDev *d_it = (ItemDev *)dd;
     BatchDev *d_b = (BatchDev *)(dd + sizeof(ItemDev));
     uint32_t *d_base = (uint32_t *)(dd + sizeof(ItemDev) + sizeof(BatchDev));
     BatchDev b{};
     b.items = d_it;
+    b.counters = (unsigned long long *)(dd + counters_at); // the gather's tile counter
     b.px_base = d_base;
     b.dof_base = d_base + 2;
     b.n_items = 1;
@@ -729,6 +731,7 @@ SGL_API sgl_status sgl_dof(sgl_ctx *c, const sgl_view *view, const sgl_target *i
     CUDA_TRY(cudaMemcpyAsync(d_it, &it, sizeof it, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_b, &b, sizeof b, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_base, base, sizeof base, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(b.counters, 0, sizeof(unsigned long long) * kCounterWords, st));
     CUDA_TRY(launch_dof(d_b, st));
     if (!device_buffers) {
         CUDA_TRY(cudaMemcpy2DAsync((uint8_t *)out->pixels + (size_t)v.y * out->pitch + 4 * (size_t)v.x, out->pitch,

@@ -214,7 +214,7 @@ static_assert(offsetof(TriRec, flags) == 4 * kRecFlagsWord, "TriRec::flags word"
 
 // Batch counters (32-bit words); the drawn-triangle and fragment counts are
 // kept per item (item_counters) and summed by the host.
-enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_FRAGS = 8, C_TALL = 10, C_WINS = 12 };
+enum { C_LIST = 4, C_CLIP = 5, C_SPANS = 6, C_OVERFLOW = 7, C_FRAGS = 8, C_TALL = 10, C_WINS = 12, C_DOF_NEXT = 14 };
 // Work queues of the shade kernel's tiles: kQueues counters, one per 128-byte
 // line so that blocks of different queues do not contend.
 constexpr int kQueues = 16;
