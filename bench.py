@@ -696,11 +696,14 @@ def run_serve(args, rank, world, local_rank):
     batched_same_fps = n_seq / (e0.elapsed_time(e1) / 1e3)
 
     srv.close()
+    # e2e: closed loop with every frame copied to pinned host memory.  It runs
+    # before the open-loop latency leg: after that leg's minute of deliveries
+    # into a pinned ring, copy-out throughput on the same box measured lower
+    # for later allocations, in this process and in later ones
+    e2e = e2e_run(r, torch, sids, timed, args)
+
     # open-loop latency at the Poisson arrival times, frames delivered to the host
     lat = latency_run(r, torch, sids, args.duration, 70 + rank, args)
-
-    # e2e: closed loop with every frame copied to pinned host memory
-    e2e = e2e_run(r, torch, sids, timed, args)
 
     kshares = serve_kernel_shares(r, torch, sids, timed[:args.profile_requests], args.max_batch)
     fm = frame_measure(r, torch, 10, 3, False)

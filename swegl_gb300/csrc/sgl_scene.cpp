@@ -43,9 +43,25 @@ cudaError_t DevBuf::ensure(size_t need)
 {
     if (need <= bytes && ptr)
         return cudaSuccess;
+    // A first allocation takes what is asked (scene arrays are allocated once).
+    // A buffer that has to grow — a scratch pool meeting a larger batch —
+    // takes half again its size, in 2 MB steps, so that a stream of batches of
+    // varying size reallocates rarely: each reallocation frees the old block,
+    // and cudaFree waits for the whole device, every stream included.
+    const size_t want = std::max<size_t>(need, 256);
+    size_t n = want;
+    if (ptr) {
+        constexpr size_t kStep = 2u << 20;
+        n = std::max(n, bytes + bytes / 2);
+        n = (n + kStep - 1) / kStep * kStep;
+    }
     release();
-    size_t n = std::max<size_t>(need, 256);
     cudaError_t e = cudaMalloc(&ptr, n);
+    if (e != cudaSuccess && n > want) {
+        cudaGetLastError(); // no room for the headroom: take what is needed
+        n = want;
+        e = cudaMalloc(&ptr, n);
+    }
     if (e != cudaSuccess) {
         ptr = nullptr;
         return e;
