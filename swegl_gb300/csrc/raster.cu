@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(256) k_flags(const BatchDev *b)
         if (!inside_frustum(a, c1, c2))
             return;
         // front facing, else double sided (the material is read only then)
-        bool vis = cross_n_z(sub3(c1, a), sub3(c2, a)) > 0.0f;
+        bool vis = cross_z_positive(sub3(c1, a), sub3(c2, a));
         if (!vis) {
             const int m = prims[tri.w].material;
             vis = m >= 0 && m < n_mats && mats[m].double_sided;
@@ -633,7 +633,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32, kGeomBlocks) k_geom(const Bat
                         const V3 a = mk3(pos[3 * ia], pos[3 * ia + 1], pos[3 * ia + 2]);
                         const V3 c1v = mk3(pos[3 * ib], pos[3 * ib + 1], pos[3 * ib + 2]);
                         const V3 c2v = mk3(pos[3 * ic], pos[3 * ic + 1], pos[3 * ic + 2]);
-                        if (inside_frustum(a, c1v, c2v) && (ds || cross_n_z(sub3(c1v, a), sub3(c2v, a)) > 0.0f)) {
+                        if (inside_frustum(a, c1v, c2v) && (ds || cross_z_positive(sub3(c1v, a), sub3(c2v, a)))) {
                             sy[ia] = kYesDrawn | (below_near(a.z) ? kYesBehind : 0);
                             sy[ib] = kYesDrawn | (below_near(c1v.z) ? kYesBehind : 0);
                             sy[ic] = kYesDrawn | (below_near(c2v.z) ? kYesBehind : 0);
@@ -1240,7 +1240,7 @@ __device__ __forceinline__ bool tri_setup(const BatchDev *b, uint32_t r, uint32_
     const ViewDev &v = it.v;
     const uint4 tri = it.s.tris[t];
     V3 a = load_vp(it, tri.x), c1 = load_vp(it, tri.y), c2 = load_vp(it, tri.z);
-    const bool ffv = cross_n_z(sub3(c1, a), sub3(c2, a)) < 0.0f;
+    const bool ffv = cross_z_negative(sub3(c1, a), sub3(c2, a));
     int pa = 0, pb = 1, pc = 2;
     sort_z_desc(a, c1, c2, pa, pb, pc);
     sort_y_asc(a, c1, c2, pa, pb, pc);
@@ -1632,7 +1632,7 @@ __device__ __forceinline__ void clip_triangle(const ItemDev &it, uint32_t t, Emi
     const float *rs = it.s.node_rs + 16 * it.s.prims[tri.w].node;
     const ViewDev &v = it.v;
     const TV *a = &tv[0], *b = &tv[1], *c = &tv[2], *tp;
-    bool ffv = cross_n_z(sub3(b->vp, a->vp), sub3(c->vp, a->vp)) < 0.0f;
+    bool ffv = cross_z_negative(sub3(b->vp, a->vp), sub3(c->vp, a->vp));
     bool inverted_order = false;
     if (b->vp.z > a->vp.z) { tp = a; a = b; b = tp; inverted_order = !inverted_order; }
     if (c->vp.z > b->vp.z) { tp = b; b = c; c = tp; inverted_order = !inverted_order; }
@@ -1644,7 +1644,7 @@ __device__ __forceinline__ void clip_triangle(const ItemDev &it, uint32_t t, Emi
         TV n1, n2;
         clip_vertex(v, n1, *a, *b, (v0.z - 0.001f) / (v0.z - v1.z), rs);
         clip_vertex(v, n2, *a, *c, (v0.z - 0.001f) / (v0.z - v2.z), rs);
-        ffv = cross_n_z(sub3(n1.vp, v0), sub3(n2.vp, v0)) < 0.0f;
+        ffv = cross_z_negative(sub3(n1.vp, v0), sub3(n2.vp, v0));
         if (inverted_order)
             ffv = !ffv;
         emit(2 * t, *a, n1, n2, ffv);
@@ -1652,11 +1652,11 @@ __device__ __forceinline__ void clip_triangle(const ItemDev &it, uint32_t t, Emi
         TV n1, n2;
         clip_vertex(v, n1, *a, *c, (v0.z - 0.001f) / (v0.z - v2.z), rs);
         clip_vertex(v, n2, *b, *c, (v1.z - 0.001f) / (v1.z - v2.z), rs);
-        ffv = cross_n_z(sub3(v1, v0), sub3(n2.vp, v0)) < 0.0f;
+        ffv = cross_z_negative(sub3(v1, v0), sub3(n2.vp, v0));
         if (inverted_order)
             ffv = !ffv;
         emit(2 * t, *a, *b, n2, ffv);
-        ffv = cross_n_z(sub3(n2.vp, v0), sub3(n1.vp, v0)) < 0.0f;
+        ffv = cross_z_negative(sub3(n2.vp, v0), sub3(n1.vp, v0));
         if (inverted_order)
             ffv = !ffv;
         emit(2 * t + 1, *a, n2, n1, ffv);

@@ -81,14 +81,36 @@ __device__ __forceinline__ V3 cross_n(V3 a, V3 b)
     return normalize3(mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x));
 }
 
-// cross(a, b).z() of the normalised cross product (points.cpp:32-37) without
-// the two divisions whose results are discarded: normalize() divides each
-// component by the same length independently.
-__device__ __forceinline__ float cross_n_z(V3 a, V3 b)
+// cross(a, b).z() > 0 for the normalised cross product (points.cpp:32-37;
+// front_face_visible, renderer.cpp:72-75): normalize() divides each
+// component by the same length l = sqrt(x^2 + y^2 + z^2), so only z / l is
+// needed, and only its sign.  z <= 0 (or NaN) gives z / l <= 0 (or NaN).
+// For z >= 2^-80 with a finite sum of squares, l is at most sqrt(FLT_MAX) <
+// 2^64, so z / l >= 2^-144 rounds to a positive float (or l = 0, and
+// normalize() leaves z, positive); only smaller z or an infinite or NaN sum
+// take the reference's expression.
+__host__ __device__ __forceinline__ bool cross_z_positive(V3 a, V3 b)
 {
     const float x = a.y * b.z - a.z * b.y, y = a.z * b.x - a.x * b.z, z = a.x * b.y - a.y * b.x;
-    const float l = sqrtf(x * x + y * y + z * z);
-    return l != 0.0f ? z / l : z;
+    if (!(z > 0.0f))
+        return false;
+    const float s = x * x + y * y + z * z;
+    if (z >= 0x1p-80f && s <= 3.40282347e38f)
+        return true;
+    const float l = sqrtf(s);
+    return (l != 0.0f ? z / l : z) > 0.0f;
+}
+// cross(a, b).z() < 0 for the normalised cross product, by the same argument.
+__host__ __device__ __forceinline__ bool cross_z_negative(V3 a, V3 b)
+{
+    const float x = a.y * b.z - a.z * b.y, y = a.z * b.x - a.x * b.z, z = a.x * b.y - a.y * b.x;
+    if (!(z < 0.0f))
+        return false;
+    const float s = x * x + y * y + z * z;
+    if (z <= -0x1p-80f && s <= 3.40282347e38f)
+        return true;
+    const float l = sqrtf(s);
+    return (l != 0.0f ? z / l : z) < 0.0f;
 }
 
 // transform(vertex, m): rows 0-2 only (src/projection/points.cpp:8-13)

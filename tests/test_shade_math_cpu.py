@@ -11,7 +11,12 @@ seeded inputs:
 * sgl::light_sum, which skips lights clearly behind the surface before their
   division and normalisation, against the reference's loop taking every light
   through every step (src/render/pixel_shaders.cpp:159-205): equal bit for
-  bit, including lights placed almost in the surface's tangent plane."""
+  bit, including lights placed almost in the surface's tangent plane.
+* sgl::cross_z_positive / cross_z_negative, the back-face and front-face
+  tests, which decide the sign of the normalised cross product's z without
+  its square root and division where that is provably the same, against the
+  reference's normalised expression (src/projection/points.cpp:32-37), on
+  ordinary, tiny, huge, subnormal, infinite and NaN edge vectors."""
 import os
 import shutil
 import subprocess
@@ -36,7 +41,7 @@ def _build(tmp, name):
 @pytest.fixture(scope="module")
 def exes(tmp_path_factory):
     tmp = tmp_path_factory.mktemp("shade_math")
-    return {n: _build(tmp, n) for n in ("spec_pow_host", "light_sum_host")}
+    return {n: _build(tmp, n) for n in ("spec_pow_host", "light_sum_host", "cross_sign_host")}
 
 
 @pytest.mark.parametrize("pmax, allowed", [(128, 2e-6), (1024, 1e-5)])
@@ -54,3 +59,9 @@ def test_light_sum_skips_only_lights_the_reference_skips(exes):
     assert diff == 0, f"{diff} of {cases} light sums differ from the reference's loop"
     assert early > cases  # about half of the four lights per case are skipped early
     assert tangent == cases // 2
+
+
+def test_cross_sign_matches_normalised_cross(exes):
+    r = subprocess.run([exes["cross_sign_host"], "2000000"], capture_output=True, text=True, check=True)
+    cases, diff = map(int, r.stdout.split())
+    assert cases == 2000000 and diff == 0, f"{diff} of {cases} sign tests differ from the normalised cross product"
