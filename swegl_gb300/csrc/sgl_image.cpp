@@ -471,12 +471,16 @@ bool decode_png(const uint8_t *d, size_t size, Image &out, std::string &err)
 
 // ------------------------------------------------------------------ JPEG --
 //
-// Baseline and extended sequential Huffman JPEG (ITU T.81 / JFIF), decoded
-// the way libjpeg's default decompression (which read_jpeg_file uses) does
-// it: the accurate integer IDCT (the Loeffler-Ligtenberg-Moschytz flow graph
-// in 13-bit fixed point, two passes, columns then rows), "fancy" triangle
-// upsampling of subsampled chroma, and fixed-point YCbCr -> RGB with 16
-// fraction bits.  Progressive and arithmetic-coded files are errors.
+// Baseline, extended sequential and progressive Huffman JPEG (ITU T.81 /
+// JFIF), decoded the way libjpeg's default decompression (which
+// read_jpeg_file uses) does it: the accurate integer IDCT (the
+// Loeffler-Ligtenberg-Moschytz flow graph in 13-bit fixed point, two passes,
+// columns then rows), "fancy" triangle upsampling of subsampled chroma, and
+// fixed-point YCbCr -> RGB with 16 fraction bits.  A progressive file's scans
+// (spectral selection and successive approximation, T.81 Annex G) fill the
+// same coefficient store that a sequential scan fills at once; the pixels
+// are then made the same way.  Lossless, hierarchical and arithmetic-coded
+// files are errors.
 
 namespace {
 
@@ -791,7 +795,7 @@ bool decode_jpeg(const uint8_t *d, size_t size, Image &out, std::string &err)
     JHuff dc[4], ac[4];
     std::vector<JComp> comps;
     int width = 0, height = 0, hmax = 1, vmax = 1, restart = 0;
-    bool frame = false, adobe = false, jfif = false, scanned = false;
+    bool frame = false, adobe = false, jfif = false, scanned = false, progressive = false;
     int adobe_transform = -1;
     size_t p = 2;
     while (p + 4 <= size) {
@@ -834,7 +838,10 @@ bool decode_jpeg(const uint8_t *d, size_t size, Image &out, std::string &err)
                 jhuff_build(tc ? ac[th] : dc[th], b + k + 1, b + k + 17, total);
                 k += 17 + (size_t)total;
             }
-        } else if (m == 0xC0 || m == 0xC1) { // SOF0 / SOF1: sequential, Huffman
+        } else if (m == 0xC0 || m == 0xC1 || m == 0xC2) { // SOF0 / SOF1 / SOF2: sequential or progressive, Huffman
+            if (frame)
+                return fail(err, "JPEG: second frame header");
+            progressive = m == 0xC2;
             if (n < 6 || b[0] != 8)
                 return fail(err, "JPEG: only 8-bit samples are decoded");
             height = (b[1] << 8) | b[2];
@@ -865,8 +872,8 @@ bool decode_jpeg(const uint8_t *d, size_t size, Image &out, std::string &err)
                 c.coef.assign((size_t)c.bw * c.bh * 64, 0);
             }
             frame = true;
-        } else if (m >= 0xC2 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) {
-            return fail(err, "JPEG: progressive, lossless or arithmetic-coded files are not decoded");
+        } else if (m >= 0xC3 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) {
+            return fail(err, "JPEG: lossless, hierarchical or arithmetic-coded files are not decoded");
         } else if (m == 0xDD) { // DRI
             if (n < 2)
                 return fail(err, "JPEG: bad DRI");
@@ -882,6 +889,16 @@ bool decode_jpeg(const uint8_t *d, size_t size, Image &out, std::string &err)
             const int ns = b[0];
             if (ns < 1 || ns > 4 || n < 1 + 2 * (size_t)ns + 3)
                 return fail(err, "JPEG: bad scan header");
+            // spectral selection and successive approximation (sequential: 0, 63, 0, 0)
+            const int ss = b[1 + 2 * ns], se = b[2 + 2 * ns], ah = b[3 + 2 * ns] >> 4, al = b[3 + 2 * ns] & 15;
+            if (progressive) {
+                // a DC scan has Ss = Se = 0; an AC scan holds one component and a band within 1..63
+                const bool ok = ss == 0 ? se == 0 : (ns == 1 && ss <= se && se <= 63);
+                if (!ok || al > 13 || ah > 13 || (ah && ah != al + 1))
+                    return fail(err, "JPEG: bad progressive scan parameters");
+            } else if (ss != 0 || se != 63 || ah != 0 || al != 0) {
+                return fail(err, "JPEG: bad scan parameters for a sequential frame");
+            }
             std::vector<JComp *> sc;
             for (int k = 0; k < ns; k++) {
                 const int cid = b[1 + 2 * k];
@@ -893,7 +910,12 @@ bool decode_jpeg(const uint8_t *d, size_t size, Image &out, std::string &err)
                     return fail(err, "JPEG: scan names an unknown component");
                 c->td = b[2 + 2 * k] >> 4;
                 c->ta = b[2 + 2 * k] & 15;
-                if (c->td > 3 || c->ta > 3 || !dc[c->td].present || !ac[c->ta].present || !have_qt[c->tq])
+                // the Huffman tables a scan codes with: DC for a first DC scan, AC
+                // for an AC scan, both for a sequential one (a DC refinement scan
+                // sends raw bits only)
+                const bool need_dc = !progressive || (ss == 0 && ah == 0), need_ac = !progressive || ss > 0;
+                if (c->td > 3 || c->ta > 3 || (need_dc && !dc[c->td].present) || (need_ac && !ac[c->ta].present) ||
+                    !have_qt[c->tq])
                     return fail(err, "JPEG: scan uses a missing table");
                 c->pred = 0;
                 sc.push_back(c);
@@ -925,6 +947,107 @@ bool decode_jpeg(const uint8_t *d, size_t size, Image &out, std::string &err)
                 }
                 return true;
             };
+            // progressive scans (T.81 G.1.2): the end-of-band run carries over
+            // from block to block within a scan
+            int eobrun = 0;
+            const int p1 = 1 << al, m1 = -(1 << al);
+            auto refine = [&](int16_t &coefv) { // a correction bit for a coefficient already nonzero
+                if (bits.bit() && (coefv & p1) == 0)
+                    coefv = (int16_t)(coefv + (coefv >= 0 ? p1 : m1));
+            };
+            auto pblock = [&](JComp &c, int bx, int by) {
+                int16_t *co = &c.coef[((size_t)by * c.bw + bx) * 64];
+                if (ss == 0) {
+                    if (ah == 0) { // DC, first pass: the difference of the point-transformed values
+                        const int t = jdecode(bits, dc[c.td]);
+                        if (t < 0 || t > 11)
+                            return false;
+                        c.pred += t ? jextend(bits.bits(t), t) : 0;
+                        co[0] = (int16_t)(c.pred * (1 << al));
+                    } else if (bits.bit()) { // DC, refinement: one more bit
+                        co[0] = (int16_t)(co[0] | p1);
+                    }
+                    return true;
+                }
+                if (ah == 0) { // AC, first pass over the band
+                    if (eobrun > 0) {
+                        eobrun--;
+                        return true;
+                    }
+                    for (int k = ss; k <= se;) {
+                        const int rs = jdecode(bits, ac[c.ta]);
+                        if (rs < 0)
+                            return false;
+                        const int r = rs >> 4, s2 = rs & 15;
+                        if (s2) {
+                            k += r;
+                            if (k > se)
+                                return false;
+                            co[kZigzag[k]] = (int16_t)(jextend(bits.bits(s2), s2) * (1 << al));
+                            k++;
+                        } else if (r == 15) {
+                            k += 16;
+                        } else { // an end-of-band run of 2^r + r more bits blocks, this one included
+                            eobrun = (1 << r) - 1;
+                            if (r)
+                                eobrun += bits.bits(r);
+                            break;
+                        }
+                    }
+                    return true;
+                }
+                // AC, refinement: newly nonzero coefficients (magnitude 1 at bit
+                // al) and a correction bit for every coefficient of the band that
+                // was already nonzero, sent where the decoder passes over it
+                int k = ss;
+                if (eobrun == 0) {
+                    for (; k <= se; k++) {
+                        const int rs = jdecode(bits, ac[c.ta]);
+                        if (rs < 0)
+                            return false;
+                        int r = rs >> 4;
+                        const int s2 = rs & 15;
+                        int val = 0;
+                        if (s2) {
+                            if (s2 != 1)
+                                return false;
+                            val = bits.bit() ? p1 : m1;
+                        } else if (r != 15) { // end of band here and in the run's next blocks
+                            eobrun = 1 << r;
+                            if (r)
+                                eobrun += bits.bits(r);
+                            break;
+                        }
+                        // skip r zero coefficients (refining the nonzero ones on the way),
+                        // then place the new one; a zero run of 16 places nothing
+                        for (; k <= se; k++) {
+                            int16_t &cv = co[kZigzag[k]];
+                            if (cv != 0) {
+                                refine(cv);
+                            } else {
+                                if (r == 0)
+                                    break;
+                                r--;
+                            }
+                        }
+                        if (val) {
+                            if (k > se)
+                                return false;
+                            co[kZigzag[k]] = (int16_t)val;
+                        }
+                    }
+                }
+                if (eobrun > 0) { // the rest of the band: correction bits only
+                    for (; k <= se; k++) {
+                        int16_t &cv = co[kZigzag[k]];
+                        if (cv != 0)
+                            refine(cv);
+                    }
+                    eobrun--;
+                }
+                return true;
+            };
+            auto unit = [&](JComp &c, int bx, int by) { return progressive ? pblock(c, bx, by) : block(c, bx, by); };
             int units_x, units_y;
             if (ns == 1) {
                 units_x = (sc[0]->dw + 7) / 8;
@@ -941,16 +1064,17 @@ bool decode_jpeg(const uint8_t *d, size_t size, Image &out, std::string &err)
                             return fail(err, "JPEG: missing restart marker");
                         for (JComp *c : sc)
                             c->pred = 0;
+                        eobrun = 0;
                         todo = restart;
                     }
                     if (ns == 1) {
-                        if (!block(*sc[0], mx, my))
+                        if (!unit(*sc[0], mx, my))
                             return fail(err, "JPEG: corrupt entropy-coded data");
                     } else {
                         for (JComp *c : sc)
                             for (int v = 0; v < c->v; v++)
                                 for (int h = 0; h < c->h; h++)
-                                    if (!block(*c, mx * c->h + h, my * c->v + v))
+                                    if (!unit(*c, mx * c->h + h, my * c->v + v))
                                         return fail(err, "JPEG: corrupt entropy-coded data");
                     }
                     todo--;

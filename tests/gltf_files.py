@@ -385,13 +385,10 @@ def _cat(v: int) -> int:
     return 0 if v == 0 else int(abs(v)).bit_length()
 
 
-def encode_jpeg(rgb: np.ndarray, sampling=(2, 2), quality: int = 80, restart: int = 0, grey: bool = False,
-                interleaved: bool = True):
-    """A baseline JPEG of an (h, w, 3) uint8 image: JFIF YCbCr, luma sampled
-    `sampling` (h, v) times the chroma, float DCT, scaled standard-shaped
-    quantisers, per-file Huffman tables, optional restart interval and
-    separate scans per component.  Returns (bytes, info) with the quantised
-    coefficients of every block (natural order) for checking."""
+def _jpeg_coefficients(rgb: np.ndarray, sampling, quality: int, grey: bool):
+    """The quantised DCT coefficients of an (h, w, 3) uint8 image as a JFIF
+    encoder makes them: YCbCr, luma sampled `sampling` (h, v) times the
+    chroma, float DCT, scaled standard-shaped quantisers."""
     h, w, _ = rgb.shape
     f = rgb.astype(np.float64)
     y = 0.299 * f[..., 0] + 0.587 * f[..., 1] + 0.114 * f[..., 2]
@@ -422,6 +419,31 @@ def encode_jpeg(rgb: np.ndarray, sampling=(2, 2), quality: int = 80, restart: in
         qt = qts[0 if k == 0 else 1]
         qc = np.round(coef / qt).astype(np.int64)
         comps.append(dict(id=k + 1, h=ch, v=cv, tq=0 if k == 0 else 1, coef=qc, bw=bw, bh=bh, dw=dw, dh=dh))
+    return dict(h=h, w=w, comps=comps, qts=qts, hmax=hmax, vmax=vmax, mcux=mcux, mcuy=mcuy)
+
+
+def _jpeg_header(out: bytearray, cf: dict, sof_marker: int, ntab: int):
+    """SOI, JFIF, quantisation tables and the frame header."""
+    out += b"\xff\xd8"
+    out += b"\xff\xe0" + struct.pack(">H", 16) + b"JFIF\0" + bytes([1, 1, 0, 0, 1, 0, 1, 0, 0])
+    for t in range(ntab):
+        out += b"\xff\xdb" + struct.pack(">H", 67) + bytes([t]) + bytes(cf["qts"][t].reshape(-1)[ZIGZAG].astype(np.uint8))
+    sof = bytes([8]) + struct.pack(">HH", cf["h"], cf["w"]) + bytes([len(cf["comps"])])
+    for c in cf["comps"]:
+        sof += bytes([c["id"], (c["h"] << 4) | c["v"], c["tq"]])
+    out += bytes([0xFF, sof_marker]) + struct.pack(">H", 2 + len(sof)) + sof
+
+
+def encode_jpeg(rgb: np.ndarray, sampling=(2, 2), quality: int = 80, restart: int = 0, grey: bool = False,
+                interleaved: bool = True):
+    """A baseline JPEG of an (h, w, 3) uint8 image: JFIF YCbCr, luma sampled
+    `sampling` (h, v) times the chroma, float DCT, scaled standard-shaped
+    quantisers, per-file Huffman tables, optional restart interval and
+    separate scans per component.  Returns (bytes, info) with the quantised
+    coefficients of every block (natural order) for checking."""
+    cf = _jpeg_coefficients(rgb, sampling, quality, grey)
+    h, w, comps, qts = cf["h"], cf["w"], cf["comps"], cf["qts"]
+    hmax, vmax, mcux, mcuy = cf["hmax"], cf["vmax"], cf["mcux"], cf["mcuy"]
     # symbols per scan
     scans = [list(range(len(comps)))] if interleaved else [[k] for k in range(len(comps))]
     seqs = []  # per scan: list of (component, (by, bx)) in coding order, with restart flags
@@ -486,14 +508,8 @@ def encode_jpeg(rgb: np.ndarray, sampling=(2, 2), quality: int = 80, restart: in
             store.append(codes)
             body = bytes([(cls << 4) | t]) + bytes(counts) + bytes(order)
             dht += b"\xff\xc4" + struct.pack(">H", 2 + len(body)) + body
-    out = bytearray(b"\xff\xd8")
-    out += b"\xff\xe0" + struct.pack(">H", 16) + b"JFIF\0" + bytes([1, 1, 0, 0, 1, 0, 1, 0, 0])
-    for t in range(ntab):
-        out += b"\xff\xdb" + struct.pack(">H", 67) + bytes([t]) + bytes(qts[t].reshape(-1)[ZIGZAG].astype(np.uint8))
-    sof = bytes([8]) + struct.pack(">HH", h, w) + bytes([len(comps)])
-    for c in comps:
-        sof += bytes([c["id"], (c["h"] << 4) | c["v"], c["tq"]])
-    out += b"\xff\xc0" + struct.pack(">H", 2 + len(sof)) + sof
+    out = bytearray()
+    _jpeg_header(out, cf, 0xC0, ntab)
     out += dht
     if restart:
         out += b"\xff\xdd" + struct.pack(">HH", 4, restart)
@@ -538,4 +554,189 @@ def encode_jpeg(rgb: np.ndarray, sampling=(2, 2), quality: int = 80, restart: in
         out += data
     out += b"\xff\xd9"
     info = dict(width=w, height=h, comps=comps, qts=qts, hmax=hmax, vmax=vmax)
+    return bytes(out), info
+
+
+class _BitWriter:
+    """An entropy-coded segment: bits MSB first, 0xFF bytes stuffed."""
+
+    def __init__(self):
+        self.data = bytearray()
+        self.acc = 0
+        self.n = 0
+
+    def put(self, code: int, n: int):
+        for i in range(n - 1, -1, -1):
+            self.acc = (self.acc << 1) | ((code >> i) & 1)
+            self.n += 1
+            if self.n == 8:
+                self.data.append(self.acc)
+                if self.acc == 0xFF:
+                    self.data.append(0)
+                self.acc = self.n = 0
+
+    def flush(self):
+        if self.n:
+            self.put((1 << (8 - self.n)) - 1, 8 - self.n)
+
+
+def _bits_of(v: int, s: int) -> int:
+    return v if v > 0 else v + (1 << s) - 1
+
+
+def encode_jpeg_progressive(rgb: np.ndarray, sampling=(2, 2), quality: int = 80, restart: int = 0,
+                            grey: bool = False):
+    """The same coefficients as encode_jpeg, written as a progressive JPEG
+    (SOF2, ITU T.81 Annex G): a DC scan of all components with a point
+    transform of 1, its refinement; for luma AC bands 1..5 and 6..63 with a
+    point transform of 2 and two refinement scans; for chroma one AC band
+    1..63 with a point transform of 1 and one refinement.  End-of-band runs
+    span blocks (up to 32767), refinement scans send correction bits for the
+    coefficients already nonzero, and each scan has its own Huffman tables.
+    Returns (bytes, info) like encode_jpeg."""
+    cf = _jpeg_coefficients(rgb, sampling, quality, grey)
+    comps = cf["comps"]
+    nc = len(comps)
+    scans = [(list(range(nc)), 0, 0, 0, 1), (list(range(nc)), 0, 0, 1, 0),
+             ([0], 1, 5, 0, 2), ([0], 6, 63, 0, 2)]
+    scans += [([k], 1, 63, 0, 1) for k in range(1, nc)]
+    scans += [([0], 1, 63, 2, 1), ([0], 1, 63, 1, 0)]
+    scans += [([k], 1, 63, 1, 0) for k in range(1, nc)]
+    out = bytearray()
+    _jpeg_header(out, cf, 0xC2, 1 if grey else 2)
+    if restart:
+        out += b"\xff\xdd" + struct.pack(">HH", 4, restart)
+
+    def blocks_of(sc):
+        """Coding units: MCUs of an interleaved scan, blocks of one component."""
+        if len(sc) > 1:
+            return [[(k, my * comps[k]["v"] + v, mx * comps[k]["h"] + hh) for k in sc
+                     for v in range(comps[k]["v"]) for hh in range(comps[k]["h"])]
+                    for my in range(cf["mcuy"]) for mx in range(cf["mcux"])]
+        c = comps[sc[0]]
+        return [[(sc[0], by, bx)] for by in range(-(-c["dh"] // 8)) for bx in range(-(-c["dw"] // 8))]
+
+    for sc, ss, se, ah, al in scans:
+        units = blocks_of(sc)
+        ev = []  # per unit: events ("sym", table, symbol) or ("bits", value, n) or ("rst",)
+        state = {"eobrun": 0, "be": []}
+        table = lambda k: 0 if k == 0 else 1
+
+        def emit_eob(out_ev, t):
+            if state["eobrun"]:
+                r = state["eobrun"].bit_length() - 1
+                out_ev.append(("sym", t, r << 4))
+                if r:
+                    out_ev.append(("bits", state["eobrun"] - (1 << r), r))
+                for bit in state["be"]:
+                    out_ev.append(("bits", bit, 1))
+                state["eobrun"], state["be"] = 0, []
+
+        pred = {}
+        for n, unit in enumerate(units):
+            u = []
+            if restart and n and n % restart == 0:
+                if ss:
+                    emit_eob(u, table(sc[0]))
+                u.append(("rst",))
+                pred = {}
+            for (k, by, bx) in unit:
+                zz = comps[k]["coef"][by, bx].reshape(-1)[ZIGZAG]
+                t = table(k)
+                if ss == 0 and ah == 0:
+                    dc = int(zz[0]) >> al
+                    diff = dc - pred.get(k, 0)
+                    pred[k] = dc
+                    s = _cat(diff)
+                    u.append(("sym", t, s))
+                    if s:
+                        u.append(("bits", _bits_of(diff, s), s))
+                elif ss == 0:
+                    u.append(("bits", (int(zz[0]) >> al) & 1, 1))
+                elif ah == 0:
+                    vals = [int(np.sign(v)) * (abs(int(v)) >> al) for v in zz[ss:se + 1]]
+                    r = 0
+                    for v in vals:
+                        if v == 0:
+                            r += 1
+                            continue
+                        emit_eob(u, t)
+                        while r > 15:
+                            u.append(("sym", t, 0xF0))
+                            r -= 16
+                        s = _cat(v)
+                        u.append(("sym", t, (r << 4) | s))
+                        u.append(("bits", _bits_of(v, s), s))
+                        r = 0
+                    if r:
+                        state["eobrun"] += 1
+                        if state["eobrun"] == 0x7FFF:
+                            emit_eob(u, t)
+                else:
+                    absv = [abs(int(v)) >> al for v in zz[ss:se + 1]]
+                    eob = max([i for i, a in enumerate(absv) if a == 1], default=-1)
+                    r, br = 0, []
+                    for i, a in enumerate(absv):
+                        if a == 0:
+                            r += 1
+                            continue
+                        while r > 15 and i <= eob:
+                            emit_eob(u, t)
+                            u.append(("sym", t, 0xF0))
+                            u.extend(("bits", bit, 1) for bit in br)
+                            br = []
+                            r -= 16
+                        if a > 1:
+                            br.append(a & 1)
+                            continue
+                        emit_eob(u, t)
+                        u.append(("sym", t, (r << 4) | 1))
+                        u.append(("bits", 1 if zz[ss + i] > 0 else 0, 1))
+                        u.extend(("bits", bit, 1) for bit in br)
+                        br, r = [], 0
+                    if r or br:
+                        state["eobrun"] += 1
+                        state["be"].extend(br)
+                        if state["eobrun"] == 0x7FFF or len(state["be"]) > 900:
+                            emit_eob(u, t)
+            ev.append(u)
+        if ss:
+            emit_eob(ev[-1], table(sc[0]))
+        # one Huffman table per table id used in the scan (DC tables for a
+        # first DC scan, AC tables for AC scans; a DC refinement needs none)
+        freq = {}
+        for u in ev:
+            for e in u:
+                if e[0] == "sym":
+                    freq.setdefault(e[1], {})
+                    freq[e[1]][e[2]] = freq[e[1]].get(e[2], 0) + 1
+        codes = {}
+        cls = 0 if ss == 0 else 1
+        for t, fq in sorted(freq.items()):
+            counts, order, cd = _canonical(_huff_lengths(fq))
+            codes[t] = cd
+            body = bytes([(cls << 4) | t]) + bytes(counts) + bytes(order)
+            out += b"\xff\xc4" + struct.pack(">H", 2 + len(body)) + body
+        sos = bytes([len(sc)])
+        for k in sc:
+            sos += bytes([comps[k]["id"], (table(k) << 4) | table(k)])
+        sos += bytes([ss, se, (ah << 4) | al])
+        out += b"\xff\xda" + struct.pack(">H", 2 + len(sos)) + sos
+        bw = _BitWriter()
+        rst = 0
+        for u in ev:
+            for e in u:
+                if e[0] == "sym":
+                    code, ln = codes[e[1]][e[2]]
+                    bw.put(code, ln)
+                elif e[0] == "bits":
+                    bw.put(e[1], e[2])
+                else:
+                    bw.flush()
+                    bw.data += bytes([0xFF, 0xD0 + rst % 8])
+                    rst += 1
+        bw.flush()
+        out += bw.data
+    out += b"\xff\xd9"
+    info = dict(width=cf["w"], height=cf["h"], comps=comps, qts=cf["qts"], hmax=cf["hmax"], vmax=cf["vmax"])
     return bytes(out), info

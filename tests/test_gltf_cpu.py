@@ -153,6 +153,38 @@ def test_jpeg_matches_the_libjpeg_restatement(lib, tmp_path, sampling, restart, 
     assert np.abs(rgb - smooth.astype(int)).mean() < 3.0
 
 
+PROGRESSIVE_CASES = [(s, r, g) for s in [(1, 1), (2, 1), (2, 2), (1, 2)] for (r, g) in [(0, False), (3, False), (0, True)]]
+
+
+@pytest.mark.parametrize("sampling,restart,grey", PROGRESSIVE_CASES)
+def test_progressive_jpeg_matches_the_libjpeg_restatement(lib, tmp_path, sampling, restart, grey):
+    """Progressive JPEGs (SOF2: a DC scan with a point transform and its
+    refinement, AC bands with point transforms, end-of-band runs across
+    blocks and AC refinement scans with correction bits; restart intervals;
+    grey) decode to exactly the pixels of the baseline file that holds the
+    same coefficients: the restated libjpeg pixel path on the encoder's
+    quantised coefficients."""
+    from swegl_gb300.gltf import load_image
+
+    yy, xx = np.mgrid[0:29, 0:37]
+    smooth = np.stack([(xx * 7) % 256, (yy * 9) % 256, ((xx + yy) * 5) % 256], -1).astype(np.uint8)
+    noisy = np.random.default_rng(5).integers(0, 256, size=(40, 56, 3)).astype(np.uint8)
+    for img in (smooth, noisy):
+        for q in (30, 95):
+            data, info = GF.encode_jpeg_progressive(img, sampling, q, restart, grey=grey)
+            assert data[2:].find(b"\xff\xc2") >= 0
+            path = str(tmp_path / "p.jpg")
+            with open(path, "wb") as fh:
+                fh.write(data)
+            got = load_image(path)
+            exp = GO.jpeg_pixels(info)
+            assert np.array_equal(got, exp), (img.shape, q)
+            base, _ = GF.encode_jpeg(img, sampling, q, restart, grey=grey)
+            with open(str(tmp_path / "b.jpg"), "wb") as fh:
+                fh.write(base)
+            assert np.array_equal(load_image(str(tmp_path / "b.jpg")), got)
+
+
 def test_bad_images_are_errors_not_crashes(lib, tmp_path):
     from swegl_gb300.gltf import load_image
     from swegl_gb300.runtime import SglError
