@@ -131,7 +131,11 @@ typedef struct sgl_scene_desc {
 /* ----------------------------------------------------------------- views -- */
 
 /* Depth-of-field gather (replaces post_shader_depth_box,
- * swegl/render/post_shaders.hpp:51-132, whose own output is not usable). */
+ * swegl/render/post_shaders.hpp:51-132, whose own output is not usable).  It
+ * runs over the view's rectangle after the view is rendered; for a view with
+ * transparency layers, after the layers are flattened and copied to the
+ * surface (the reference's post shader reads the first layer), with the
+ * view's opaque depth. */
 typedef struct sgl_dof_desc {
     int   enabled;
     float focus;        /* view-space focus distance */

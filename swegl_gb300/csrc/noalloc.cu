@@ -235,6 +235,8 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
         it.dof_pitch = it.pitch_px;
         it.pixels = (uint32_t *)(base + o_dof);
         it.pitch_px = v.w;
+        it.dof_src = it.pixels;
+        it.dof_src_pitch = v.w;
         if (!it.zbuf)
             it.zbuf = (float *)(base + o_dof + 4 * px);
         const float k = d.px_scale > 0.0f ? d.px_scale : (v.proj[5] * (float)v.h) / 2.0f;

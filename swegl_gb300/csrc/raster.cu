@@ -2179,6 +2179,12 @@ __global__ void __launch_bounds__(kShadeThreads, SGL_SHADE_MIN_BLOCKS) k_shade_w
 
 // ------------------------------------------------------------ depth of field --
 
+// The fragment pool was too small: nothing is written, the host renders again.
+__device__ __forceinline__ bool frags_overflowed(const BatchDev *b)
+{
+    return *frag_counter(b) > (unsigned long long)b->frag_cap;
+}
+
 __constant__ float2 c_dof_taps[SGL_DOF_TAPS];
 
 // Circle of confusion of pixel i of a depth-of-field item.
@@ -2216,6 +2222,8 @@ constexpr int kDofBlocks = 5; // resident blocks per SM (shared memory: 37 KB ea
 
 __global__ void __launch_bounds__(256, kDofBlocks) k_dof(const BatchDev *b)
 {
+    if (frags_overflowed(b))
+        return; // a layered view whose fragment pool was too small: rendered again
     __shared__ uint32_t halo[kDofPitch * kDofPitch];
     __shared__ uint32_t claim[2]; // this tile and the next (tiles cost from a copy to a full gather)
     int item = -1;
@@ -2249,13 +2257,13 @@ __global__ void __launch_bounds__(256, kDofBlocks) k_dof(const BatchDev *b)
             c1 = c1 < 0 ? 0 : (c1 >= w ? w - 1 : c1);
             c2 = c2 < 0 ? 0 : (c2 >= w ? w - 1 : c2);
             // the staged pixels' common value, if they all have one
-            const uint32_t ref = __ldg(it.pixels + (size_t)y0 * it.pitch_px + x0);
+            const uint32_t ref = __ldg(it.dof_src + (size_t)y0 * it.dof_src_pitch + x0);
             bool same = true;
 #pragma unroll 4
             for (int yy = warp; yy < S; yy += 8) {
                 int sy = y0 - R + yy;
                 sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
-                const uint32_t *row = it.pixels + (size_t)sy * it.pitch_px;
+                const uint32_t *row = it.dof_src + (size_t)sy * it.dof_src_pitch;
                 uint32_t *dst = halo + yy * kDofPitch;
                 if (lane < S) {
                     const uint32_t v = __ldg(row + c0);
@@ -2382,17 +2390,34 @@ __global__ void __launch_bounds__(256, kDofBlocks) k_dof(const BatchDev *b)
                     int sx = xs + __float2int_rn(r * t.x), sy = y + __float2int_rn(r * t.y);
                     sx = sx < 0 ? 0 : (sx >= w ? w - 1 : sx);
                     sy = sy < 0 ? 0 : (sy >= h ? h - 1 : sy);
-                    const uint32_t v = __ldg(it.pixels + (size_t)sy * it.pitch_px + sx);
+                    const uint32_t v = __ldg(it.dof_src + (size_t)sy * it.dof_src_pitch + sx);
                     sb += v & 0xFFu;
                     sg += (v >> 8) & 0xFFu;
                     sr += (v >> 16) & 0xFFu;
                 }
                 if (valid)
                     it.dof_out[(size_t)y * it.dof_pitch + x] =
-                        dof_average(it.pixels[(size_t)y * it.pitch_px + xs], sb, sg, sr);
+                        dof_average(it.dof_src[(size_t)y * it.dof_src_pitch + xs], sb, sg, sr);
             }
         }
         __syncthreads(); // the halo is reused by the next tile, claim[cb ^ 1] is written
+    }
+}
+
+// The gather's input for a view with transparency layers: its rectangle of
+// the surface after the layer passes (the flatten and copy write the surface
+// at the reference's offsets, so the rectangle is read back whole), copied
+// to the scratch buffer, since the gather writes the rectangle in place.
+__global__ void __launch_bounds__(256) k_dof_source(const BatchDev *b)
+{
+    if (frags_overflowed(b))
+        return;
+    const ItemDev &it = b->items[0];
+    const int w = it.v.w;
+    const uint32_t total = (uint32_t)w * (uint32_t)it.v.h;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int y = (int)(i / (uint32_t)w), x = (int)(i - (uint32_t)y * (uint32_t)w);
+        it.dof_src[(size_t)y * it.dof_src_pitch + x] = it.dof_out[(long long)y * it.dof_pitch + x];
     }
 }
 
@@ -2415,11 +2440,6 @@ __global__ void __launch_bounds__(256, kDofBlocks) k_dof(const BatchDev *b)
 // (viewport.cpp:43-86) and post_shader_t's copy of the first layer to the
 // screen (post_shaders.hpp:22-47).  A layered batch holds one view.
 
-// The fragment pool was too small: nothing is written, the host renders again.
-__device__ __forceinline__ bool frags_overflowed(const BatchDev *b)
-{
-    return *frag_counter(b) > (unsigned long long)b->frag_cap;
-}
 
 // blend (src/render/colors.cpp:39-57): back * (256 - a) / 256 + front * a / 256
 // truncated, which is exact in integers (both terms are multiples of 1/256).
@@ -2991,6 +3011,11 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
         k_copy_layer<<<sms * 8, 256, 0, st>>>(b);
         ran(PK_COPY);
         n += 7;
+        if (flags & kSeqDof) { // the gather over the view's rectangle, from a copy of it (timed with the copy)
+            k_dof_source<<<sms * 8, 256, 0, st>>>(b);
+            k_dof<<<sms * kDofBlocks, 256, 0, st>>>(b);
+            n += 2;
+        }
         if (timed) {
             cudaEventRecord(prof->ev[kProfKernels], st);
             prof->pending = true;

@@ -51,10 +51,6 @@ sgl_status check_view(Ctx *ctx, const sgl_view &v, const sgl_target &t)
         ctx->fail("depth-of-field max_radius %g outside 0..4096 pixels", (double)v.dof.max_radius);
         return SGL_ERR_INVALID;
     }
-    if (v.layers > 0 && v.dof.enabled) {
-        ctx->fail("depth of field on a view with transparency layers is not implemented");
-        return SGL_ERR_UNSUPPORTED;
-    }
     if (v.w <= 0 || v.h <= 0 || v.x < 0 || v.y < 0 || (int64_t)v.w * v.h > (1ll << 28)) {
         ctx->fail("bad viewport %d,%d %dx%d", v.x, v.y, v.w, v.h);
         return SGL_ERR_INVALID;
@@ -700,6 +696,8 @@ SGL_API sgl_status sgl_dof(sgl_ctx *c, const sgl_view *view, const sgl_target *i
     it.v = make_view(v);
     it.pixels = src;
     it.pitch_px = src_pitch;
+    it.dof_src = src;
+    it.dof_src_pitch = src_pitch;
     it.zbuf = z;
     it.dof = 1;
     it.dof_out = dst;

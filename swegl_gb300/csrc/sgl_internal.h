@@ -116,6 +116,8 @@ struct ItemDev {
     float dof_focus, dof_ka, dof_rmax, p22, p23;
     uint32_t *dof_out;
     int dof_pitch;
+    uint32_t *dof_src;  // the gather's colour input (pitch dof_src_pitch): the shade's scratch buffer, or for a
+    int dof_src_pitch;  // view with transparency layers a copy of its rectangle after the layer passes
     int dof_halo;    // tap reach in pixels (ceil of max_radius, <= kDofMaxHalo), -1: gather from memory
     int dof_tiles_x; // kDofTile tiles across the view
     // transparency layers (viewport_t::m_transparency_layers); when layers

@@ -220,8 +220,8 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
     if (layers > 0) {
         // one view per layered batch: its flatten and copy passes read and
         // write the whole surface, in view order
-        if (n != 1 || e[0].view.dof.enabled || !e[0].surface) {
-            ctx->fail("transparency layers take one view per launch sequence, without depth of field");
+        if (n != 1 || !e[0].surface) {
+            ctx->fail("transparency layers take one view per launch sequence");
             return SGL_ERR_UNSUPPORTED;
         }
         frag_want = std::max<size_t>(frag_want, std::max<size_t>(4 * tp, 65536));
@@ -254,14 +254,21 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         it.tiles_x = (en.view.w + tile - 1) / tile;
         it.tile_base = gb[i];
         if (en.view.dof.enabled) {
-            // the shade kernel fills a scratch colour buffer; the gather writes the target
+            // the shade kernel fills a scratch colour buffer; the gather writes
+            // the target (a layered view: the layer passes write the surface,
+            // then its rectangle is copied to the scratch buffer and gathered
+            // back in place)
             const sgl_dof_desc &d = en.view.dof;
             seq_flags |= kSeqDof;
             it.dof = 1;
             it.dof_out = en.rect_pixels;
             it.dof_pitch = en.pitch_px;
-            it.pixels = (uint32_t *)doftmp.ptr + dof_at[i];
-            it.pitch_px = en.view.w;
+            it.dof_src = (uint32_t *)doftmp.ptr + dof_at[i];
+            it.dof_src_pitch = en.view.w;
+            if (en.view.layers == 0) {
+                it.pixels = it.dof_src;
+                it.pitch_px = en.view.w;
+            }
             if (!en.zbuf)
                 it.zbuf = (float *)dofz.ptr + dofz_at[i];
             const float k = d.px_scale > 0.0f ? d.px_scale : (en.view.proj[5] * (float)en.view.h) / 2.0f;

@@ -392,8 +392,6 @@ static sgl_status make_job(Server *srv, const sgl_request *req, Job &j)
         return SGL_ERR_INVALID;
     if (v.dof.enabled && !(v.dof.max_radius >= 0.0f && v.dof.max_radius <= 4096.0f))
         return SGL_ERR_INVALID;
-    if (v.layers > 0 && v.dof.enabled)
-        return SGL_ERR_UNSUPPORTED; // depth of field on a layered view is not implemented
     j = Job{};
     j.req = *req;
     j.scene = scene;
