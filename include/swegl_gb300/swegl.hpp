@@ -18,8 +18,8 @@
 //   * the reference's pixel shaders (pixel_shader_t, the flat and Phong light
 //     shaders, the nearest and bilinear texture shaders and their
 //     pixel_shader_light_and_texture<L, T> combinations) and viewports with
-//     0 to SGL_MAX_LAYERS transparency layers run on the GPU; more layers, or
-//     layers with the depth-of-field post shader, throw swegl::render_error
+//     0 to SGL_MAX_LAYERS transparency layers run on the GPU, with or without
+//     the depth-of-field post shader; more layers throw swegl::render_error
 //     (there is no CPU fallback);
 //   * the scene is not mutated (v_world, v_viewport, normal_world, yes and
 //     the temporary clip vertices of the reference are not written back);
