@@ -251,14 +251,15 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     const uint32_t dof_tiles =
         dof ? (uint32_t)((v.w + kDofTile - 1) / kDofTile) * (uint32_t)((v.h + kDofTile - 1) / kDofTile) : 0u;
     const bool fused = s->dev.fused != 0;
+    const bool split = !fused || s->dev.mixed != 0; // the general passes run (all, or the larger primitives)
     // prefixes of one item (vertices, triangles, pixels, tiles, depth-of-field
     // tiles, the general geometry pass's vertices and triangles), then the
     // fused pass's one group: its chunks, its items, the item
     const uint32_t chunks = fused ? (s->dev.n_prims + kGeomWarps - 1) / kGeomWarps : 0u;
     const NoAllocBases bases = {{0u, (uint32_t)nv,              0u, (uint32_t)nt,
                                  0u, (uint32_t)px,              0u, (uint32_t)tiles,
-                                 0u, dof_tiles,                 0u, fused ? 0u : (uint32_t)nv,
-                                 0u, fused ? 0u : (uint32_t)nt, 0u, chunks,
+                                 0u, dof_tiles,                 0u, split ? (uint32_t)nv : 0u,
+                                 0u, split ? (uint32_t)nt : 0u, 0u, chunks,
                                  0u, fused ? 1u : 0u,           0u, 0u}};
     BatchDev b{};
     b.items = (const ItemDev *)(base + o_item);
@@ -273,8 +274,8 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     b.grp_item_base = bp + 16;
     b.grp_items = bp + 18;
     b.n_groups = fused ? 1 : 0;
-    b.total_gvtx = fused ? 0u : (uint32_t)nv;
-    b.total_gtri = fused ? 0u : (uint32_t)nt;
+    b.total_gvtx = split ? (uint32_t)nv : 0u;
+    b.total_gtri = split ? (uint32_t)nt : 0u;
     b.total_chunks = chunks;
     b.n_items = 1;
     b.inline_span = ctx->inline_span;
@@ -304,7 +305,7 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     CUDA_TRY(cudaMemsetAsync(base + o_key, 0xFF, 8 * px, st)); // kEmptyKey
 
     const int seq = (dof ? kSeqDof : 0) | (v.shader != SGL_SHADER_PHONG_BILINEAR ? kSeqShaders : 0) |
-                    (fused ? kSeqFused : kSeqSplit) | (win_list ? kSeqWinList : 0);
+                    (fused ? kSeqFused : 0) | (split ? kSeqSplit : 0) | (win_list ? kSeqWinList : 0);
     CUDA_TRY(launch_batch((const BatchDev *)(base + o_batch), tile, seq, st, nullptr, nullptr));
     return SGL_OK;
 }

@@ -141,6 +141,7 @@ __global__ void __launch_bounds__(256) k_vertex(const BatchDev *b)
     const float4 *wpos = nullptr;
     float4 *ndc = nullptr;
     uint8_t *yes = nullptr;
+    const uint8_t *vsmall = nullptr; // a mixed scene: vertices the fused pass transforms
     const uint32_t total = b->total_gvtx;
     auto bind = [&](uint32_t g) {
         const int item = find_item(b->g_vtx_base, b->n_items, g);
@@ -155,8 +156,11 @@ __global__ void __launch_bounds__(256) k_vertex(const BatchDev *b)
         wpos = it.s.wpos;
         ndc = it.ndc;
         yes = it.yes;
+        vsmall = it.s.vsmall;
     };
     auto project = [&](uint32_t l, float4 w) {
+        if (vsmall && vsmall[l])
+            return;
         V3 p = transform3(mk3(w.x, w.y, w.z), m);
         p = transform3(p, m + 12);
         if (p.z != 0.0f) {
@@ -220,6 +224,7 @@ __global__ void __launch_bounds__(256) k_flags(const BatchDev *b)
     uint8_t *yes = nullptr;
     const PrimDesc *prims = nullptr;
     const MatDesc *mats = nullptr;
+    const uint8_t *psmall = nullptr; // a mixed scene: primitives of the fused pass
     int n_mats = 0;
     const uint32_t total = b->total_gtri;
     auto bind = [&](uint32_t g) {
@@ -233,9 +238,10 @@ __global__ void __launch_bounds__(256) k_flags(const BatchDev *b)
         prims = it.s.prims;
         mats = it.s.mats;
         n_mats = it.s.n_mats;
+        psmall = it.s.psmall;
     };
     auto flag = [&](uint4 tri, V3 a, V3 c1, V3 c2) {
-        if (!inside_frustum(a, c1, c2))
+        if ((psmall && psmall[tri.w]) || !inside_frustum(a, c1, c2))
             return;
         // front facing, else double sided (the material is read only then)
         bool vis = cross_z_positive(sub3(c1, a), sub3(c2, a));
@@ -391,6 +397,7 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
     uint32_t lo = 0, hi = 0;
     const uint4 *tris = nullptr;
     const uint8_t *yes = nullptr;
+    const uint8_t *psmall = nullptr; // a mixed scene: primitives of the fused pass
     const uint32_t total = b->total_gtri;
     ItemAcc acc; // triangles counted as drawn here (no pixel column)
     // every thread of the block runs the same number of iterations (barriers inside)
@@ -411,10 +418,13 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(const BatchDev *b)
                 const ItemDev &it = b->items[item];
                 tris = it.s.tris;
                 yes = it.yes;
+                psmall = it.s.psmall;
             }
             t = g - lo;
             const uint4 tri = tris[t];
-            const uint32_t ya = yes[tri.x], yb = yes[tri.y], yc = yes[tri.z];
+            const bool general = !psmall || !psmall[tri.w];
+            const uint32_t ya = general ? yes[tri.x] : 0u, yb = general ? yes[tri.y] : 0u,
+                           yc = general ? yes[tri.z] : 0u;
             if (ya & yb & yc & kYesDrawn) {
                 // fill_triangle's cases (renderer.cpp:281-318): the smallest z' decides
                 list = ((ya | yb | yc) & kYesBehind) ? 1 : 0;
@@ -562,7 +572,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32, kGeomBlocks) k_geom(const Bat
         const uint32_t i_lo = __ldg(b->grp_item_base + g), i_hi = __ldg(b->grp_item_base + g + 1);
         const SceneDev &sc = b->items[__ldg(b->grp_items + i_lo)].s; // vertex data shared by the group
         const uint32_t q = (c - c_lo) * kGeomWarps + warp;             // this warp's primitive
-        const bool has = q < sc.n_prims;
+        const bool has = q < sc.n_prims && (!sc.psmall || sc.psmall[q]); // (a mixed scene's larger ones: general passes)
         uint4 gq = make_uint4(0u, 0u, 0u, 0u); // first vertex, vertex count, first triangle, triangle count
         bool ds = false;
         uint32_t tr0 = 0, tr1 = 0; // the first 64 triangles, local vertex indices

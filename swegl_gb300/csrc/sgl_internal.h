@@ -82,7 +82,10 @@ struct SceneDev {
     uint32_t n_vertices;
     uint32_t n_triangles;
     uint32_t n_prims;
-    int fused;               // every primitive within kFuseVerts / kFuseTris
+    int fused;               // some primitive within kFuseVerts / kFuseTris: the fused geometry pass runs
+    int mixed;               // fused, and some primitive beyond the limits: the general passes run too
+    const uint8_t *psmall;   // mixed: per draw-order primitive, 1 when the fused pass takes it
+    const uint8_t *vsmall;   // mixed: per vertex, 1 when only primitives of the fused pass use it
     int n_mats;
     int n_texs;
     MatDesc default_mat;

@@ -138,7 +138,8 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
             }
             grp_members[gk].push_back((uint32_t)i);
             geom_flags |= kSeqFused;
-        } else {
+        }
+        if (!s.dev.fused || s.dev.mixed) { // the general passes (of a mixed scene: its larger primitives)
             tgv += s.n_vertices;
             tgt += s.n_triangles;
             geom_flags |= kSeqSplit;

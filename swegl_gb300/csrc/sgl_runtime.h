@@ -53,7 +53,7 @@ struct Ctx;
 // A scene resident in device memory.
 struct Scene {
     DevBuf d_pos_u, d_nrm_v, d_vnode, d_tris, d_prims, d_mats, d_texs, d_texels, d_wpos, d_wnrm, d_uv,
-        d_node_world, d_node_rs, d_lights, d_pgeo, d_pshade;
+        d_node_world, d_node_rs, d_lights, d_pgeo, d_pshade, d_psmall, d_vsmall;
     SceneDev dev{};
     LightsDev lights{};
     std::vector<sgl_node_desc> nodes;

@@ -306,7 +306,8 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     }
     std::vector<PrimDesc> prims(order.size());
     std::vector<uint4> pgeo(order.size());
-    bool fused = true;
+    std::vector<uint8_t> psmall(std::max<size_t>(order.size(), 1), 0);
+    bool any_small = false, any_big = false;
     std::vector<uint4> tris;
     std::vector<uint32_t> vnode(d->n_vertices, 0);
     uint64_t total = 0;
@@ -323,8 +324,9 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
         const uint32_t base = p.vertex_offset;
         const uint32_t nt = prim_triangles(p);
         pgeo[q] = make_uint4(p.vertex_offset, p.vertex_count, (uint32_t)tris.size(), nt);
-        if (p.vertex_count > kFuseVerts || nt > kFuseTris)
-            fused = false;
+        psmall[q] = (p.vertex_count <= kFuseVerts && nt <= kFuseTris) ? 1 : 0;
+        any_small |= psmall[q] != 0;
+        any_big |= psmall[q] == 0;
         for (uint32_t t = 0; t < nt; t++) {
             uint32_t i0, i1, i2;
             if (p.mode == SGL_TRIANGLE_STRIP) { // renderer.cpp:198-207, with the parity swap
@@ -419,7 +421,27 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     dev.pgeo = (const uint4 *)d_pgeo.ptr;
     dev.pshade = (const PrimShade *)d_pshade.ptr;
     dev.n_prims = (uint32_t)pgeo.size();
-    dev.fused = fused ? 1 : 0;
+    // Primitives within kFuseVerts / kFuseTris take the fused geometry pass.
+    // A scene that also has larger ones runs the general passes as well, and
+    // each pass skips the other's primitives: the general passes skip the
+    // triangles of fused-pass primitives and the vertices that only those use
+    // (a vertex that a larger primitive shares is transformed by both, to the
+    // same value).
+    dev.fused = any_small ? 1 : 0;
+    dev.mixed = any_small && any_big ? 1 : 0;
+    if (dev.mixed) {
+        std::vector<uint8_t> vsmall(std::max<uint32_t>(n_vertices, 1), 0);
+        for (size_t q = 0; q < pgeo.size(); q++)
+            if (psmall[q])
+                std::fill(vsmall.begin() + pgeo[q].x, vsmall.begin() + pgeo[q].x + pgeo[q].y, (uint8_t)1);
+        for (size_t q = 0; q < pgeo.size(); q++)
+            if (!psmall[q])
+                std::fill(vsmall.begin() + pgeo[q].x, vsmall.begin() + pgeo[q].x + pgeo[q].y, (uint8_t)0);
+        CUDA_TRY(upload(d_psmall, psmall.data(), psmall.size()));
+        CUDA_TRY(upload(d_vsmall, vsmall.data(), vsmall.size()));
+        dev.psmall = (const uint8_t *)d_psmall.ptr;
+        dev.vsmall = (const uint8_t *)d_vsmall.ptr;
+    }
     dev.n_vertices = n_vertices;
     dev.n_triangles = n_triangles;
     dev.n_mats = d->n_materials;
@@ -435,7 +457,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     if (st != SGL_OK)
         return st;
     device_bytes = d_pos_u.bytes + d_nrm_v.bytes + d_vnode.bytes + d_tris.bytes + d_prims.bytes + d_mats.bytes +
-                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_uv.bytes + d_node_world.bytes + d_node_rs.bytes + d_lights.bytes + d_pgeo.bytes + d_pshade.bytes;
+                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_uv.bytes + d_node_world.bytes + d_node_rs.bytes + d_lights.bytes + d_pgeo.bytes + d_pshade.bytes + d_psmall.bytes + d_vsmall.bytes;
     return SGL_OK;
 }
 

@@ -653,6 +653,40 @@ def grid_scene(n: int = 40, extent: float = 10.0, seed: int = 6) -> Scene:
     return s.finalize()
 
 
+def mixed_size_scene(seed: int = 7) -> Scene:
+    """A floor of one 3,200-triangle list (beyond the fused geometry pass's
+    primitive limits) with three cubes and a sphere standing on it (within
+    them): a scene whose primitives take both geometry passes."""
+    s = Scene()
+    s.textures.append(texture_value_noise(seed, 128, octaves=3))
+    s.textures.append(texture_uniform(seed + 1, 64, 64))
+    s.materials.append((0xFFFFFFFF, 0, 0, 32))
+    s.materials.append((0xFFFFFFFF, 1, 1, 48))
+    floor = s.add_node()
+    n, extent = 40, 10.0
+    g = np.arange(n + 1, dtype=np.float64)
+    xs = (-extent + 2.0 * extent * g / n)
+    X, Z = np.meshgrid(xs, xs)
+    pos = np.stack([X, np.full_like(X, -0.5), Z], -1).reshape(-1, 3).astype(np.float32)
+    uv = np.stack(np.meshgrid(g / n, g / n), -1).reshape(-1, 2).astype(np.float32)
+    nrm = np.tile(np.array([0.0, 1.0, 0.0], np.float32), (len(pos), 1))
+    idx = []
+    for j in range(n):
+        for i in range(n):
+            a, b, c, d = j * (n + 1) + i, j * (n + 1) + i + 1, (j + 1) * (n + 1) + i, (j + 1) * (n + 1) + i + 1
+            idx += [a, c, b, b, c, d]
+    s.add_primitive(floor, TRIANGLES, 0, pos, nrm, uv, np.asarray(idx, np.uint32))
+    for k, (x, z) in enumerate(((-1.5, -2.0), (1.0, -1.0), (0.0, -3.5))):
+        nk = s.add_node(translation=(x, -0.1, z), rotation=rot_y(0.3 * k + 0.2).astype(np.float32))
+        for (p, nm, t, i) in cube_mesh(0.8):
+            s.add_primitive(nk, TRIANGLE_FAN, 1, p, nm, t, i)
+    ns = s.add_node(translation=(0.5, 0.2, -2.2))
+    for (p, nm, t, i) in uv_sphere_mesh(16, 8, 0.7):
+        s.add_primitive(ns, TRIANGLE_STRIP, 1, p, nm, t, i)
+    s.point_lights = [(0.0, 1.5, -1.0, 3.0), (-2.0, 1.0, 1.0, 2.0)]
+    return s.finalize()
+
+
 SERVE_TRIANGLES = (10_000, 50_000, 100_000, 250_000, 500_000, 800_000, 1_200_000, 2_000_000)
 
 

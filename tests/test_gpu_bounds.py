@@ -3,7 +3,8 @@ kernels compiled with -DSGL_BOUNDS_CHECK; a guarded access whose index falls
 outside its buffer is recorded and skipped, nothing traps) over the edge-case,
 view-volume and transparency-layer scenes of the other GPU tests, then over a
 full-size frame, a 3840x2160 depth-of-field frame, a near-clipped floor, a
-batch of uneven views and the serving loop.  Every guarded access stays in its
+scene whose primitives take both geometry passes, a batch of uneven views
+and the serving loop.  Every guarded access stays in its
 buffer (the check record stays clear), and the checked library's frames equal
 the normal library's bit for bit."""
 import ctypes as C
@@ -85,7 +86,8 @@ def test_full_size_frames_batch_and_serving_match_the_unchecked_library(checked)
     dof = S.spheres_view(3840, 2160)
     dof.dof = True
     m, c = S.look_at((0.3, -0.3, 2.0), (0.0, -0.5, -3.0))
-    cases = [(spheres, [S.spheres_view(1920, 1080)]), (spheres, [dof]), (floor, [S.view_for(640, 480, m, c)])]
+    cases = [(spheres, [S.spheres_view(1920, 1080)]), (spheres, [dof]), (floor, [S.view_for(640, 480, m, c)]),
+             (S.mixed_size_scene(), [S.view_for(640, 480, m, c)])]  # both geometry passes on one scene
     for sc, views in cases:
         a = plain.upload(sc)
         b = checked.upload(sc)
