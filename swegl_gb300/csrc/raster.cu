@@ -128,6 +128,45 @@ __global__ void k_pose(SceneDev s, const float *node_world, const float *node_rs
     wnrm[g] = make_float4(nw.x, nw.y, nw.z, 0.0f);
 }
 
+// The box of each primitive's world positions (a warp per primitive), for the
+// fused pass's whole-primitive frustum test: pbox[2 q] = centre, pbox[2 q + 1]
+// = half extent.  NaN coordinates are left out (a triangle with one fails
+// each test of inside_camera_frustum that its other vertices fail, the
+// comparisons with NaN being false); a box that is empty or not finite gets a
+// NaN centre and is never culled.
+__global__ void k_box(SceneDev s, const float4 *wpos, float4 *pbox)
+{
+    const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (q >= s.n_prims)
+        return;
+    const uint4 gq = s.pgeo[q];
+    V3 lo = mk3(INFINITY, INFINITY, INFINITY), hi = mk3(-INFINITY, -INFINITY, -INFINITY);
+    for (uint32_t i = lane; i < gq.y; i += 32) {
+        if (!in_bounds(gq.x + i < s.n_vertices, CHK_NDC, gq.x + i))
+            break;
+        const float4 w = wpos[gq.x + i];
+        lo = mk3(fminf(lo.x, w.x), fminf(lo.y, w.y), fminf(lo.z, w.z));
+        hi = mk3(fmaxf(hi.x, w.x), fmaxf(hi.y, w.y), fmaxf(hi.z, w.z));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo.x = fminf(lo.x, __shfl_xor_sync(0xFFFFFFFFu, lo.x, o));
+        lo.y = fminf(lo.y, __shfl_xor_sync(0xFFFFFFFFu, lo.y, o));
+        lo.z = fminf(lo.z, __shfl_xor_sync(0xFFFFFFFFu, lo.z, o));
+        hi.x = fmaxf(hi.x, __shfl_xor_sync(0xFFFFFFFFu, hi.x, o));
+        hi.y = fmaxf(hi.y, __shfl_xor_sync(0xFFFFFFFFu, hi.y, o));
+        hi.z = fmaxf(hi.z, __shfl_xor_sync(0xFFFFFFFFu, hi.z, o));
+    }
+    if (lane == 0) {
+        V3 c = mk3(0.5f * lo.x + 0.5f * hi.x, 0.5f * lo.y + 0.5f * hi.y, 0.5f * lo.z + 0.5f * hi.z);
+        const V3 h = mk3(0.5f * hi.x - 0.5f * lo.x, 0.5f * hi.y - 0.5f * lo.y, 0.5f * hi.z - 0.5f * lo.z);
+        if (!(fabsf(c.x) + h.x + fabsf(c.y) + h.y + fabsf(c.z) + h.z < 0x1p100f))
+            c.x = __int_as_float(0x7FC00000); // empty or not finite
+        pbox[2 * q] = make_float4(c.x, c.y, c.z, 0.0f);
+        pbox[2 * q + 1] = make_float4(h.x, h.y, h.z, 0.0f);
+    }
+}
+
 // world_to_camera_or_frustum (vertex_shaders.hpp:35-52): view, projection
 // (rows 0-2), x and y divided by |z'|; also clears the visibility flag.  The
 // item's matrices stay in registers while the index is inside it.  Each
@@ -549,6 +588,38 @@ __device__ __forceinline__ uint32_t geom_tri(const uint4 *tris, uint4 gq, uint32
     return (tri.x - gq.x) | ((tri.y - gq.x) << 8) | ((tri.z - gq.x) << 16);
 }
 
+// Box (centre bc, half extent bh, ba = |bc| + bh) against region r of
+// ViewDev::cull: negative when the whole box is in the region.
+__device__ __forceinline__ float cull_region(const float4 *r, float4 bc, float4 bh, float4 ba)
+{
+    const float4 a = r[0], e = r[1];
+    return (a.x * bc.x + a.y * bc.y + a.z * bc.z + a.w) + (fabsf(a.x) * bh.x + fabsf(a.y) * bh.y + fabsf(a.z) * bh.z) +
+           (e.x * ba.x + e.y * ba.y + e.z * ba.z + e.w);
+}
+
+// Bit i (i < n <= 8) set when item grp_items[v0 + i] sees none of the
+// triangles of primitive q (box pbox[2 q], pbox[2 q + 1]): the box is in the
+// region z' > 0 and in one beyond a side plane (ViewDev::cull).  Lane 4 i + r
+// tests item i's side r; the mask is the same in every lane.  A box with a
+// NaN is in no region.
+__device__ __forceinline__ uint32_t geom_unseen(const BatchDev *b, const float4 *pbox, uint32_t q, uint32_t v0,
+                                                uint32_t n, uint32_t lane)
+{
+    bool out = false;
+    if ((lane >> 2) < n) {
+        const float4 *cull = &b->items[__ldg(b->grp_items + v0 + (lane >> 2))].v.cull[0][0];
+        const float4 bc = pbox[2 * q], bh = pbox[2 * q + 1];
+        const float4 ba = make_float4(fabsf(bc.x) + bh.x, fabsf(bc.y) + bh.y, fabsf(bc.z) + bh.z, 0.0f);
+        out = cull_region(cull + 2 * (lane & 3), bc, bh, ba) < 0.0f && cull_region(cull + 8, bc, bh, ba) < 0.0f;
+    }
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, out);
+    uint32_t u = 0;
+#pragma unroll
+    for (int i = 0; i < kGeomPass; i++)
+        u |= ((m >> (4 * i)) & 15u) ? 1u << i : 0u;
+    return u;
+}
+
 __global__ void __launch_bounds__(kGeomWarps * 32, kGeomBlocks) k_geom(const BatchDev *b)
 {
     extern __shared__ __align__(16) unsigned char geom_smem[];
@@ -576,6 +647,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32, kGeomBlocks) k_geom(const Bat
         uint4 gq = make_uint4(0u, 0u, 0u, 0u); // first vertex, vertex count, first triangle, triangle count
         bool ds = false;
         uint32_t tr0 = 0, tr1 = 0; // the first 64 triangles, local vertex indices
+        uint32_t unseen = 0; // bit vi: item vi of the pass in hand sees none of the primitive
         const float4 *wpos = sc.wpos;
         const uint4 *tris = sc.tris;
         if (has) {
@@ -590,9 +662,19 @@ __global__ void __launch_bounds__(kGeomWarps * 32, kGeomBlocks) k_geom(const Bat
         }
         for (uint32_t v0 = i_lo; v0 < i_hi; v0 += kGeomPass) {
             const int nv = (int)min((uint32_t)kGeomPass, i_hi - v0);
+            if (has && sc.pbox)
+                unseen = geom_unseen(b, sc.pbox, q, v0, (uint32_t)nv, lane);
             for (int vi = 0; vi < nv; vi++) {
                 uint32_t c0 = 0, c1 = 0, nx = 0;
-                if (has) {
+                const bool seen = has && !((unseen >> vi) & 1u);
+                if (!seen && has) {
+                    // the item sees none of the primitive's triangles
+                    if (lane < (uint32_t)kGeomTG) {
+                        S.walk[vi][warp][lane] = 0u;
+                        S.clip[vi][warp][lane] = 0u;
+                    }
+                }
+                if (seen) {
                     const uint32_t item = __ldg(b->grp_items + v0 + vi);
                     const ItemDev &it = b->items[item];
                     __syncwarp(); // the previous item's reads of pos, sy and vw are done
@@ -2860,15 +2942,19 @@ cudaError_t launch_world(const SceneDev &s, cudaStream_t st)
     if (s.n_vertices == 0)
         return cudaSuccess;
     k_world<<<grid_for(s.n_vertices, 256), 256, 0, st>>>(s);
+    if (s.pbox && s.n_prims)
+        k_box<<<(s.n_prims + 7) / 8, 256, 0, st>>>(s, s.wpos, s.pbox);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pose(const SceneDev &s, const float *node_world, const float *node_rs, float4 *wpos, float4 *wnrm,
-                        cudaStream_t st)
+                        float4 *pbox, cudaStream_t st)
 {
     if (s.n_vertices == 0)
         return cudaSuccess;
     k_pose<<<grid_for(s.n_vertices, 256), 256, 0, st>>>(s, node_world, node_rs, wpos, wnrm);
+    if (pbox && s.n_prims)
+        k_box<<<(s.n_prims + 7) / 8, 256, 0, st>>>(s, wpos, pbox);
     return cudaGetLastError();
 }
 

@@ -1,6 +1,7 @@
 // sgl_api.cpp — the C ABI of include/sgl.h: contexts, scenes, the plain
 // one-frame-per-launch renderer, the batched renderer and its autotuner.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -13,6 +14,38 @@
 #include "sgl_runtime.h"
 
 namespace sgl {
+
+// The planes of ViewDev::cull.  The vertex transform computes x' (and y', z')
+// as projection row . (view rows . (w, 1), 1) in float, with an error below
+// 16 ulp of E(|w|) = |P| . (|V| . |w| + |Vt|) + |Pt| for its row; the bound
+// taken is 2^-16 E, so a box that passes the test keeps every vertex at
+// least 2^-17 E from the plane (x'/|z'| then rounds strictly past +-1).
+static void cull_planes(const sgl_view &v, float4 cull[5][2])
+{
+    double M[3][4], E[3][4];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 4; c++) {
+            double m = c == 3 ? (double)v.proj[4 * r + 3] : 0.0, e = c == 3 ? std::fabs((double)v.proj[4 * r + 3]) : 0.0;
+            for (int k = 0; k < 3; k++) {
+                m += (double)v.proj[4 * r + k] * (double)v.view[4 * k + c];
+                e += std::fabs((double)v.proj[4 * r + k]) * std::fabs((double)v.view[4 * k + c]);
+            }
+            M[r][c] = m;
+            E[r][c] = e;
+        }
+    // a . (w, 1) < 0 where x' < -z', x' > z', y' < -z', y' > z'; and where z' > 0
+    const double sx[5] = {1.0, -1.0, 0.0, 0.0, 0.0}, sy[5] = {0.0, 0.0, 1.0, -1.0, 0.0};
+    const double sz[5] = {1.0, 1.0, 1.0, 1.0, -1.0};
+    for (int p = 0; p < 5; p++) {
+        float a[4], e[4];
+        for (int c = 0; c < 4; c++) {
+            a[c] = (float)(sx[p] * M[0][c] + sy[p] * M[1][c] + sz[p] * M[2][c]);
+            e[c] = (float)(0x1p-16 * (std::fabs(sx[p]) * E[0][c] + std::fabs(sy[p]) * E[1][c] + E[2][c]));
+        }
+        cull[p][0] = make_float4(a[0], a[1], a[2], a[3]);
+        cull[p][1] = make_float4(e[0], e[1], e[2], e[3]);
+    }
+}
 
 ViewDev make_view(const sgl_view &v)
 {
@@ -34,6 +67,7 @@ ViewDev make_view(const sgl_view &v)
     d.vm03 = (float)v.x + (float)v.w / 2.0f;
     d.vm11 = (float)(-v.h) / 2.0f;
     d.vm13 = (float)v.y + (float)v.h / 2.0f;
+    cull_planes(v, d.cull);
     return d;
 }
 
@@ -63,7 +97,6 @@ sgl_status check_view(Ctx *ctx, const sgl_view &v, const sgl_target &t)
     }
     return SGL_OK;
 }
-
 
 // The lane bound to a caller's stream (created on first use).
 static sgl_status ext_lane(Ctx *ctx, cudaStream_t st, Lane **out)
@@ -477,8 +510,8 @@ static sgl_status batch_entries(Ctx *ctx, const sgl_batch_item *items, int n, st
 
 // Batch items with their own pose: the node matrices composed on the host (as
 // sgl_scene_set_nodes does), then k_pose writes the item's world positions and
-// normals into the lane's pose scratch on the lane's stream, and the item's
-// entry points at them (the scene's own arrays and nodes are untouched).
+// normals (and k_box its primitives' boxes) into the lane's pose scratch on
+// the lane's stream, and the item's entry points at them (the scene's own arrays and nodes are untouched).
 static sgl_status pose_items(Ctx *ctx, Lane *lane, const sgl_batch_item *items, int n, std::vector<BatchEntry> &e)
 {
     std::vector<std::vector<float>> mats((size_t)n);
@@ -501,7 +534,8 @@ static sgl_status pose_items(Ctx *ctx, Lane *lane, const sgl_batch_item *items, 
         }
         mats[i] = std::move(world);
         mats[i].insert(mats[i].end(), rs.begin(), rs.end());
-        total += up(sizeof(float) * mats[i].size()) + up(2 * sizeof(float4) * std::max<size_t>(s->n_vertices, 1));
+        total += up(sizeof(float) * mats[i].size()) + up(2 * sizeof(float4) * std::max<size_t>(s->n_vertices, 1)) +
+                 (s->dev.pbox ? up(2 * sizeof(float4) * s->dev.n_prims) : 0);
     }
     if (!total)
         return SGL_OK;
@@ -517,13 +551,19 @@ static sgl_status pose_items(Ctx *ctx, Lane *lane, const sgl_batch_item *items, 
         float4 *wpos = (float4 *)(base + off);
         float4 *wnrm = wpos + s->n_vertices;
         off += up(2 * sizeof(float4) * std::max<size_t>(s->n_vertices, 1));
+        float4 *pbox = nullptr;
+        if (s->dev.pbox) {
+            pbox = (float4 *)(base + off);
+            off += up(2 * sizeof(float4) * s->dev.n_prims);
+        }
         const size_t nm = mats[i].size() / 2;
         // (from pageable memory: staged before the call returns)
         CUDA_TRY(cudaMemcpyAsync(m, mats[i].data(), sizeof(float) * mats[i].size(), cudaMemcpyHostToDevice,
                                  lane->stream));
-        CUDA_TRY(launch_pose(s->dev, m, m + nm, wpos, wnrm, lane->stream));
+        CUDA_TRY(launch_pose(s->dev, m, m + nm, wpos, wnrm, pbox, lane->stream));
         e[i].wpos = wpos;
         e[i].wnrm = wnrm;
+        e[i].pbox = pbox;
         e[i].node_world = m;
         e[i].node_rs = m + nm;
     }

@@ -86,6 +86,8 @@ struct SceneDev {
     int mixed;               // fused, and some primitive beyond the limits: the general passes run too
     const uint8_t *psmall;   // mixed: per draw-order primitive, 1 when the fused pass takes it
     const uint8_t *vsmall;   // mixed: per vertex, 1 when only primitives of the fused pass use it
+    float4 *pbox;            // fused: per draw-order primitive, the centre then the half extent of the box of its
+                             // world positions (k_box, after k_world); the fused pass's whole-primitive frustum test
     int n_mats;
     int n_texs;
     MatDesc default_mat;
@@ -98,6 +100,16 @@ struct ViewDev {
     float campos[3];
     float vm00, vm03, vm11, vm13; // viewport_t::m_viewportmatrix (viewport.cpp:94-99)
     int shader;                   // SGL_SHADER_* (include/sgl.h)
+    // Whole-primitive frustum test (make_view): for each of the regions
+    // x' < -z', x' > z', y' < -z', y' > z' and z' > 0 of the projected
+    // coordinates, a world-space plane a (negative in the region) and an
+    // error bound e (>= 0), as cull[r][0] = a and cull[r][1] = e.  Over a box
+    // with centre C and half extent H, a negative a.C + a3 + |a|.H +
+    // e.(|C| + H) + e3 puts every point of the box in the region by far more
+    // than the rounding of the vertex transform; a box in one of the first
+    // four regions and in the fifth holds no triangle that
+    // inside_camera_frustum accepts.
+    float4 cull[5][2];
 };
 
 // One view of a batch: its scene, camera and buffers.
@@ -286,10 +298,11 @@ void prof_flush(Profiler *p);
 // kernel launchers (raster.cu)
 cudaError_t launch_world(const SceneDev &s, cudaStream_t st);
 // The world positions and normals of a scene under other node matrices
-// (`node_world`, `node_rs`, device) into `wpos` / `wnrm` (a posed request);
-// the scene's own arrays are not touched.
+// (`node_world`, `node_rs`, device) into `wpos` / `wnrm` (a posed request),
+// and the boxes of its primitives into `pbox` (2 float4 per primitive, may
+// be null); the scene's own arrays are not touched.
 cudaError_t launch_pose(const SceneDev &s, const float *node_world, const float *node_rs, float4 *wpos, float4 *wnrm,
-                        cudaStream_t st);
+                        float4 *pbox, cudaStream_t st);
 // The launch sequence of a batch whose BatchDev lives at `b` (device memory).
 // `flags`: kSeqDof adds the depth-of-field gather, kSeqShaders shades with
 // every pixel shader (a view asks for another than the default).  The depth

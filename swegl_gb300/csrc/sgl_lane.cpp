@@ -241,6 +241,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         if (en.wpos) { // a posed request: its own world positions, normals and node matrices
             it.s.wpos = en.wpos;
             it.s.wnrm = en.wnrm;
+            it.s.pbox = en.pbox;
             it.s.node_world = en.node_world;
             it.s.node_rs = en.node_rs;
         }

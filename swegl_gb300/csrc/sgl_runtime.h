@@ -53,7 +53,7 @@ struct Ctx;
 // A scene resident in device memory.
 struct Scene {
     DevBuf d_pos_u, d_nrm_v, d_vnode, d_tris, d_prims, d_mats, d_texs, d_texels, d_wpos, d_wnrm, d_uv,
-        d_node_world, d_node_rs, d_lights, d_pgeo, d_pshade, d_psmall, d_vsmall;
+        d_node_world, d_node_rs, d_lights, d_pgeo, d_pshade, d_psmall, d_vsmall, d_pbox;
     SceneDev dev{};
     LightsDev lights{};
     std::vector<sgl_node_desc> nodes;
@@ -77,6 +77,7 @@ struct BatchEntry {
     uint32_t *surface = nullptr; // device, the whole surface (row 0, column 0): views with transparency layers
     float4 *wpos = nullptr;      // device: this view's own world positions and normals (a posed request)
     float4 *wnrm = nullptr;
+    float4 *pbox = nullptr;            // device: the boxes of its primitives under the pose (fused scenes)
     const float *node_world = nullptr; // device: this view's own node matrices (a posed request)
     const float *node_rs = nullptr;
 };

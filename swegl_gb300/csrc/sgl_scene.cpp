@@ -442,6 +442,10 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
         dev.psmall = (const uint8_t *)d_psmall.ptr;
         dev.vsmall = (const uint8_t *)d_vsmall.ptr;
     }
+    if (dev.fused) { // the primitives' boxes, written with the world positions
+        CUDA_TRY(d_pbox.ensure(2 * sizeof(float4) * pgeo.size()));
+        dev.pbox = (float4 *)d_pbox.ptr;
+    }
     dev.n_vertices = n_vertices;
     dev.n_triangles = n_triangles;
     dev.n_mats = d->n_materials;
@@ -457,7 +461,7 @@ sgl_status Scene::upload_desc(Ctx *ctx, const sgl_scene_desc *d)
     if (st != SGL_OK)
         return st;
     device_bytes = d_pos_u.bytes + d_nrm_v.bytes + d_vnode.bytes + d_tris.bytes + d_prims.bytes + d_mats.bytes +
-                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_uv.bytes + d_node_world.bytes + d_node_rs.bytes + d_lights.bytes + d_pgeo.bytes + d_pshade.bytes + d_psmall.bytes + d_vsmall.bytes;
+                   d_texs.bytes + d_texels.bytes + d_wpos.bytes + d_wnrm.bytes + d_uv.bytes + d_node_world.bytes + d_node_rs.bytes + d_lights.bytes + d_pgeo.bytes + d_pshade.bytes + d_psmall.bytes + d_vsmall.bytes + d_pbox.bytes;
     return SGL_OK;
 }
 

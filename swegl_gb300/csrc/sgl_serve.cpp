@@ -106,7 +106,8 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
     }
     // posed requests: their node matrices and world arrays, then k_pose
     auto pose_span = [](const Job &j) {
-        return (sizeof(float) * j.pose.size() + 16 + 32 * (size_t)j.scene->n_vertices + 255) & ~(size_t)255;
+        return (sizeof(float) * j.pose.size() + 16 + 32 * (size_t)j.scene->n_vertices +
+                (j.scene->dev.pbox ? 32 * (size_t)j.scene->dev.n_prims : 0) + 255) & ~(size_t)255;
     };
     size_t pose_bytes = 0;
     for (auto &j : jobs)
@@ -137,15 +138,17 @@ void Server::launch_batch_on(LaneState &ls, std::vector<Job> &&jobs)
             const size_t nm = j.pose.size() / 2;
             float4 *wpos = (float4 *)(base + ((sizeof(float) * j.pose.size() + 15) & ~(size_t)15));
             float4 *wnrm = wpos + j.scene->n_vertices;
+            float4 *pbox = j.scene->dev.pbox ? wnrm + j.scene->n_vertices : nullptr; // (2 per primitive)
             pose_off += pose_span(j);
             if (cudaMemcpyAsync(mats, j.pose.data(), sizeof(float) * j.pose.size(), cudaMemcpyHostToDevice,
                                 ls.lane->stream) != cudaSuccess ||
-                launch_pose(j.scene->dev, mats, mats + nm, wpos, wnrm, ls.lane->stream) != cudaSuccess) {
+                launch_pose(j.scene->dev, mats, mats + nm, wpos, wnrm, pbox, ls.lane->stream) != cudaSuccess) {
                 c->fail("serving: pose of request %llu failed", (unsigned long long)j.ticket);
                 st = SGL_ERR_CUDA;
             }
             entries.back().wpos = wpos;
             entries.back().wnrm = wnrm;
+            entries.back().pbox = pbox;
             entries.back().node_world = mats;
             entries.back().node_rs = mats + nm;
         }

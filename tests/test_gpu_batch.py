@@ -298,6 +298,47 @@ def test_posed_items_equal_the_scene_set_to_each_pose(rig, make):
     r.release(check)
 
 
+def test_poses_that_bring_culled_primitives_into_view(rig):
+    """The fused geometry pass skips a primitive for a view when the box of
+    its world positions lies beyond one of the view's side planes; a posed
+    item must use the boxes of its own pose.  The scene's own nodes put every
+    sphere far to the side of the cameras (each primitive out of view), the
+    poses put them back in view: each posed item matches the oracle's render
+    of the scene under that pose (depth bit-exact, colour within 2 LSB,
+    drawn triangles equal), and the items without a pose draw nothing."""
+    r, torch = rig
+    posed = S.spheres_scene(n_spheres=40, tex_size=64)
+    away = copy.deepcopy(posed)
+    n = len(posed.node_parent)
+    for i in range(n):
+        away.node_translation[i] = np.asarray(posed.node_translation[i], np.float32) + np.float32([400.0, 0.0, 0.0])
+    sid = r.upload(away)
+    views = []
+    for k, (pos, w, h) in enumerate([((0.0, 0.0, 35.0), 320, 180), ((30.0, 5.0, 20.0), 96, 240),
+                                     ((-10.0, 25.0, 20.0), 256, 64), ((0.0, 0.0, 35.0), 200, 200)]):
+        m, c = S.look_at(pos, (0.0, 0.0, 0.0))
+        views.append(S.view_for(w, h, m, c))
+    pose = abi.SceneDescHolder(posed).nodes
+    plan = [pose, None, pose, pose]
+    bufs, tgts = device_targets(torch, views)
+    st = r.render_batch([(sid, v, t, p) for v, t, p in zip(views, tgts, plan)], stats=True)
+    torch.cuda.synchronize()
+    got = frames_of(bufs)
+    drawn = 0
+    for i, (v, p) in enumerate(zip(views, plan)):
+        ref = oracle.render(posed if p is not None else away, [v])
+        assert np.array_equal(got[i][1].view(np.uint32), ref.zbuffer.view(np.uint32)), f"item {i}: depth"
+        d = np.abs(got[i][0].view(np.uint8).astype(np.int16) - ref.pixels.view(np.uint8).astype(np.int16))
+        assert int(d.max()) <= 2, f"item {i}: colour"
+        drawn += ref.stats[0][0]
+        if p is None:
+            assert ref.stats[0][0] == 0
+        else:
+            assert ref.stats[0][0] > 0
+    assert st["drawn_triangles"] == drawn
+    r.release(sid)
+
+
 def test_winner_list_shade_equals_tiled_shade(rig):
     """A batch of one view of a million pixels or more shades through a winner
     list (k_classify, then k_shade_wins); other batches shade in tiles
