@@ -696,10 +696,12 @@ def run_serve(args, rank, world, local_rank):
     batched_same_fps = n_seq / (e0.elapsed_time(e1) / 1e3)
 
     srv.close()
-    # e2e: closed loop with every frame copied to pinned host memory.  It runs
-    # before the open-loop latency leg: after that leg's minute of deliveries
-    # into a pinned ring, copy-out throughput on the same box measured lower
-    # for later allocations, in this process and in later ones
+    # e2e: closed loop with every frame copied to page-locked host memory.
+    # The frames go to write-combined memory: copies into ordinary page-locked
+    # memory slowed down the longer the host had been running (29.8 k frames/s
+    # on a fresh host, 19.9-27.0 k a minute later, with the device-only rate
+    # and the raw copy rate unchanged), into write-combined memory they did not
+    # (27.6-28.1 k in both states)
     e2e = e2e_run(r, torch, sids, timed, args)
 
     # open-loop latency at the Poisson arrival times, frames delivered to the host
@@ -724,6 +726,7 @@ def run_serve(args, rank, world, local_rank):
         "roofline": roofline_of(fm),
         "e2e": {"value": round(e2e["fps"], 2), "unit": "frames/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"], "step": "%d requests submitted together" % args.e2e_chunk,
+                "host_frames": "write-combined page-locked memory (sgl_host_alloc)",
                 "chunks": e2e["chunks"], "requests": e2e["requests"], "seconds": round(e2e["seconds"], 2)},
         "gpu_launches": gpu_launches,
         "clocks": clocks.summary(),
@@ -794,11 +797,13 @@ def _pct(a: np.ndarray) -> dict:
 
 class PinnedRing:
     """Host frame buffers for the requests in flight, carved in order from one
-    pinned pool; a region is reused once the requests holding it are done
-    (their results are collected then)."""
+    pinned pool (write-combined, sgl_host_alloc); a region is reused once the
+    requests holding it are done (their results are collected then)."""
 
     def __init__(self, torch, srv, nbytes: int):
-        self.pool = torch.empty(nbytes // 4, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+        from swegl_gb300.runtime import host_buffer
+
+        self.pool = host_buffer(nbytes // 4)
         self.n = self.pool.size
         self.srv = srv
         self.head = 0
@@ -871,20 +876,21 @@ def latency_run(r, torch, sids, duration: float, seed: int, args) -> dict:
 
 def e2e_run(r, torch, sids, timed, args):
     """Closed loop through the public API with every frame (colour + depth)
-    copied to pinned host memory: chunks of args.e2e_chunk requests of the
-    stream, each chunk's frames into one half of a pinned pool (chunk k + 2
+    copied to page-locked host memory: chunks of args.e2e_chunk requests of the
+    stream, each chunk's frames into one half of a write-combined page-locked
+    pool from sgl_host_alloc (chunk k + 2
     reuses chunk k's half once chunk k is delivered, so the GPU is never left
     idle between chunks); chunks are taken from the stream's timed requests in
     turn until at least args.e2e_seconds have passed (and at least 8 chunks).
     A chunk is queued with one sgl_server_submit_batch call and collected with
     one sgl_server_wait_batch call; its request descriptors (view, camera,
     host buffer pointers) are packed before the timed region."""
-    from swegl_gb300.runtime import Server
+    from swegl_gb300.runtime import Server, host_buffer
 
     M = args.e2e_chunk
     chunks = [timed[i:i + M] for i in range(0, len(timed) - M + 1, M)][:32] or [timed[:M]]
     half = max(sum(2 * v.w * v.h for (_, _, v) in ch) for ch in chunks) + 16
-    pool = torch.empty(2 * half, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    pool = host_buffer(2 * half)  # write-combined page-locked memory (sgl_host_alloc)
     srv = r.server(budget_bytes=args.budget, max_batch=args.max_batch, streams=args.streams, copy_out=True)
 
     def pack(ch, h):

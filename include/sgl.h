@@ -371,6 +371,16 @@ SGL_API sgl_status sgl_server_drain(sgl_server *srv, double timeout_s);
 SGL_API sgl_status sgl_server_stats(sgl_server *srv, uint64_t *batches, uint64_t *kernels, uint64_t *completed);
 SGL_API void       sgl_server_destroy(sgl_server *srv);
 
+/* Page-locked host memory for request frames (cudaHostAlloc on the current
+ * device; `write_combined` adds cudaHostAllocWriteCombined).  Frames copied
+ * into write-combined memory kept their delivery rate on GB300 hosts where
+ * copies into ordinary page-locked memory slowed down the longer the host ran
+ * (27.6-28.1 k against 19.9-29.8 k frames/s end to end); CPU reads of it
+ * measured the same as of ordinary memory there.  Free with sgl_host_free.
+ * No reference counterpart (the reference renders into host surfaces). */
+SGL_API sgl_status sgl_host_alloc(size_t bytes, int write_combined, void **out);
+SGL_API sgl_status sgl_host_free(void *p);
+
 /* Device-side bounds checks.  The library built with them (libsgl_check.so,
  * compiled with -DSGL_BOUNDS_CHECK beside libsgl.so) tests the index of each
  * guarded device access — projected vertices, set-up records, depth keys,

@@ -190,6 +190,31 @@ extern "C" {
 
 SGL_API int sgl_version(void) { return 2; }
 
+SGL_API sgl_status sgl_host_alloc(size_t bytes, int write_combined, void **out)
+{
+    if (!out)
+        return SGL_ERR_INVALID;
+    *out = nullptr;
+    if (bytes == 0)
+        return SGL_ERR_INVALID;
+    const unsigned flags = cudaHostAllocPortable | (write_combined ? cudaHostAllocWriteCombined : 0u);
+    if (cudaHostAlloc(out, bytes, flags) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return SGL_ERR_OOM;
+    }
+    return SGL_OK;
+}
+
+SGL_API sgl_status sgl_host_free(void *p)
+{
+    if (p && cudaFreeHost(p) != cudaSuccess) {
+        cudaGetLastError();
+        return SGL_ERR_CUDA;
+    }
+    return SGL_OK;
+}
+
 SGL_API const char *sgl_status_string(sgl_status s)
 {
     switch (s) {

@@ -82,6 +82,8 @@ def library(checked: bool = False) -> C.CDLL:
             "sgl_image_load": ([C.c_char_p, P(P(C.c_uint32)), P(C.c_int), P(C.c_int), C.c_char_p, C.c_size_t],
                                C.c_int),
             "sgl_image_free": ([P(C.c_uint32)], None),
+            "sgl_host_alloc": ([C.c_size_t, C.c_int, P(C.c_void_p)], C.c_int),
+            "sgl_host_free": ([C.c_void_p], C.c_int),
         }
         for name, (args, res) in sigs.items():
             fn = getattr(lib, name)
@@ -89,6 +91,22 @@ def library(checked: bool = False) -> C.CDLL:
             fn.restype = res
         _libs[path] = lib
     return _libs[path]
+
+
+def host_buffer(n_words: int, write_combined: bool = True, checked: bool = False) -> np.ndarray:
+    """Page-locked host memory from sgl_host_alloc as a uint32 array (for
+    request frames; write-combined by default), freed when the array and
+    every view of it are gone."""
+    import weakref
+
+    lib = library(checked)
+    p = C.c_void_p()
+    st = lib.sgl_host_alloc(4 * int(n_words), 1 if write_combined else 0, C.byref(p))
+    if st != 0:
+        raise SglError(st, f"sgl_host_alloc of {4 * int(n_words)} bytes failed")
+    buf = (C.c_uint32 * int(n_words)).from_address(p.value)
+    weakref.finalize(buf, lib.sgl_host_free, p.value)
+    return np.frombuffer(buf, dtype=np.uint32)
 
 
 class Renderer:

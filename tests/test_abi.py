@@ -46,6 +46,18 @@ def test_no_device_is_reported_not_crashed(lib):
     assert lib.sgl_status_string(-7) == b"no CUDA device"
 
 
+def test_host_alloc_refuses_bad_arguments(lib):
+    """sgl_host_alloc checks its arguments before any CUDA call: zero bytes or
+    no output pointer is SGL_ERR_INVALID; freeing NULL is a no-op."""
+    lib.sgl_host_alloc.argtypes = [C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]
+    lib.sgl_host_free.argtypes = [C.c_void_p]
+    p = C.c_void_p(1)
+    assert lib.sgl_host_alloc(0, 1, C.byref(p)) == -1
+    assert p.value is None
+    assert lib.sgl_host_alloc(64, 0, None) == -1
+    assert lib.sgl_host_free(None) == 0
+
+
 STRUCTS = {
     "sgl_node_desc": abi.NodeDesc, "sgl_primitive_desc": abi.PrimitiveDesc, "sgl_material_desc": abi.MaterialDesc,
     "sgl_texture_desc": abi.TextureDesc, "sgl_point_light": abi.PointLight, "sgl_scene_desc": abi.SceneDesc,

@@ -229,10 +229,14 @@ def test_serving_budget_and_poll(renderer):
     renderer.release(sid)
 
 
-def test_serving_copy_out_into_one_pool(renderer):
+@pytest.mark.parametrize("pool_kind", ["pageable", "write_combined", "page_locked"])
+def test_serving_copy_out_into_one_pool(renderer, pool_kind):
     """Host buffers carved from one pool in framebuffer order (colour, depth,
     next request): the loop merges the copies of a batch into one; every
-    request still receives exactly its own frame."""
+    request still receives exactly its own frame — into pageable memory and
+    into page-locked memory from sgl_host_alloc, write-combined or not."""
+    from swegl_gb300.runtime import host_buffer
+
     scenes = [S.spheres_scene(n_spheres=k, seed=60 + k, tex_size=128) for k in (4, 9)]
     sids = [renderer.upload(sc) for sc in scenes]
     rng = S.Rng(91)
@@ -242,7 +246,12 @@ def test_serving_copy_out_into_one_pool(renderer):
         h = S.log_uniform_int(rng, 64, 300)
         m, c = S.camera_on_sphere(rng, 35.0)
         reqs.append((i % 2, S.view_for(w, h, m, c)))
-    pool = np.zeros(sum(2 * v.w * v.h for (_, v) in reqs), np.uint32)
+    words = sum(2 * v.w * v.h for (_, v) in reqs)
+    if pool_kind == "pageable":
+        pool = np.zeros(words, np.uint32)
+    else:
+        pool = host_buffer(words, write_combined=pool_kind == "write_combined")
+        pool[:] = 0
     srv = renderer.server(budget_bytes=256 << 20, max_batch=8, streams=2, copy_out=True)
     outs, tickets, off = [], [], 0
     for k, v in reqs:
