@@ -32,6 +32,7 @@
 // new key pools are filled once and the shade kernel empties what it reads.
 #include <cstdint>
 
+#include "sgl_cull.h"
 #include "sgl_device.cuh"
 #include "sgl_dof_taps.h"
 #include "sgl_internal.h"
@@ -158,12 +159,10 @@ __global__ void k_box(SceneDev s, const float4 *wpos, float4 *pbox)
         hi.z = fmaxf(hi.z, __shfl_xor_sync(0xFFFFFFFFu, hi.z, o));
     }
     if (lane == 0) {
-        V3 c = mk3(0.5f * lo.x + 0.5f * hi.x, 0.5f * lo.y + 0.5f * hi.y, 0.5f * lo.z + 0.5f * hi.z);
-        const V3 h = mk3(0.5f * hi.x - 0.5f * lo.x, 0.5f * hi.y - 0.5f * lo.y, 0.5f * hi.z - 0.5f * lo.z);
-        if (!(fabsf(c.x) + h.x + fabsf(c.y) + h.y + fabsf(c.z) + h.z < 0x1p100f))
-            c.x = __int_as_float(0x7FC00000); // empty or not finite
-        pbox[2 * q] = make_float4(c.x, c.y, c.z, 0.0f);
-        pbox[2 * q + 1] = make_float4(h.x, h.y, h.z, 0.0f);
+        float4 c, h;
+        cull_box(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z), c, h);
+        pbox[2 * q] = c;
+        pbox[2 * q + 1] = h;
     }
 }
 
@@ -586,15 +585,6 @@ __device__ __forceinline__ uint32_t geom_tri(const uint4 *tris, uint4 gq, uint32
     const uint4 tri = tris[gq.z + t];
     in_bounds(tri.x - gq.x < gq.y && tri.y - gq.x < gq.y && tri.z - gq.x < gq.y, CHK_LOCAL, gq.z + t);
     return (tri.x - gq.x) | ((tri.y - gq.x) << 8) | ((tri.z - gq.x) << 16);
-}
-
-// Box (centre bc, half extent bh, ba = |bc| + bh) against region r of
-// ViewDev::cull: negative when the whole box is in the region.
-__device__ __forceinline__ float cull_region(const float4 *r, float4 bc, float4 bh, float4 ba)
-{
-    const float4 a = r[0], e = r[1];
-    return (a.x * bc.x + a.y * bc.y + a.z * bc.z + a.w) + (fabsf(a.x) * bh.x + fabsf(a.y) * bh.y + fabsf(a.z) * bh.z) +
-           (e.x * ba.x + e.y * ba.y + e.z * ba.z + e.w);
 }
 
 // Bit i (i < n <= 8) set when item grp_items[v0 + i] sees none of the

@@ -10,42 +10,11 @@
 #include <cuda_runtime.h>
 
 #include "sgl.h"
+#include "sgl_cull.h"
 #include "sgl_internal.h"
 #include "sgl_runtime.h"
 
 namespace sgl {
-
-// The planes of ViewDev::cull.  The vertex transform computes x' (and y', z')
-// as projection row . (view rows . (w, 1), 1) in float, with an error below
-// 16 ulp of E(|w|) = |P| . (|V| . |w| + |Vt|) + |Pt| for its row; the bound
-// taken is 2^-16 E, so a box that passes the test keeps every vertex at
-// least 2^-17 E from the plane (x'/|z'| then rounds strictly past +-1).
-static void cull_planes(const sgl_view &v, float4 cull[5][2])
-{
-    double M[3][4], E[3][4];
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 4; c++) {
-            double m = c == 3 ? (double)v.proj[4 * r + 3] : 0.0, e = c == 3 ? std::fabs((double)v.proj[4 * r + 3]) : 0.0;
-            for (int k = 0; k < 3; k++) {
-                m += (double)v.proj[4 * r + k] * (double)v.view[4 * k + c];
-                e += std::fabs((double)v.proj[4 * r + k]) * std::fabs((double)v.view[4 * k + c]);
-            }
-            M[r][c] = m;
-            E[r][c] = e;
-        }
-    // a . (w, 1) < 0 where x' < -z', x' > z', y' < -z', y' > z'; and where z' > 0
-    const double sx[5] = {1.0, -1.0, 0.0, 0.0, 0.0}, sy[5] = {0.0, 0.0, 1.0, -1.0, 0.0};
-    const double sz[5] = {1.0, 1.0, 1.0, 1.0, -1.0};
-    for (int p = 0; p < 5; p++) {
-        float a[4], e[4];
-        for (int c = 0; c < 4; c++) {
-            a[c] = (float)(sx[p] * M[0][c] + sy[p] * M[1][c] + sz[p] * M[2][c]);
-            e[c] = (float)(0x1p-16 * (std::fabs(sx[p]) * E[0][c] + std::fabs(sy[p]) * E[1][c] + E[2][c]));
-        }
-        cull[p][0] = make_float4(a[0], a[1], a[2], a[3]);
-        cull[p][1] = make_float4(e[0], e[1], e[2], e[3]);
-    }
-}
 
 ViewDev make_view(const sgl_view &v)
 {

@@ -114,7 +114,7 @@ __host__ __device__ __forceinline__ bool cross_z_negative(V3 a, V3 b)
 }
 
 // transform(vertex, m): rows 0-2 only (src/projection/points.cpp:8-13)
-__device__ __forceinline__ V3 transform3(V3 v, const float *m)
+__host__ __device__ __forceinline__ V3 transform3(V3 v, const float *m)
 {
     return mk3(m[0] * v.x + m[1] * v.y + m[2] * v.z + m[3], m[4] * v.x + m[5] * v.y + m[6] * v.z + m[7],
                m[8] * v.x + m[9] * v.y + m[10] * v.z + m[11]);

@@ -16,7 +16,15 @@ seeded inputs:
   tests, which decide the sign of the normalised cross product's z without
   its square root and division where that is provably the same, against the
   reference's normalised expression (src/projection/points.cpp:32-37), on
-  ordinary, tiny, huge, subnormal, infinite and NaN edge vectors."""
+  ordinary, tiny, huge, subnormal, infinite and NaN edge vectors.
+* The fused geometry pass's whole-primitive frustum test (sgl_cull.h):
+  wherever it skips a primitive's box for a view, every vertex in the box,
+  transformed as the pass transforms it, is in front of the camera and
+  beyond the side the test found (inside_camera_frustum,
+  src/render/renderer.cpp:58-70, rejects every triangle there); boxes are
+  placed across and within 1e-6 of each side.  The same check with the
+  test's rounding margin set to zero finds thousands of violations, so the
+  placement reaches the margin."""
 import os
 import shutil
 import subprocess
@@ -41,7 +49,7 @@ def _build(tmp, name):
 @pytest.fixture(scope="module")
 def exes(tmp_path_factory):
     tmp = tmp_path_factory.mktemp("shade_math")
-    return {n: _build(tmp, n) for n in ("spec_pow_host", "light_sum_host", "cross_sign_host")}
+    return {n: _build(tmp, n) for n in ("spec_pow_host", "light_sum_host", "cross_sign_host", "cull_host")}
 
 
 @pytest.mark.parametrize("pmax, allowed", [(128, 2e-6), (1024, 1e-5)])
@@ -65,3 +73,11 @@ def test_cross_sign_matches_normalised_cross(exes):
     r = subprocess.run([exes["cross_sign_host"], "2000000"], capture_output=True, text=True, check=True)
     cases, diff = map(int, r.stdout.split())
     assert cases == 2000000 and diff == 0, f"{diff} of {cases} sign tests differ from the normalised cross product"
+
+
+def test_primitive_frustum_test_skips_only_unseen_boxes(exes):
+    r = subprocess.run([exes["cull_host"], "300000"], capture_output=True, text=True, check=True)
+    boxes, skipped, vertices, bad = map(int, r.stdout.split())
+    assert boxes == 300000
+    assert skipped > boxes // 10 and vertices == 40 * skipped
+    assert bad == 0, f"{bad} of {vertices} vertices of skipped boxes are not beyond the side the test found"
