@@ -305,7 +305,7 @@ SGL_API sgl_status sgl_render_noalloc(sgl_ctx *c, int scene_id, const sgl_view *
     CUDA_TRY(cudaMemsetAsync(base + o_key, 0xFF, 8 * px, st)); // kEmptyKey
 
     const int seq = (dof ? kSeqDof : 0) | (v.shader != SGL_SHADER_PHONG_BILINEAR ? kSeqShaders : 0) |
-                    (fused ? kSeqFused : 0) | (split ? kSeqSplit : 0) | (win_list ? kSeqWinList : 0);
+                    (fused ? kSeqFused : 0) | (split ? kSeqSplit : 0) | (win_list ? kSeqWinList : 0) | kSeqOne;
     CUDA_TRY(launch_batch((const BatchDev *)(base + o_batch), tile, seq, st, nullptr, nullptr));
     return SGL_OK;
 }

@@ -1548,7 +1548,7 @@ __device__ __noinline__ void walk_tall_all(const BatchDev *b, ItemAcc &acc);
 // set-ups into shared memory (one 128-byte record per load) and deals their
 // rows across its lanes.  FRAGS: the fragment capture of a layered view (the
 // near-clipped triangles are captured by k_frags).
-template <bool FRAGS>
+template <bool FRAGS, bool STRIDED>
 __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(const BatchDev *b)
 {
     __shared__ WalkRow sm[kWalkWarps][2][kWalkFields];
@@ -1556,19 +1556,17 @@ __global__ void __launch_bounds__(kWalkWarps * 32, SGL_WALK_MIN_BLOCKS) k_walk(c
     const uint32_t n_raw = *counter32(b, C_LIST);
     const uint32_t n = n_raw < b->list_cap ? n_raw : b->list_cap;
     const uint32_t n_groups = (n + 31) / 32;
-    // Group g holds entries g + j * n_groups (j < 32) in a batch of one view:
-    // every group then samples the whole list, so the large triangles of
-    // nearby primitives, which sit together in list order, spread over all
-    // groups and warps (1080p frame: 41.7 -> 30.3 us).  In a batch of several
-    // views a strided group would mix the views' triangles, whose view
-    // parameters each row then reloads (serving: 5.5 -> 12.3 us per request),
-    // so there group g holds entries 32 g + j.
-    const bool strided = b->n_items == 1;
-    const uint32_t gstep = strided ? n_groups : 1u;
-    auto entry = [&](uint32_t g, uint32_t j) -> uint32_t { return strided ? g + j * gstep : 32 * g + j; };
+    // STRIDED (a batch of one view, kSeqOne): group g holds entries
+    // g + j * n_groups (j < 32), so every group samples the whole list and the
+    // large triangles of nearby primitives, which sit together in list order,
+    // spread over all groups and warps (1080p frame: 41.7 -> 30.3 us).  In a
+    // batch of several views a strided group would mix the views' triangles,
+    // whose view parameters each row then reloads (serving: 5.5 -> 12.3 us
+    // per request), so there group g holds entries 32 g + j.
+    auto entry = [&](uint32_t g, uint32_t j) -> uint32_t { return STRIDED ? g + j * n_groups : 32 * g + j; };
     auto count = [&](uint32_t g) -> uint32_t {
-        if (strided)
-            return min(32u, (n - g + gstep - 1) / gstep);
+        if (STRIDED)
+            return min(32u, (n - g + n_groups - 1) / n_groups);
         return n - 32 * g < 32u ? n - 32 * g : 32u;
     };
     // the record (batch triangle) of entry `lane` of group g; loaded one
@@ -2626,7 +2624,7 @@ struct FragVisitor {
 };
 
 // Fragment capture of the near-clipped triangles (the walk list is captured
-// by k_walk<true>): one thread per triangle runs fill_triangle's clip cases
+// by k_walk<true, true>): one thread per triangle runs fill_triangle's clip cases
 // and the fill_triangle_2 walk.  Each lane first counts its triangle's
 // fragments; the warp then reserves its lanes' ranges with one atomic and
 // walks again to store them.
@@ -3093,7 +3091,7 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
         for (int k = PK_WALK; k <= PK_DOF; k++)
             mark(k);
         mark(PK_FRAGS);
-        k_walk<true><<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
+        k_walk<true, true><<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b); // (one view)
         k_frags<<<sms * 2, 256, 0, st>>>(b);
         k_frag_spans<<<sms * 4, 256, 0, st>>>(b);
         k_link<<<sms * 8, 256, 0, st>>>(b);
@@ -3125,7 +3123,10 @@ cudaError_t launch_batch(const BatchDev *b, int tile, int flags, cudaStream_t st
         return cudaGetLastError();
     }
     mark(PK_WALK);
-    k_walk<false><<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
+    if (flags & kSeqOne)
+        k_walk<false, true><<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
+    else
+        k_walk<false, false><<<sms * SGL_WALK_MIN_BLOCKS, kWalkWarps * 32, 0, st>>>(b);
     ran(PK_WALK);
     n++;
     mark(PK_SPANS);

@@ -316,9 +316,10 @@ cudaError_t launch_pose(const SceneDev &s, const float *node_world, const float 
 // kSeqFused: items of fused scenes (k_geom); kSeqSplit: other items (k_vertex,
 // k_flags, k_compact).  kSeqWinList shades through a winner list (k_classify
 // then k_shade_wins, for a batch of one large view) instead of the tiled
-// k_shade; BatchDev::wins must then hold total_px entries.
+// k_shade; BatchDev::wins must then hold total_px entries.  kSeqOne: the
+// batch has one view (the walk deals its list entries strided over groups).
 constexpr int kSeqDof = 1, kSeqShaders = 2, kSeqLayers = 4, kSeqFused = 8, kSeqSplit = 16, kSeqWinList = 32,
-              kSeqVariants = 64;
+              kSeqOne = 64, kSeqVariants = 128;
 // A batch of one view of at least this many pixels shades through the winner
 // list: the tiled shade's per-tile key reads and barriers then cost more than
 // the list's second kernel and its round trip through L2.

@@ -213,7 +213,7 @@ sgl_status Lane::prepare(Ctx *ctx, const BatchEntry *e, int n, int tile, int inl
         if (dofz_px)
             CUDA_TRY(dofz.ensure(4 * dofz_px));
     }
-    int seq_flags = geom_flags | (win_list ? kSeqWinList : 0);
+    int seq_flags = geom_flags | (win_list ? kSeqWinList : 0) | (n == 1 ? kSeqOne : 0);
     int layers = 0;
     for (int i = 0; i < n; i++)
         layers = std::max(layers, e[i].view.layers);
