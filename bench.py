@@ -16,12 +16,13 @@ continuous-batching loop under a 40 GB budget.
             one-frame-per-launch renderer, one call after another.
   latency   p50/p99/p999 with the requests submitted at their Poisson
             arrival times (open loop) for --duration seconds (60 by
-            default), every frame copied to pinned host memory: delivered
+            default), every frame copied to write-combined page-locked host
+            memory (sgl_host_alloc): delivered
             (frame in the caller's buffers) and rendered (frame complete in
             device memory) latencies of the same run.
   e2e       closed loop through the public API, every frame (colour + depth)
-            copied to pinned host memory, in pipelined chunks of 256
-            requests for at least 2 s.
+            copied to write-combined page-locked host memory, in pipelined
+            chunks of 256 requests for at least 2 s.
 Request descriptors are packed before the timed regions (the application's
 own work); a step queues them with one sgl_server_submit_batch call.
   roofline  the plain renderer's 1080p frame of the 200-sphere scene
